@@ -1,0 +1,80 @@
+"""The C restatement (oracle/vjo.c) reproduces the reference's own outputs bit for bit.
+
+The fixtures in tests/golden/ were produced by VecJac compiled from its sources
+(tests/golden/make_golden.py); this pins the oracle that the GPU tests rely on.
+"""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+@pytest.fixture(scope="module")
+def rst():
+    O.build()
+    return O.Restatement()
+
+
+def same_bits(a, b):
+    a = np.ascontiguousarray(a)
+    b = np.ascontiguousarray(b)
+    return a.shape == b.shape and np.array_equal(a.view(np.uint8), b.view(np.uint8))
+
+
+@pytest.mark.parametrize("kind", list("dszc"))
+@pytest.mark.parametrize("tag,sgn,internal", [("sin", -1, False), ("tan", 1, False), ("isec", -1, True),
+                                              ("itan", 1, True)])
+def test_bjac2_golden(rst, kind, tag, sgn, internal):
+    g = np.load(os.path.join(GOLD, f"bjac2_{kind}.npz"))
+    ins = [g["a11"], g["a22"], g["a21"]] + ([g["a21i"]] if kind in "zc" else [])
+    n = ins[0].size
+    r = rst.bjac2(kind, sgn * n, *ins, internal=internal, p=(g["p_in"].copy() if internal else None))
+    assert r[0] >= 0
+    names = ["c", "at", "sat", "l1", "l2", "p"] if kind in "zc" else ["c", "at", "l1", "l2", "p"]
+    for name, arr in zip(names, r[1:]):
+        assert same_bits(arr, g[f"{tag}_{name}"]), (kind, tag, name)
+
+
+SVD_FILES = sorted(glob.glob(os.path.join(GOLD, "svd_*.npz")))
+
+
+@pytest.mark.parametrize("path", SVD_FILES, ids=[os.path.basename(p)[4:-4] for p in SVD_FILES])
+def test_svd_golden(rst, path):
+    g = np.load(path)
+    kind = os.path.basename(path)[4]
+    kw = dict(js=g["js"], stp=int(g["stp"]), swp=int(g["swp"]), V=(g["V0"] if "V0" in g else None))
+    if kind in "zc":
+        kw.update(Gi=g["Gi"], Vi=(g["Vi0"] if "Vi0" in g else None))
+    r = rst.vjsvd(kind, g["G"], **kw)
+    assert r[0] == int(g["ret"])
+    for i, name in enumerate(["U", "V", "eS", "fS"] + (["Ui", "Vi"] if kind in "zc" else [])):
+        assert same_bits(r[1 + i], g[name]), name
+
+
+def test_pjs_placeholder_contract(rst):
+    """Each row is a permutation of 0..n-1 read as pairs with p < q; a sweep covers every pair."""
+    for sid, n in ((2, 16), (4, 16), (2, 64), (4, 32)):
+        t, stp = rst.pjs(sid, n)
+        assert stp == (n - 1 if sid == 2 else n)
+        seen = set()
+        for row in t:
+            assert sorted(row) == list(range(n))
+            for k in range(0, n, 2):
+                p, q = int(row[k]), int(row[k + 1])
+                assert p < q
+                seen.add((p, q))
+        assert len(seen) == n * (n - 1) // 2
+
+
+def test_nrm2_properties(rst):
+    rng = np.random.default_rng(0)
+    x = rng.standard_normal(1000)
+    assert abs(rst.nrm2(x) - np.linalg.norm(x)) <= 4e-16 * 1000 * np.linalg.norm(x)
+    assert rst.nrm2(x * 2.0 ** 900) == rst.nrm2(x) * 2.0 ** 900
+    assert rst.nrm2(x * 2.0 ** -1000) > 0
+    assert rst.nrm2(np.zeros(7)) == 0.0
