@@ -1,0 +1,145 @@
+/* vecjac_gb300 -- GB300 (sm_103a) one-sided Jacobi SVD and batched 2x2 Hermitian EVD.
+ *
+ * C ABI of libvecjac_gb300.so. The entry points without a prefix are drop-in
+ * replacements for VecJac's C entry points (same names, Fortran-style by-pointer
+ * scalars, ILP64 integers as under MKL_ILP64, split real/imaginary planes for complex
+ * data, caller-owned buffers, same error codes); they take HOST pointers, copy to the
+ * GPU, compute there and copy back, synchronously. The vj_*_dev entry points take
+ * DEVICE pointers and a CUDA stream (passed as void*) and are asynchronous.
+ *
+ * There is no CPU fallback: without a usable GPU every entry point returns
+ * VJ_ERR_NO_GPU (or the CUDA error mapped to VJ_ERR_CUDA).
+ */
+#ifndef VECJAC_GB300_H
+#define VECJAC_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef long long vj_fint;           /* fint under MKL_ILP64 (src/common.h:180-183) */
+typedef unsigned long long vj_fnat;  /* fnat under MKL_ILP64 */
+
+/* library-specific failures; never produced by the reference */
+#define VJ_ERR_NO_GPU   (-100001LL)
+#define VJ_ERR_CUDA     (-100002LL)
+#define VJ_ERR_NOMEM    (-100003LL)
+#define VJ_ERR_ARG      (-100004LL)
+
+/* ---------------- batched 2x2 Hermitian EVD ----------------
+ * n < 0: cosines and sines; n > 0: cosines and tangents. For each i < |n|:
+ *   [c  -s'] [a11  a21'] [ c  s]  = diag(l1, l2) with s = at (real) or cat + i*sat (complex)
+ * p[i/8] (FP64) or p[i/16] (FP32) bit (i%8 or i%16) = (L1 < L2) of the scaled eigenvalues.
+ * |n| must be a multiple of 8 (d, z) or 16 (s, c); returns 1 on success (like the
+ * reference's OpenMP build), -1 if |n| is not such a multiple.
+ *   replaces dbjac2_  src/dbjac2.h:6,  src/dbjac2.c:81
+ *            zbjac2_  src/zbjac2.h:6,  src/zbjac2.c:108
+ *            sbjac2_  src/sbjac2.h:6,  src/sbjac2.c:81
+ *            cbjac2_  src/cbjac2.h:6,  src/cbjac2.c:108 */
+vj_fint dbjac2_(const vj_fint n[1], const double a11[], const double a22[], const double a21[],
+                double c[], double at[], double l1[], double l2[], unsigned p[]);
+vj_fint zbjac2_(const vj_fint n[1], const double a11[], const double a22[], const double a21r[], const double a21i[],
+                double c[], double cat[], double sat[], double l1[], double l2[], unsigned p[]);
+vj_fint sbjac2_(const vj_fint n[1], const float a11[], const float a22[], const float a21[],
+                float c[], float at[], float l1[], float l2[], unsigned p[]);
+vj_fint cbjac2_(const vj_fint n[1], const float a11[], const float a22[], const float a21r[], const float a21i[],
+                float c[], float cat[], float sat[], float l1[], float l2[], unsigned p[]);
+
+/* The internal masked variants (src/dbjac2.c:178 dbjac2i, src/zbjac2.c:222 zbjac2i,
+ * src/sbjac2.c sbjac2i, src/cbjac2.c cbjac2i): only the groups whose low 8 (d, z) or
+ * 16 (s, c) bits of p are nonzero are computed; those bits are replaced by the
+ * permutation bits and the high bits are kept. n < 0 stores secants in c. */
+vj_fint dbjac2i(const vj_fint n[1], const double a11[], const double a22[], const double a21[],
+                double c[], double at[], double l1[], double l2[], unsigned p[]);
+vj_fint zbjac2i(const vj_fint n[1], const double a11[], const double a22[], const double a21r[], const double a21i[],
+                double c[], double cat[], double sat[], double l1[], double l2[], unsigned p[]);
+vj_fint sbjac2i(const vj_fint n[1], const float a11[], const float a22[], const float a21[],
+                float c[], float at[], float l1[], float l2[], unsigned p[]);
+vj_fint cbjac2i(const vj_fint n[1], const float a11[], const float a22[], const float a21r[], const float a21i[],
+                float c[], float cat[], float sat[], float l1[], float l2[], unsigned p[]);
+
+/* Device-pointer forms: the same computation on GPU-resident arrays, enqueued on
+ * `stream` (a cudaStream_t; NULL = the legacy default stream). `internal` selects the
+ * masked i-variant. Return 1, or a negative code. */
+vj_fint vj_dbjac2_dev(vj_fint n, int internal, const double *a11, const double *a22, const double *a21,
+                      double *c, double *at, double *l1, double *l2, unsigned *p, void *stream);
+vj_fint vj_zbjac2_dev(vj_fint n, int internal, const double *a11, const double *a22, const double *a21r,
+                      const double *a21i, double *c, double *cat, double *sat, double *l1, double *l2, unsigned *p,
+                      void *stream);
+vj_fint vj_sbjac2_dev(vj_fint n, int internal, const float *a11, const float *a22, const float *a21,
+                      float *c, float *at, float *l1, float *l2, unsigned *p, void *stream);
+vj_fint vj_cbjac2_dev(vj_fint n, int internal, const float *a11, const float *a22, const float *a21r,
+                      const float *a21i, float *c, float *cat, float *sat, float *l1, float *l2, unsigned *p,
+                      void *stream);
+
+/* ---------------- one-sided Jacobi SVD ----------------
+ * G (m x n, column-major, leading dimension ldG) is overwritten by U = G V diag(1/sigma)
+ * on convergence; V (n x n) accumulates the rotations (V := I first when iwork[0] == 0,
+ * otherwise V is a preset matrix that the rotations are applied to). sigma_j =
+ * fS[j] * 2^eS[j]. js holds stp rows of n column indices (n/2 pairs per row, p < q);
+ * swp caps the number of sweeps. Returns the number of sweeps (== *swp: not converged,
+ * G and V left scaled) or a negative error code (the reference's: -1..-6, -12, -13
+ * (zero preset V), and -__LINE__ codes of the reference's sources for numerical
+ * failures: d/s -80, -92, -320, -580, -588; z/c -92, -104, -345, -347, -630, -638).
+ * Preconditions as in the reference: m >= n, m % 8 == 0 (s, c: % 16), n even,
+ * (n/2) % 8 == 0 (s, c: % 16), ld >= rows and % 8 (16), 64-byte aligned G, V, work.
+ * work: >= 5n (real) / 7n (complex) elements, iwork >= n/8 (d, z) / n/16 (s, c).
+ *   replaces dvjsvd_  src/dvjsvd.h:10, src/dvjsvd.c:40
+ *            zvjsvd_  src/zvjsvd.h:10, src/zvjsvd.c:40
+ *            svjsvd_  src/svjsvd.h:10, src/svjsvd.c:40
+ *            cvjsvd_  src/cvjsvd.h:22, src/cvjsvd.c:40 */
+vj_fint dvjsvd_(const vj_fnat m[1], const vj_fnat n[1], double G[], const vj_fnat ldG[1], double V[],
+                const vj_fnat ldV[1], double eS[], double fS[], const unsigned js[], const unsigned stp[1],
+                const unsigned swp[1], double work[], unsigned iwork[]);
+vj_fint zvjsvd_(const vj_fnat m[1], const vj_fnat n[1], double Gr[], const vj_fnat ldGr[1], double Gi[],
+                const vj_fnat ldGi[1], double Vr[], const vj_fnat ldVr[1], double Vi[], const vj_fnat ldVi[1],
+                double eS[], double fS[], const unsigned js[], const unsigned stp[1], const unsigned swp[1],
+                double work[], unsigned iwork[]);
+vj_fint svjsvd_(const vj_fnat m[1], const vj_fnat n[1], float G[], const vj_fnat ldG[1], float V[],
+                const vj_fnat ldV[1], float eS[], float fS[], const unsigned js[], const unsigned stp[1],
+                const unsigned swp[1], float work[], unsigned iwork[]);
+vj_fint cvjsvd_(const vj_fnat m[1], const vj_fnat n[1], float Gr[], const vj_fnat ldGr[1], float Gi[],
+                const vj_fnat ldGi[1], float Vr[], const vj_fnat ldVr[1], float Vi[], const vj_fnat ldVi[1],
+                float eS[], float fS[], const unsigned js[], const unsigned stp[1], const unsigned swp[1],
+                float work[], unsigned iwork[]);
+
+/* Device-pointer SVD: all arrays (G, V, eS, fS, js) on the GPU; Gi/Vi NULL for real
+ * data. preset != 0 means V holds a preset matrix. Synchronises `stream` once per
+ * sweep (to test convergence). Returns like the host form. */
+vj_fint vj_dvjsvd_dev(vj_fnat m, vj_fnat n, double *G, vj_fnat ldG, double *V, vj_fnat ldV, double *eS, double *fS,
+                      const unsigned *js, unsigned stp, unsigned swp, int preset, void *stream);
+vj_fint vj_zvjsvd_dev(vj_fnat m, vj_fnat n, double *Gr, vj_fnat ldGr, double *Gi, vj_fnat ldGi, double *Vr,
+                      vj_fnat ldVr, double *Vi, vj_fnat ldVi, double *eS, double *fS, const unsigned *js,
+                      unsigned stp, unsigned swp, int preset, void *stream);
+vj_fint vj_svjsvd_dev(vj_fnat m, vj_fnat n, float *G, vj_fnat ldG, float *V, vj_fnat ldV, float *eS, float *fS,
+                      const unsigned *js, unsigned stp, unsigned swp, int preset, void *stream);
+vj_fint vj_cvjsvd_dev(vj_fnat m, vj_fnat n, float *Gr, vj_fnat ldGr, float *Gi, vj_fnat ldGi, float *Vr,
+                      vj_fnat ldVr, float *Vi, vj_fnat ldVi, float *eS, float *fS, const unsigned *js,
+                      unsigned stp, unsigned swp, int preset, void *stream);
+
+/* ---------------- pivot strategy tables ----------------
+ * replaces pjs() src/pjs.h:21, src/pjs.c:9: returns a malloc'ed table of *stp rows of n
+ * unsigned (n/2 pairs per row, p < q inside a pair), generated on the GPU, or NULL.
+ * id 2 (PJS_ME): *stp = n-1; id 4 (PJS_MM): *stp = n. The orderings are published
+ * parallel orderings standing in for libpvn's (see the project's design notes): the
+ * shape and pair contract match, the exact tables are not pinned. Free with free().
+ * vj_pjs_dev writes the table to device memory (stp*n unsigned). */
+unsigned *pjs(long id, unsigned n, unsigned stp[1]);
+vj_fint vj_pjs_dev(long id, unsigned n, unsigned *table, void *stream);
+
+/* ---------------- library ---------------- */
+/* Number of sweeps-per-phase statistics of the last host-API SVD call (the JTRACE
+ * equivalent): total rotations per sweep and per-phase GPU times in seconds. */
+typedef struct vj_trace {
+  unsigned sweeps;
+  unsigned long long rotations[64];
+  double t_total;
+} vj_trace;
+vj_fint vj_last_trace(vj_trace *out);
+const char *vj_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* !VECJAC_GB300_H */

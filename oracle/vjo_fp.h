@@ -31,7 +31,9 @@ static inline double vjo_dsgn(double x) { return vjo_u2d(vjo_d2u(x) & (UINT64_C(
 static inline double vjo_dor(double a, double b) { return vjo_u2d(vjo_d2u(a) | vjo_d2u(b)); }
 static inline double vjo_dxor(double a, double b) { return vjo_u2d(vjo_d2u(a) ^ vjo_d2u(b)); }
 static inline double vjo_dneg(double x) { return vjo_dxor(x, -0.0); }
-static inline double vjo_dqnan(void) { return vjo_u2d(UINT64_C(0xFFF8000000000000)); }
+/* the x86 default NaN; read through a volatile so that the compiler cannot fold later
+ * arithmetic on it into a NaN of another sign */
+static inline double vjo_dqnan(void) { volatile uint64_t u = UINT64_C(0xFFF8000000000000); return vjo_u2d(u); }
 
 /* floor(log2|x|) as an int for finite nonzero x */
 static inline int vjo_dilogb(double x)
@@ -50,7 +52,7 @@ static inline int vjo_dilogb(double x)
 static inline double vjo_dgetexp(double x)
 {
   if (isnan(x))
-    return x + x;
+    return vjo_u2d(vjo_d2u(x) | (UINT64_C(1) << 51));
   if (isinf(x))
     return HUGE_VAL;
   if (x == 0.0)
@@ -95,12 +97,16 @@ static inline double vjo_dscale2(double x, int n)
   return x * vjo_u2d((uint64_t)(n + 1023) << 52);
 }
 
+static inline double vjo_dquiet(double x) { return vjo_u2d(vjo_d2u(x) | (UINT64_C(1) << 51)); }
+
+/* VSCALEFPD as measured on an AVX-512 core: a NaN x gives +inf for y = +inf and +0 for
+ * y = -inf, otherwise the quieted x; a NaN y (x not NaN) gives the quieted y */
 static inline double vjo_dscalef(double x, double y)
 {
   if (isnan(x))
-    return x + x;
+    return ((y == HUGE_VAL) ? HUGE_VAL : ((y == -HUGE_VAL) ? 0.0 : vjo_dquiet(x)));
   if (isnan(y))
-    return y + y;
+    return vjo_dquiet(y);
   if (isinf(x))
     return (y == -HUGE_VAL) ? vjo_dqnan() : x;
   if (x == 0.0)
@@ -125,7 +131,7 @@ static inline float vjo_ssgn(float x) { return vjo_u2f(vjo_f2u(x) & (UINT32_C(1)
 static inline float vjo_sor(float a, float b) { return vjo_u2f(vjo_f2u(a) | vjo_f2u(b)); }
 static inline float vjo_sxor(float a, float b) { return vjo_u2f(vjo_f2u(a) ^ vjo_f2u(b)); }
 static inline float vjo_sneg(float x) { return vjo_sxor(x, -0.0f); }
-static inline float vjo_sqnan(void) { return vjo_u2f(UINT32_C(0xFFC00000)); }
+static inline float vjo_sqnan(void) { volatile uint32_t u = UINT32_C(0xFFC00000); return vjo_u2f(u); }
 
 static inline int vjo_silogb(float x)
 {
@@ -143,7 +149,7 @@ static inline int vjo_silogb(float x)
 static inline float vjo_sgetexp(float x)
 {
   if (isnan(x))
-    return x + x;
+    return vjo_u2f(vjo_f2u(x) | (UINT32_C(1) << 22));
   if (isinf(x))
     return HUGE_VALF;
   if (x == 0.0f)
@@ -183,12 +189,14 @@ static inline float vjo_sscale2(float x, int n)
   return x * vjo_u2f((uint32_t)(n + 127) << 23);
 }
 
+static inline float vjo_squiet(float x) { return vjo_u2f(vjo_f2u(x) | (UINT32_C(1) << 22)); }
+
 static inline float vjo_sscalef(float x, float y)
 {
   if (isnan(x))
-    return x + x;
+    return ((y == HUGE_VALF) ? HUGE_VALF : ((y == -HUGE_VALF) ? 0.0f : vjo_squiet(x)));
   if (isnan(y))
-    return y + y;
+    return vjo_squiet(y);
   if (isinf(x))
     return (y == -HUGE_VALF) ? vjo_sqnan() : x;
   if (x == 0.0f)

@@ -22,6 +22,30 @@ from oracle import oracle as O  # noqa: E402
 from vecjac_gb300 import workloads as W  # noqa: E402
 
 
+def special2x2(kind, n, seed):
+    """2x2 inputs with infinities and NaNs among the special finite values"""
+    rng = np.random.default_rng(seed)
+    dt = np.float64 if kind in "dz" else np.float32
+    fi = np.finfo(dt)
+    vals = np.array([0.0, -0.0, 1.0, -2.0, fi.max, -fi.max, fi.tiny, fi.smallest_subnormal, -fi.smallest_subnormal,
+                     np.inf, -np.inf, np.nan, 3e-300 if dt == np.float64 else 3e-40, 5.0], dt)
+    return [rng.choice(vals, n).astype(dt) for _ in range(4 if kind in "zc" else 3)]
+
+
+def bjac2_special_fixtures(ref):
+    for kind in "dszc":
+        ins = special2x2(kind, 1024, 4)
+        out = {"a11": ins[0], "a22": ins[1], "a21": ins[2]}
+        if kind in "zc":
+            out["a21i"] = ins[3]
+        names = ["c", "at", "sat", "l1", "l2", "p"] if kind in "zc" else ["c", "at", "l1", "l2", "p"]
+        for tag, sgn in (("sin", -1), ("tan", 1)):
+            r = ref.bjac2(kind, sgn * 1024, *ins)
+            for name, arr in zip(names, r[1:]):
+                out[f"{tag}_{name}"] = np.array(arr)
+        np.savez_compressed(os.path.join(HERE, f"bjac2_{kind}_special.npz"), **out)
+
+
 def bjac2_fixtures(ref):
     for kind in "dszc":
         lanes = 8 if kind in "dz" else 16
@@ -108,6 +132,7 @@ def main():
     ref = O.Reference()
     rst = O.Restatement()
     bjac2_fixtures(ref)
+    bjac2_special_fixtures(ref)
     svd_fixtures(ref, rst)
 
 

@@ -1,0 +1,151 @@
+"""Batched 2x2 EVD on the GPU, through the C ABI: bit-exact against the reference.
+
+* golden fixtures (outputs of VecJac compiled from its sources) for all four precisions,
+  both output forms (n < 0 sines, n > 0 tangents) and the masked i-variants;
+* the oracle restatement on larger seeded batches of the benchmark's distribution and on
+  special values (signed zeros, subnormals, extremes, inf and NaN);
+* the device-pointer entry points on CUDA tensors, and argument errors.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def vj():
+    import vecjac_gb300
+    from vecjac_gb300 import build
+    build.build()
+    return vecjac_gb300
+
+
+@pytest.fixture(scope="module")
+def rst():
+    O.build()
+    return O.Restatement()
+
+
+def same(a, b, zero_sign=True):
+    """bit equality, with any NaN equal to any NaN (payloads differ between CPUs and GPUs);
+    zero_sign=False also equates +0 and -0"""
+    a = np.ascontiguousarray(a)
+    b = np.ascontiguousarray(b)
+    if a.shape != b.shape:
+        return False
+    if a.dtype.kind == "f":
+        na, nb = np.isnan(a), np.isnan(b)
+        if not np.array_equal(na, nb):
+            return False
+        if not zero_sign:
+            return np.array_equal(a[~na], b[~nb])
+        return np.array_equal(a[~na].view(np.uint8), b[~nb].view(np.uint8))
+    return np.array_equal(a, b)
+
+
+NAMES = {"r": ["c", "at", "l1", "l2", "p"], "c": ["c", "at", "sat", "l1", "l2", "p"]}
+VARIANTS = [("sin", -1, False), ("tan", 1, False), ("isec", -1, True), ("itan", 1, True)]
+
+
+@pytest.mark.parametrize("kind", list("dszc"))
+@pytest.mark.parametrize("tag,sgn,internal", VARIANTS)
+def test_golden(vj, kind, tag, sgn, internal):
+    g = np.load(os.path.join(GOLD, f"bjac2_{kind}.npz"))
+    ins = [g["a11"], g["a22"], g["a21"]] + ([g["a21i"]] if kind in "zc" else [None])
+    n = ins[0].size
+    dt = ins[0].dtype
+    outs = dict(c=np.zeros(n, dt), at=np.zeros(n, dt), l1=np.zeros(n, dt), l2=np.zeros(n, dt))
+    if kind in "zc":
+        outs["sat"] = np.zeros(n, dt)
+    r = vj.bjac2(kind, sgn * n, *ins, p=(g["p_in"].copy() if internal else None), internal=internal, **outs)
+    assert r[0] == 1
+    for name, arr in zip(NAMES["c" if kind in "zc" else "r"], r[1:]):
+        assert same(arr, g[f"{tag}_{name}"]), (kind, tag, name)
+
+
+def special_inputs(kind, n, seed):
+    rng = np.random.default_rng(seed)
+    dt = np.float64 if kind in "dz" else np.float32
+    fi = np.finfo(dt)
+    vals = np.array([0.0, -0.0, 1.0, -2.0, fi.max, -fi.max, fi.tiny, fi.smallest_subnormal, -fi.smallest_subnormal,
+                     np.inf, -np.inf, np.nan, 3e-300 if dt == np.float64 else 3e-40, 5.0], dt)
+    return [rng.choice(vals, n).astype(dt) for _ in range(4 if kind in "zc" else 3)]
+
+
+@pytest.mark.parametrize("kind", list("dszc"))
+@pytest.mark.parametrize("src", ["bench", "special"])
+def test_vs_oracle(vj, rst, kind, src):
+    from vecjac_gb300 import workloads as W
+    n = (1 << 18) if src == "bench" else 4096
+    ins = W.pairs2x2(kind, n, seed=3) if src == "bench" else special_inputs(kind, n, 4)
+    a21i = ins[3] if kind in "zc" else None
+    for sgn, internal in ((-1, False), (1, False), (-1, True)):
+        lanes = 8 if kind in "dz" else 16
+        pin = (np.arange(n // lanes, dtype=np.uint32) % 3) * np.uint32(0x10001) if internal else None
+        ro = rst.bjac2(kind, sgn * n, ins[0], ins[1], ins[2], a21i, internal=internal,
+                       p=None if pin is None else pin.copy())
+        dt = ins[0].dtype
+        outs = dict(c=np.zeros(n, dt), at=np.zeros(n, dt), l1=np.zeros(n, dt), l2=np.zeros(n, dt))
+        if kind in "zc":
+            outs["sat"] = np.zeros(n, dt)
+        rg = vj.bjac2(kind, sgn * n, ins[0], ins[1], ins[2], a21i, p=None if pin is None else pin.copy(),
+                      internal=internal, **outs)
+        assert rg[0] == 1
+        # finite inputs: bit-exact. Inputs with inf/NaN create NaNs inside the computation,
+        # and IEEE 754 leaves the sign and payload of a propagated NaN to the hardware
+        # (x86, Arm and the GPU differ); that sign can reach the sign of a zero output, so
+        # those batches are compared up to NaN payloads and the sign of zero.
+        for x, y in zip(ro[1:], rg[1:]):
+            assert same(x, y, zero_sign=(src == "bench")), (kind, src, sgn, internal)
+
+
+@pytest.mark.parametrize("kind", list("dszc"))
+def test_device_entry(vj, rst, kind):
+    import torch
+    from vecjac_gb300 import workloads as W
+    n = 1 << 20
+    ins = W.pairs2x2(kind, n, seed=9)
+    dt = torch.float64 if kind in "dz" else torch.float32
+    lanes = 8 if kind in "dz" else 16
+    d_in = [torch.from_numpy(a).cuda() for a in ins]
+    outs = [torch.empty(n, dtype=dt, device="cuda") for _ in range(5 if kind in "zc" else 4)]
+    p = torch.zeros(n // lanes, dtype=torch.int32, device="cuda")
+    if kind in "zc":
+        r = vj.bjac2_dev(kind, -n, d_in[0], d_in[1], d_in[2], d_in[3], outs[0], outs[1], outs[2], outs[3], outs[4],
+                         p)
+    else:
+        r = vj.bjac2_dev(kind, -n, d_in[0], d_in[1], d_in[2], None, outs[0], outs[1], None, outs[2], outs[3], p)
+    torch.cuda.synchronize()
+    assert r == 1
+    ro = rst.bjac2(kind, -n, *ins)
+    for x, y in zip(ro[1:-1], outs):
+        assert same(x, y.cpu().numpy())
+    assert same(ro[-1], p.cpu().numpy().view(np.uint32))
+
+
+def test_errors_and_empty(vj):
+    a = np.zeros(12, np.float64)
+    assert vj.bjac2("d", 12, a, a, a)[0] == -1      # not a multiple of 8
+    assert vj.bjac2("s", -24, *(3 * [np.zeros(24, np.float32)]))[0] == -1
+    assert vj.bjac2("d", 0, a, a, a)[0] == 1
+    z = np.zeros(8)
+    assert vj.bjac2("z", 8, z, z, z, z)[0] == 1
+
+
+@pytest.mark.parametrize("kind", list("dszc"))
+@pytest.mark.parametrize("tag,sgn", [("sin", -1), ("tan", 1)])
+def test_special_golden(vj, kind, tag, sgn):
+    """inputs with infinities and NaNs against the reference: identical up to NaN payloads
+    (the GPU follows the x86 NaN-propagation rules on this path)"""
+    g = np.load(os.path.join(GOLD, f"bjac2_{kind}_special.npz"))
+    ins = [g["a11"], g["a22"], g["a21"]] + ([g["a21i"]] if kind in "zc" else [None])
+    n = ins[0].size
+    r = vj.bjac2(kind, sgn * n, *ins)
+    assert r[0] == 1
+    for name, arr in zip(NAMES["c" if kind in "zc" else "r"], r[1:]):
+        assert same(arr, g[f"{tag}_{name}"]), (kind, tag, name)

@@ -78,3 +78,25 @@ def test_nrm2_properties(rst):
     assert rst.nrm2(x * 2.0 ** 900) == rst.nrm2(x) * 2.0 ** 900
     assert rst.nrm2(x * 2.0 ** -1000) > 0
     assert rst.nrm2(np.zeros(7)) == 0.0
+
+
+def nan_same(a, b):
+    a = np.ascontiguousarray(a)
+    b = np.ascontiguousarray(b)
+    if a.dtype.kind != "f":
+        return np.array_equal(a, b)
+    na, nb = np.isnan(a), np.isnan(b)
+    return np.array_equal(na, nb) and np.array_equal(a[~na].view(np.uint8), b[~nb].view(np.uint8))
+
+
+@pytest.mark.parametrize("kind", list("dszc"))
+@pytest.mark.parametrize("tag,sgn", [("sin", -1), ("tan", 1)])
+def test_bjac2_special_golden(rst, kind, tag, sgn):
+    """inf and NaN inputs: identical to the reference up to NaN payloads"""
+    g = np.load(os.path.join(GOLD, f"bjac2_{kind}_special.npz"))
+    ins = [g["a11"], g["a22"], g["a21"]] + ([g["a21i"]] if kind in "zc" else [])
+    n = ins[0].size
+    r = rst.bjac2(kind, sgn * n, *ins)
+    names = ["c", "at", "sat", "l1", "l2", "p"] if kind in "zc" else ["c", "at", "l1", "l2", "p"]
+    for name, arr in zip(names, r[1:]):
+        assert nan_same(arr, g[f"{tag}_{name}"]), (kind, tag, name)

@@ -1,0 +1,117 @@
+#include <cstring>
+#include <mutex>
+
+#include "vj_host.h"
+
+namespace vj {
+namespace host {
+
+bool gpu_ready()
+{
+  static int ok = -1;
+  if (ok < 0) {
+    int cnt = 0;
+    ok = ((cudaGetDeviceCount(&cnt) == cudaSuccess) && (cnt > 0)) ? 1 : 0;
+  }
+  return ok == 1;
+}
+
+int sm_count()
+{
+  static int n = 0;
+  if (!n) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0)
+      n = 1;
+  }
+  return n;
+}
+
+bool Staging::reserve(size_t bytes)
+{
+  if (bytes <= size)
+    return true;
+  if (ptr) {
+    cudaDeviceSynchronize();
+    cudaFree(ptr);
+    ptr = nullptr;
+    size = 0;
+  }
+  if (cudaMalloc(&ptr, bytes) != cudaSuccess) {
+    ptr = nullptr;
+    cudaGetLastError();
+    return false;
+  }
+  size = bytes;
+  return true;
+}
+
+Staging &staging()
+{
+  static Staging s;
+  return s;
+}
+
+Staging &staging2()
+{
+  static Staging s;
+  return s;
+}
+
+bool streams2(cudaStream_t s[2])
+{
+  static cudaStream_t st[2] = {nullptr, nullptr};
+  static bool ok = false;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    ok = (cudaStreamCreateWithFlags(&st[0], cudaStreamNonBlocking) == cudaSuccess) &&
+         (cudaStreamCreateWithFlags(&st[1], cudaStreamNonBlocking) == cudaSuccess);
+  });
+  s[0] = st[0];
+  s[1] = st[1];
+  return ok;
+}
+
+long long bjac2_chunk(long long n, size_t elem, bool cplx, int lanes)
+{
+  // about 512 MiB of device staging per buffer
+  const size_t per_elem = elem * (cplx ? 9 : 7) + 1;
+  long long c = (long long)((size_t)512 << 20) / (long long)per_elem;
+  c -= c % (lanes * 64);
+  if (c < lanes * 64)
+    c = lanes * 64;
+  if (c > n)
+    c = n;
+  return c;
+}
+
+static vj_trace g_trace;
+
+void trace_reset()
+{
+  memset(&g_trace, 0, sizeof(g_trace));
+}
+
+void trace_sweep(unsigned sweep, unsigned long long rotations)
+{
+  if (sweep < 64)
+    g_trace.rotations[sweep] = rotations;
+  g_trace.sweeps = sweep + 1;
+}
+
+}  // namespace host
+}  // namespace vj
+
+extern "C" vj_fint vj_last_trace(vj_trace *out)
+{
+  if (!out)
+    return VJ_ERR_ARG;
+  *out = vj::host::g_trace;
+  return 0;
+}
+
+extern "C" const char *vj_version(void)
+{
+  return "vecjac_gb300 0.1 (sm_103a)";
+}

@@ -1,0 +1,189 @@
+// One 2x2 Hermitian eigenproblem per call, in VecJac's operation order, bit-exact with
+// the reference's AVX-512 lanes:
+//   real:    D8JAC2_LOOP / D8JACL_LOOP / D8JACI_LOOP   src/dbjac2.c:17-44, :51-78, :148-175
+//            (FP32: S8JAC*_LOOP, src/sbjac2.c, constants src/scjac2.h)
+//   complex: Z8JAC2_LOOP / Z8JACL_LOOP / Z8JACI_LOOP   src/zbjac2.c:18-62, :65-106, :179-219
+// KIND 0: cosine + tangent(s), KIND 1: cosine + sine(s), KIND 2: secant + tangent(s).
+// Finite inputs take a path whose exponent logic (getexp, min, scalef by an integer)
+// runs on the integer pipes; inputs with an inf or NaN take the literal transcription.
+#pragma once
+#include "vj_fp.cuh"
+
+namespace vj {
+
+template <typename T> __device__ __forceinline__ bool all_finite3(T a, T b, T c)
+{
+  return visfinite(a) && visfinite(b) && visfinite(c);
+}
+
+// 1020 - getexp(x) as an int for finite x; zero -> "huge" (the reference's DBL_MAX cap)
+template <typename T> __device__ __forceinline__ int escale(T x)
+{
+  constexpr int BE = (sizeof(T) == 8) ? 1020 : 124;
+  return ((fp<T>::bits(x) & ~fp<T>::SIGN) ? (BE - ilogb_(x)) : (1 << 20));
+}
+
+// max(q, 0) then min(., sqrt_huge) for q = |.|/|.| (q is +0, positive or NaN), as integers
+template <typename T> __device__ __forceinline__ T clamp_t2(T q)
+{
+  using F = fp<T>;
+  const typename F::U u = F::bits(q);
+  const typename F::U lim = F::bits(F::sqrt_huge());
+  // NaN (u > inf) and +0 give +0; otherwise min(q, sh)
+  if (u > F::bits(F::inf()) || u == 0)
+    return (T)0;
+  return (u < lim) ? q : F::sqrt_huge();
+}
+
+// shared tail of the real and complex lanes: angle from the prescaled (a1, a2, ab)
+template <typename T> struct angle {
+  T t1, s2, s1;
+};
+
+template <typename T> __device__ __forceinline__ angle<T> jac_angle(T a1, T a2, T ab, T &ad_out)
+{
+  using F = fp<T>;
+  const T one = (T)1;
+  const T ad = a1 - a2;
+  ad_out = ad;
+  const T t2 = vor(clamp_t2(F::div(ab, vabs(ad))), vsgn(ad));
+  const T t1 = F::div(t2, one + F::sqrt_(F::fma_(t2, t2, one)));
+  const T s2 = F::fma_(t1, t1, one);
+  return angle<T>{t1, s2, F::sqrt_(s2)};
+}
+
+template <typename T, int KIND>
+__device__ __forceinline__ unsigned rjac2(T a1, T a2, T ar, T &c, T &at, T &l1, T &l2)
+{
+  using F = fp<T>;
+  const T one = (T)1;
+  T L1, L2, t1, s1, s2, as;
+  if (all_finite3(a1, a2, ar)) {
+    const int es = min(min(escale(a1), escale(a2)), min(escale(ar), 1 << 20));
+    ar = scale2(ar, es);
+    a1 = scale2(a1, es);
+    a2 = scale2(a2, es);
+    const T aa = vabs(ar);
+    as = vsgn(ar);
+    const T ab = scale2(aa, 1);
+    T ad;
+    const angle<T> g = jac_angle(a1, a2, ab, ad);
+    t1 = g.t1; s2 = g.s2; s1 = g.s1;
+    L1 = F::div(F::fma_(t1, F::fma_(a2, t1, ab), a1), s2);
+    L2 = F::div(F::fma_(t1, F::fma_(a1, t1, vneg(ab)), a2), s2);
+    l1 = scale2(L1, -es);
+    l2 = scale2(L2, -es);
+  }
+  else {
+    const T zero = (T)0, sh = F::sqrt_huge(), huge = F::max_(), be = F::big_exp();
+    const T e1 = xsub(be, getexp(a1)), e2 = xsub(be, getexp(a2)), er = xsub(be, getexp(ar));
+    T es = vmin(vmin(e1, e2), vmin(er, huge));
+    ar = scalef(ar, es);
+    a1 = scalef(a1, es);
+    a2 = scalef(a2, es);
+    const T aa = vabs(ar);
+    as = vsgn(ar);
+    es = vneg(es);
+    const T ab = scalef(aa, one);
+    const T ad = xsub(a1, a2);
+    const T t2 = vor(vmin(vmax(xdiv(ab, vabs(ad)), zero), sh), vsgn(ad));
+    t1 = xdiv(t2, xadd(one, xsqrt(xfma(t2, t2, one))));
+    s2 = xfma(t1, t1, one);
+    s1 = xsqrt(s2);
+    L1 = xdiv(xfma(t1, xfma(a2, t1, ab), a1), s2);
+    L2 = xdiv(xfma(t1, xfma(a1, t1, vneg(ab)), a2), s2);
+    l1 = scalef(L1, es);
+    l2 = scalef(L2, es);
+  }
+  if (KIND == 2) {
+    at = vxor(t1, as);
+    c = s1;
+  }
+  else {
+    c = F::div(one, s1);
+    at = ((KIND == 1) ? F::div(vxor(t1, as), s1) : vxor(t1, as));
+  }
+  return (L1 < L2) ? 1u : 0u;
+}
+
+template <typename T, int KIND>
+__device__ __forceinline__ unsigned cjac2(T a1, T a2, T ar, T ai, T &c, T &cat, T &sat, T &l1, T &l2)
+{
+  using F = fp<T>;
+  const T one = (T)1, zero = (T)0;
+  T L1, L2, t1, s1, s2, ar_, ai_;
+  if (all_finite3(a1, a2, ar) && visfinite(ai)) {
+    const int es = min(min(1 << 20, min(escale(a1), escale(a2))), min(escale(ar), escale(ai)));
+    ar = scale2(ar, es);
+    ai = scale2(ai, es);
+    a1 = scale2(a1, es);
+    a2 = scale2(a2, es);
+    ar_ = vabs(ar);
+    ai_ = vabs(ai);
+    const T as = vsgn(ar);
+    const T am = vmin(ar_, ai_);
+    const T aM = vmax(ar_, ai_);
+    T aa = vmax(F::div(am, aM), zero);
+    aa = F::sqrt_(F::fma_(aa, aa, one)) * aM;
+    ar_ = vor(vmin(F::div(ar_, aa), one), as);
+    ai_ = F::div(ai, vmax(aa, F::true_min()));
+    const T ab = scale2(aa, 1);
+    T ad;
+    const angle<T> g = jac_angle(a1, a2, ab, ad);
+    t1 = g.t1; s2 = g.s2; s1 = g.s1;
+    L1 = F::div(F::fma_(t1, F::fma_(a2, t1, ab), a1), s2);
+    L2 = F::div(F::fma_(t1, F::fma_(a1, t1, vneg(ab)), a2), s2);
+    l1 = scale2(L1, -es);
+    l2 = scale2(L2, -es);
+  }
+  else {
+    const T sh = F::sqrt_huge(), huge = F::max_(), be = F::big_exp();
+    const T e1 = xsub(be, getexp(a1)), e2 = xsub(be, getexp(a2)), er = xsub(be, getexp(ar)), ei = xsub(be, getexp(ai));
+    T es = vmin(huge, vmin(vmin(e1, e2), vmin(er, ei)));
+    ar = scalef(ar, es);
+    ai = scalef(ai, es);
+    a1 = scalef(a1, es);
+    a2 = scalef(a2, es);
+    ar_ = vabs(ar);
+    ai_ = vabs(ai);
+    const T as = vsgn(ar);
+    const T am = vmin(ar_, ai_);
+    const T aM = vmax(ar_, ai_);
+    es = vneg(es);
+    T aa = vmax(xdiv(am, aM), zero);
+    aa = xmul(xsqrt(xfma(aa, aa, one)), aM);
+    ar_ = vor(vmin(xdiv(ar_, aa), one), as);
+    ai_ = xdiv(ai, vmax(aa, F::true_min()));
+    const T ab = scalef(aa, one);
+    const T ad = xsub(a1, a2);
+    const T t2 = vor(vmin(vmax(xdiv(ab, vabs(ad)), zero), sh), vsgn(ad));
+    t1 = xdiv(t2, xadd(one, xsqrt(xfma(t2, t2, one))));
+    s2 = xfma(t1, t1, one);
+    s1 = xsqrt(s2);
+    L1 = xdiv(xfma(t1, xfma(a2, t1, ab), a1), s2);
+    L2 = xdiv(xfma(t1, xfma(a1, t1, vneg(ab)), a2), s2);
+    l1 = scalef(L1, es);
+    l2 = scalef(L2, es);
+  }
+  // ai_ is NaN only for inputs with an inf or NaN: keep the x86 NaN rules there
+  if (KIND == 2) {
+    ar_ = ar_ * t1;
+    c = s1;
+    ai_ = xmul(ai_, t1);
+  }
+  else if (KIND == 1) {
+    c = F::div(one, s1);
+    ar_ = F::div(ar_ * t1, s1);
+    ai_ = xdiv(xmul(ai_, t1), s1);
+  }
+  else {
+    c = F::div(one, s1);
+    ar_ = ar_ * t1;
+    ai_ = xmul(ai_, t1);
+  }
+  cat = ar_;
+  sat = ai_;
+  return (L1 < L2) ? 1u : 0u;
+}
+
+}  // namespace vj

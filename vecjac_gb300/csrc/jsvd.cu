@@ -1,0 +1,1095 @@
+// One-sided Jacobi SVD: dvjsvd_/zvjsvd_/svjsvd_/cvjsvd_ on the GPU.
+//
+// The reference (src/dvjsvd.c:40-638, src/zvjsvd.c:40-694) runs every pivot step of a
+// sweep as a sequence of OpenMP loops over the n/2 column pairs of that step: norms of
+// the columns changed in the previous step, scaled compensated dot products, the
+// convergence/shear test with the Gram prescale, the batched 2x2 EVD, classification,
+// and the rotation / shear / swap of the columns of G and V. Here one kernel launch is
+// one step and one CTA owns one pair for the whole step:
+//   1. step-start decisions that the reference takes on the host (rescale G when its
+//      largest element grew past 2^1022, rescale V likewise, the norm-overflow retry) are
+//      recomputed identically by every CTA from a small control block written by the
+//      previous launch; every CTA applies them to its own two columns, which together
+//      cover all of G and V;
+//   2. the dot product is accumulated by LANES threads (8 for FP64, 16 for FP32) in the
+//      reference's lane order, with its 2Sum compensation, and summed by the same
+//      halving tree as GCC's _mm512_reduce_add: the result is bit-identical;
+//   3. one thread takes the convergence test, the shear test, the prescale and the 2x2
+//      (vj::rjac2 / vj::cjac2) and picks the transformation;
+//   4. all threads apply it to the columns of G and V, tracking max |.| for the overflow
+//      control;
+//   5. the norms of the columns this step changed are computed right away (the
+//      reference computes them at the start of the next step, on the same data) by
+//      one warp per column with the project's two-pass 32-lane norm.
+// G and V stay in HBM/L2 (16 MiB for 1024x1024 FP64, far below the 129 MB L2); every
+// launch touches each column of G and V once for the dot, once for the update and once
+// for the norm. The arithmetic is FP64-pipe bound on GB300.
+#include <cfloat>
+#include <cmath>
+#include <cstdio>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "jac2.cuh"
+#include "vj_host.h"
+
+namespace vj {
+
+template <typename T> struct svdc;
+template <> struct svdc<double> {
+  static constexpr int LANES = 8;
+  static constexpr double EPS = DBL_EPSILON;
+  static constexpr int ROT_R = 1022, ROT_C = 1021;
+  static constexpr double MAX_FIN_EXP = 1023.0;
+  static constexpr double RMAX = DBL_MAX;
+};
+template <> struct svdc<float> {
+  static constexpr int LANES = 16;
+  static constexpr float EPS = FLT_EPSILON;
+  static constexpr int ROT_R = 126, ROT_C = 125;
+  static constexpr float MAX_FIN_EXP = 127.0f;
+  static constexpr float RMAX = FLT_MAX;
+};
+
+// control block of one pivot step (triple-buffered across launches)
+struct Ctl {
+  double MGbase, MVbase;  // max |G|, max |V| after this step's own rescaling (in T's range)
+  unsigned long long nMG, nMV;  // atomicMax of max |.| of the transformed columns (T bits)
+  int sT, sV;                   // accumulated power-of-two scalings of G and V
+  int ovf;                      // a norm computed at the end of the previous step overflowed
+  int pad;
+};
+
+struct SvdGlobal {
+  long long err;                // 0 or the (negative) error code, atomicMin
+  unsigned long long swt;       // transformed pairs in the current sweep
+  Ctl ctl[3];
+};
+
+template <typename T> struct SvdArgs {
+  long long m, n, ldG, ldGi, ldV, ldVi;
+  T *G, *Gi, *V, *Vi, *eS, *fS;
+  const unsigned *js;
+  SvdGlobal *g;
+  T tol, gst;
+  int nrm_exp, rot;
+  long long e_dot, e_doti, e_appg, e_appv;
+};
+
+template <typename T> __device__ __forceinline__ unsigned long long tbits(T x)
+{
+  return (unsigned long long)fp<T>::bits(x);
+}
+template <typename T> __device__ __forceinline__ T bitst(unsigned long long u)
+{
+  return fp<T>::val((typename fp<T>::U)u);
+}
+
+// |x| bits, NaN above inf, so that an integer max flags NaNs as "not finite"
+template <typename T> __device__ __forceinline__ unsigned long long absbits(T x)
+{
+  return (unsigned long long)(fp<T>::bits(x) & ~fp<T>::SIGN);
+}
+
+__device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long v)
+{
+#pragma unroll
+  for (int o = 16; o >= 1; o >>= 1) {
+    const unsigned long long w = __shfl_xor_sync(0xffffffffu, v, o);
+    v = (w > v) ? w : v;
+  }
+  return v;
+}
+
+// (e, f) of a norm d: d = f 2^e, f in [1,2) (src/dznrm2.h:4-23)
+template <typename T> __device__ __forceinline__ void ef_split(T d, T &e, T &f)
+{
+  using F = fp<T>;
+  if (visfinite(d)) {
+    if (d == (T)0) {
+      e = vneg(F::inf());
+      f = vor((T)1, vsgn(d));
+    }
+    else {
+      const int k = ilogb_(d);
+      e = (T)k;
+      f = scale2(d, -k);
+    }
+  }
+  else {
+    e = F::inf();
+    f = vor((visnan(d) ? (T)0 : (T)1), vsgn(d));
+  }
+}
+
+// The project's column norm (two-pass power-of-two scaling, 32 lanes, halving tree) for
+// one warp; every lane returns the same value.
+template <typename T> __device__ T warp_nrm2(const T *x, long long m)
+{
+  const int lane = threadIdx.x & 31;
+  unsigned long long mx = 0ull;
+  for (long long i = lane; i < m; i += 32) {
+    const unsigned long long a = absbits(x[i]);
+    mx = (a > mx) ? a : mx;
+  }
+  mx = warp_max_u64(mx);
+  const T a = bitst<T>(mx);
+  if (!visfinite(a))
+    return visnan(a) ? fp<T>::qnan() : a;
+  if (mx == 0ull)
+    return (T)0;
+  const int k = ilogb_(a);
+  T acc = (T)0;
+  for (long long i = lane; i < m; i += 32) {
+    const T y = scale2(x[i], -k);
+    acc = fp<T>::fma_(y, y, acc);
+  }
+#pragma unroll
+  for (int w = 16; w >= 1; w >>= 1)
+    acc = acc + __shfl_down_sync(0xffffffffu, acc, w);
+  acc = __shfl_sync(0xffffffffu, acc, 0);
+  return scale2(fp<T>::sqrt_(acc), k);
+}
+
+// VDHYPOT (src/vecdef.h:80-92) on scalars
+template <typename T> __device__ __forceinline__ T vhypot(T x, T y)
+{
+  const T x_ = vabs(x), y_ = vabs(y);
+  const T m_ = vmin(x_, y_), M_ = vmax(x_, y_);
+  T z = fp<T>::div(m_, M_);
+  z = vmax(z, (T)0);
+  z = fp<T>::fma_(z, z, (T)1);
+  z = fp<T>::sqrt_(z);
+  return z * M_;
+}
+
+// norm of column c (real, or complex with planes) by one warp; writes eS/fS; returns d
+template <typename T, bool CPLX> __device__ T col_norm(const SvdArgs<T> &a, long long c)
+{
+  T d = warp_nrm2(a.G + c * a.ldG, a.m);
+  if (CPLX) {
+    const T di = warp_nrm2(a.Gi + c * a.ldGi, a.m);
+    d = vhypot(d, di);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    T e, f;
+    ef_split(d, e, f);
+    a.eS[c] = e;
+    a.fS[c] = f;
+  }
+  return d;
+}
+
+// 2Sum (src/d2sum.h)
+template <typename T> __device__ __forceinline__ void two_sum(T a, T b, T &s, T &t)
+{
+  const T s_ = a + b;
+  T a_ = s_ - b;
+  T b_ = s_ - a_;
+  a_ = a - a_;
+  b_ = b - b_;
+  s = s_;
+  t = a_ + b_;
+}
+
+// one compensated product-accumulate step (src/ddpscl.c:51-60, MUL2SUM src/zdpscl.c)
+template <typename T> __device__ __forceinline__ void mul2sum(T x, T y, T &s, T &t, T &s_, T &t_)
+{
+  const T xy = fp<T>::mul_rd(x, y);
+  const T xy_ = fp<T>::fma_(x, y, vneg(xy));
+  two_sum(s, xy + t, s, t);
+  two_sum(s_, xy_ + t_, s_, t_);
+}
+
+// halving tree over the LANES lanes of warp 0 (GCC's _mm512_reduce_add order); lane 0 has it
+template <int LANES, typename T> __device__ __forceinline__ T hsum(T v)
+{
+#pragma unroll
+  for (int w = LANES / 2; w >= 1; w >>= 1)
+    v = __shfl_down_sync(0xffffffffu, v, w) + v;
+  return v;
+}
+
+// scaled compensated dot products (src/ddpscl.c / src/zdpscl.c) by warp 0; x = G_q, y = G_p
+template <typename T, bool CPLX>
+__device__ void pair_dot(const SvdArgs<T> &a, long long p, long long q, T ex, T ey, T fx, T fy, T &zr, T &zi)
+{
+  constexpr int L = svdc<T>::LANES;
+  const int lane = threadIdx.x & 31;
+  const T *xr = a.G + q * a.ldG, *yr = a.G + p * a.ldG;
+  const T *xi = CPLX ? (a.Gi + q * a.ldGi) : nullptr, *yi = CPLX ? (a.Gi + p * a.ldGi) : nullptr;
+  const int nx = -(int)ex, ny = -(int)ey;
+  T sr = 0, tr = 0, sr_ = 0, tr_ = 0, si = 0, ti = 0, si_ = 0, ti_ = 0;
+  if (lane < L) {
+    for (long long i = lane; i < a.m; i += L) {
+      const T xri = scale2(xr[i], nx);
+      const T yri = scale2(yr[i], ny);
+      if (CPLX) {
+        const T yii = scale2(yi[i], ny);
+        T xii = scale2(xi[i], nx);
+        mul2sum(xri, yri, sr, tr, sr_, tr_);
+        mul2sum(xii, yii, sr, tr, sr_, tr_);
+        xii = vneg(xii);
+        mul2sum(xri, yii, si, ti, si_, ti_);
+        mul2sum(xii, yri, si, ti, si_, ti_);
+      }
+      else
+        mul2sum(xri, yri, sr, tr, sr_, tr_);
+    }
+  }
+  const T nur = hsum<L>(sr) + (hsum<L>(tr) + (hsum<L>(sr_) + hsum<L>(tr_)));
+  T nui = 0;
+  if (CPLX)
+    nui = hsum<L>(si) + (hsum<L>(ti) + (hsum<L>(si_) + hsum<L>(ti_)));
+  const T de = fx * fy;
+  zr = fp<T>::div(nur, de);
+  zi = CPLX ? fp<T>::div(nui, de) : (T)0;
+}
+
+// efcmp (src/defops.h:46)
+template <typename T> __device__ __forceinline__ int efcmp(T e0, T f0, T e1, T f1)
+{
+  if (e0 > e1) return 1;
+  if (e0 < e1) return -1;
+  if (f0 > f1) return 1;
+  if (f0 < f1) return -1;
+  return 0;
+}
+template <typename T> __device__ __forceinline__ bool eflt(T e0, T e1, T f0, T f1)
+{
+  return (e0 < e1) || ((e0 == e1) && (f0 < f1));
+}
+template <typename T> __device__ __forceinline__ bool efle(T e0, T e1, T f0, T f1)
+{
+  return (e0 < e1) || ((e0 == e1) && (f0 <= f1));
+}
+
+template <typename T> struct PairState {
+  T ep, fp, eq, fq;      // norms (e, f) of columns p, q
+  T a21r, a21i;          // scaled dot (cosine of the angle)
+  T c, cat, sat;         // rotation: cosine, Re/Im of e^{i alpha} tangent
+  int code;              // 3/-3 shear (+/- permute), 2/-2 rotate, -1 swap, 1 nothing
+  int skip;              // an error stops this pair
+};
+
+// step-start decisions of src/dvjsvd.c:199-233 and the overflow branch :276-295
+template <typename T> struct Decision {
+  int gres, vres, ovf;   // rescale G (sR < 0), rescale V, retry after a norm overflow
+  int sNg, sNv;          // exponents used
+  T MG, MV;              // values after the step's rescaling
+  int sT, sV;
+};
+
+template <typename T> __device__ __forceinline__ int ef_exp(T x)
+{
+  // dbl2ef exponent of a nonnegative finite MG / MV (> 0)
+  return ilogb_(x);
+}
+
+template <typename T> __device__ Decision<T> decide(const SvdArgs<T> &a, const Ctl &cur)
+{
+  Decision<T> d;
+  T MG = (T)cur.MGbase, MV = (T)cur.MVbase;
+  const T nMG = bitst<T>(cur.nMG), nMV = bitst<T>(cur.nMV);
+  MG = fmax(MG, nMG);
+  MV = fmax(MV, nMV);
+  int eM = ef_exp(MG);
+  int sR = a.rot - eM;
+  const int sN = a.nrm_exp - eM - 1;
+  d.sT = cur.sT;
+  d.gres = (sR < 0);
+  d.sNg = sN;
+  if (d.gres) {
+    MG = scale2(MG, sN);
+    d.sT += sN;
+  }
+  eM = ef_exp(MV);
+  sR = a.rot - eM;
+  d.sNv = sR;
+  d.vres = (sR < 0);
+  d.sV = cur.sV;
+  if (d.vres) {
+    MV = scale2(MV, sR);
+    d.sV += sR;
+  }
+  d.ovf = (!d.gres && cur.ovf);
+  if (d.ovf) {
+    // the reference rescales G by its current sN, which the V block has just set (src/dvjsvd.c:227,281)
+    MG = scale2(MG, d.sNv);
+    d.sT += d.sNv;
+  }
+  d.MG = MG;
+  d.MV = MV;
+  return d;
+}
+
+template <typename T> __device__ void scale_cols(T *A, long long ld, long long rows, long long c0, long long c1,
+                                                 int e)
+{
+  for (long long i = threadIdx.x; i < rows; i += blockDim.x) {
+    A[c0 * ld + i] = scale2(A[c0 * ld + i], e);
+    A[c1 * ld + i] = scale2(A[c1 * ld + i], e);
+  }
+}
+
+template <typename T> __device__ __forceinline__ void amax(unsigned long long &m, T v)
+{
+  const unsigned long long b = absbits(v);
+  m = (b > m) ? b : m;
+}
+
+template <typename T, bool CPLX, bool TRACKV>
+__global__ void __launch_bounds__(256) k_step(SvdArgs<T> a, int st, int g3)
+{
+  using F = fp<T>;
+  __shared__ PairState<T> ps;
+  __shared__ unsigned long long red[8][4];
+  __shared__ int s_err;
+  SvdGlobal *const g = a.g;
+  if (*(volatile long long *)&g->err)
+    return;
+  const Ctl &cur = g->ctl[g3];
+  Ctl &nxt = g->ctl[(g3 + 1) % 3];
+  Ctl &nn = g->ctl[(g3 + 2) % 3];
+  const unsigned *r = a.js + (size_t)st * (size_t)a.n;
+  const long long p = r[2 * blockIdx.x], q = r[2 * blockIdx.x + 1];
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const Decision<T> d = decide(a, cur);
+  if (blockIdx.x == 0 && tid == 0) {
+    nxt.MGbase = (double)d.MG;
+    nxt.MVbase = (double)d.MV;
+    nxt.sT = d.sT;
+    nxt.sV = d.sV;
+    nn.nMG = 0ull;
+    nn.nMV = 0ull;
+    nn.ovf = 0;
+  }
+  if (tid == 0)
+    s_err = 0;
+  // ---- 1. rescaling (rare) ----
+  if (d.gres || d.ovf) {
+    const int e = d.gres ? d.sNg : d.sNv;
+    scale_cols(a.G, a.ldG, a.m, p, q, e);
+    if (CPLX)
+      scale_cols(a.Gi, a.ldGi, a.m, p, q, e);
+    __syncthreads();
+    if (warp < 2) {
+      const T nv = col_norm<T, CPLX>(a, warp ? q : p);
+      if (((tid & 31) == 0) && !(nv <= svdc<T>::RMAX))
+        s_err = 1;
+    }
+    __syncthreads();
+    if (s_err) {
+      // a second overflow after rescaling: the reference would rescale again
+      if (tid == 0)
+        atomicMin((long long *)&g->err, (long long)VJ_ERR_ARG);
+      return;
+    }
+  }
+  if (d.vres) {
+    scale_cols(a.V, a.ldV, a.n, p, q, d.sNv);
+    if (CPLX)
+      scale_cols(a.Vi, a.ldVi, a.n, p, q, d.sNv);
+  }
+  __syncthreads();
+  // ---- 2. the scaled dot product (warp 0) ----
+  if (warp == 0) {
+    const T ep = a.eS[p], fp_ = a.fS[p], eq = a.eS[q], fq = a.fS[q];
+    T zr = 0, zi = 0;
+    if ((eq >= -svdc<T>::RMAX) && (ep >= -svdc<T>::RMAX))
+      pair_dot<T, CPLX>(a, p, q, eq, ep, fq, fp_, zr, zi);
+    if (tid == 0) {
+      ps.ep = ep; ps.fp = fp_; ps.eq = eq; ps.fq = fq;
+      ps.a21r = zr;
+      ps.a21i = zi;
+      ps.skip = 0;
+      long long code = 0;
+      if (CPLX) {
+        if (!visfinite(zr))
+          code = a.e_dot;
+        if (!visfinite(zi))
+          code = (a.e_doti < code) ? a.e_doti : code;
+      }
+      else if (!visfinite(zr))
+        code = a.e_dot;
+      if (code) {
+        atomicMin((long long *)&g->err, code);
+        ps.skip = 1;
+      }
+      else {
+        // ---- 3. convergence, shear test, prescale, 2x2, classification ----
+        const T ab = CPLX ? vhypot(zr, zi) : vabs(zr);
+        const bool trans = (a.tol <= ab);
+        if (trans) {
+          atomicAdd(&g->swt, 1ull);
+          const T e1 = ep, e2 = eq, f1 = fp_, f2 = fq;
+          const bool ngs = eflt(e1, e2, f1, f2);
+          T maf = ngs ? f1 : f2, mae = ngs ? e1 : e2;
+          const T Maf = ngs ? f2 : f1, Mae = ngs ? e2 : e1;
+          maf = a.gst * maf;
+          mae = mae + getexp(maf);
+          maf = getmant(maf);
+          const bool cgs = eflt(mae, Mae, maf, Maf);
+          T f12 = F::div(f1, f2), e12 = e1 - e2, f21 = F::div(f2, f1), e21 = e2 - e1;
+          e12 = e12 + getexp(f12);
+          f12 = getmant(f12);
+          e21 = e21 + getexp(f21);
+          f21 = getmant(f21);
+          const bool c12 = efle(e12, e21, f12, f21);
+          const T E = c12 ? e21 : e12;
+          const T dd = vmin(svdc<T>::MAX_FIN_EXP - E, (T)0);
+          e12 = e12 + dd;
+          e21 = e21 + dd;
+          const T w11 = scalef(f12, e12), w22 = scalef(f21, e21), w21r = scalef(zr, dd);
+          unsigned perm;
+          T cc, at, sat = 0, l1, l2;
+          if (CPLX) {
+            const T w21i = scalef(zi, dd);
+            perm = cjac2<T, 0>(w11, w22, w21r, w21i, cc, at, sat, l1, l2);
+          }
+          else
+            perm = rjac2<T, 0>(w11, w22, w21r, cc, at, l1, l2);
+          ps.c = cc;
+          ps.cat = at;
+          ps.sat = sat;
+          if (!ngs && cgs)
+            ps.code = 3;
+          else if (ngs && cgs)
+            ps.code = -3;
+          else if (perm)
+            ps.code = -2;
+          else
+            ps.code = 2;
+        }
+        else if (efcmp(ep, fp_, eq, fq) < 0) {
+          a.eS[p] = eq; a.eS[q] = ep;
+          a.fS[p] = fq; a.fS[q] = fp_;
+          ps.code = -1;
+        }
+        else
+          ps.code = 1;
+      }
+    }
+  }
+  __syncthreads();
+  if (ps.skip)
+    return;
+  // ---- 4. apply ----
+  const int code = ps.code;
+  T *Gp = a.G + p * a.ldG, *Gq = a.G + q * a.ldG, *Vp = a.V + p * a.ldV, *Vq = a.V + q * a.ldV;
+  T *Gip = CPLX ? (a.Gi + p * a.ldGi) : nullptr, *Giq = CPLX ? (a.Gi + q * a.ldGi) : nullptr;
+  T *Vip = CPLX ? (a.Vi + p * a.ldVi) : nullptr, *Viq = CPLX ? (a.Vi + q * a.ldVi) : nullptr;
+  unsigned long long mG = 0ull, mV = 0ull, mp = 0ull, mq = 0ull, mpi = 0ull, mqi = 0ull;
+  bool chp = false, chq = false, vtouch = false;
+  T tVneg = (T)0;  // a negative tV (the reference's "should never happen" codes) only feeds a max
+  if (code == 1) {
+  }
+  else if (code == -1) {
+    for (long long i = tid; i < a.m; i += blockDim.x) {
+      T t = Gp[i]; Gp[i] = Gq[i]; Gq[i] = t;
+      if (CPLX) { t = Gip[i]; Gip[i] = Giq[i]; Giq[i] = t; }
+    }
+    for (long long i = tid; i < a.n; i += blockDim.x) {
+      T t = Vp[i]; Vp[i] = Vq[i]; Vq[i] = t;
+      if (CPLX) { t = Vip[i]; Vip[i] = Viq[i]; Viq[i] = t; }
+    }
+  }
+  else if (code == 3 || code == -3) {
+    // Gram-Schmidt-like shear (src/dgsscl.c:5-85, src/zgsscl.c)
+    const T ex = ps.ep, ey = ps.eq, fx = ps.fp, fy = ps.fq;
+    const int nx = -(int)ex, ny = -(int)ey;
+    const int px = (int)ex, py = (int)ey;
+    if (code == 3) {
+      const T ff = F::div(fy, fx);
+      const T tfr = vneg(ps.a21r) * ff;
+      const T tfi = CPLX ? (ps.a21i * ff) : (T)0;
+      for (long long i = tid; i < a.m; i += blockDim.x) {
+        if (CPLX) {
+          const T xri_ = scale2(Gp[i], nx), xii_ = scale2(Gip[i], nx);
+          const T yri_ = scale2(Gq[i], ny), yii_ = scale2(Giq[i], ny);
+          const T xr = F::fma_(tfr, xri_, F::fma_(vneg(tfi), xii_, yri_));
+          const T xi = F::fma_(tfr, xii_, F::fma_(tfi, xri_, yii_));
+          const T ur = scale2(xr, py), ui = scale2(xi, py);
+          Gq[i] = ur;
+          Giq[i] = ui;
+          amax(mq, ur); amax(mqi, ui);
+        }
+        else {
+          const T xi = scale2(Gp[i], nx);
+          const T yi = scale2(Gq[i], ny);
+          const T u = scale2(F::fma_(tfr, xi, yi), py);
+          Gq[i] = u;
+          amax(mq, u);
+        }
+      }
+      chq = true;
+    }
+    else {
+      const T ff = F::div(fx, fy);
+      const T tfr = vneg(ps.a21r) * ff;
+      const T tfi = CPLX ? (vneg(ps.a21i) * ff) : (T)0;
+      for (long long i = tid; i < a.m; i += blockDim.x) {
+        if (CPLX) {
+          const T yri = Gq[i], yii = Giq[i], xri = Gp[i], xii = Gip[i];
+          Gp[i] = yri;
+          Gip[i] = yii;
+          const T yri_ = scale2(yri, ny), yii_ = scale2(yii, ny);
+          const T xri_ = scale2(xri, nx), xii_ = scale2(xii, nx);
+          const T vr = F::fma_(tfr, yri_, F::fma_(vneg(tfi), yii_, xri_));
+          const T vi = F::fma_(tfr, yii_, F::fma_(tfi, yri_, xii_));
+          const T ur = scale2(vr, px), ui = scale2(vi, px);
+          Gq[i] = ur;
+          Giq[i] = ui;
+          amax(mq, ur); amax(mqi, ui);
+        }
+        else {
+          const T xi = Gp[i], yi = Gq[i];
+          Gp[i] = yi;
+          const T u = scale2(F::fma_(tfr, scale2(yi, ny), scale2(xi, nx)), px);
+          Gq[i] = u;
+          amax(mq, u);
+        }
+      }
+      for (long long i = tid; i < a.n; i += blockDim.x) {
+        T t = Vp[i]; Vp[i] = Vq[i]; Vq[i] = t;
+        if (CPLX) { t = Vip[i]; Vip[i] = Viq[i]; Viq[i] = t; }
+      }
+      if (tid == 0) {
+        a.eS[p] = ps.eq; a.eS[q] = ps.ep;
+        a.fS[p] = ps.fq; a.fS[q] = ps.fp;
+      }
+      chq = true;
+    }
+    mG = (mq > mqi) ? mq : mqi;
+  }
+  else {
+    // rotation (src/djrot.c, src/djrotf.c, src/zjrot.c, src/zjrotf.c); code -2 permutes
+    const bool perm = (code == -2);
+    const T c = ps.c, at = ps.cat, sat = ps.sat;
+    // the reference marks both columns as changed after any rotation (src/dvjsvd.c:573)
+    chp = chq = true;
+    const bool real_rot = (!CPLX) || (sat == (T)0);
+    const bool cone = (c == (T)1);
+    if (real_rot && at == (T)0) {
+      // c == 1: identity (or a swap when permuting); c != 1 "never happens" (-4 / -10)
+      if (cone && perm) {
+        for (long long i = tid; i < a.m; i += blockDim.x) {
+          T t = Gp[i]; Gp[i] = Gq[i]; Gq[i] = t;
+          if (CPLX) { t = Gip[i]; Gip[i] = Giq[i]; Giq[i] = t; }
+        }
+        for (long long i = tid; i < a.n; i += blockDim.x) {
+          T t = Vp[i]; Vp[i] = Vq[i]; Vq[i] = t;
+          if (CPLX) { t = Vip[i]; Vip[i] = Viq[i]; Viq[i] = t; }
+        }
+      }
+      else if (!cone)
+        tVneg = (T)-4;
+    }
+    else if (real_rot) {
+      for (int pl = 0; pl < (CPLX ? 2 : 1); ++pl) {
+        T *X = pl ? Gip : Gp, *Y = pl ? Giq : Gq;
+        for (long long i = tid; i < a.m; i += blockDim.x) {
+          const T x = X[i], y = Y[i];
+          T xr = perm ? F::fma_(vneg(x), at, y) : F::fma_(y, at, x);
+          T yr = perm ? F::fma_(y, at, x) : F::fma_(vneg(x), at, y);
+          if (!cone) { xr = xr * c; yr = yr * c; }
+          X[i] = xr; Y[i] = yr;
+          amax(mG, xr); amax(mG, yr);
+        }
+        T *XV = pl ? Vip : Vp, *YV = pl ? Viq : Vq;
+        for (long long i = tid; i < a.n; i += blockDim.x) {
+          const T x = XV[i], y = YV[i];
+          T xr = perm ? F::fma_(vneg(x), at, y) : F::fma_(y, at, x);
+          T yr = perm ? F::fma_(y, at, x) : F::fma_(vneg(x), at, y);
+          if (!cone) { xr = xr * c; yr = yr * c; }
+          XV[i] = xr; YV[i] = yr;
+          if (TRACKV) { amax(mV, xr); amax(mV, yr); }
+        }
+      }
+      chp = chq = true;
+      vtouch = true;
+    }
+    else {
+      const T cta = at, sta = sat, cna = vneg(at);
+      for (int mat = 0; mat < 2; ++mat) {
+        T *Xr = mat ? Vp : Gp, *Xi = mat ? Vip : Gip, *Yr = mat ? Vq : Gq, *Yi = mat ? Viq : Giq;
+        const long long rows = mat ? a.n : a.m;
+        unsigned long long &mm = mat ? mV : mG;
+        for (long long i = tid; i < rows; i += blockDim.x) {
+          const T x_r = Xr[i], x_i = Xi[i], y_r = Yr[i], y_i = Yi[i];
+          T ar = F::fma_(y_r, cta, F::fma_(vneg(y_i), sta, x_r));
+          T ai = F::fma_(y_r, sta, F::fma_(y_i, cta, x_i));
+          T br = F::fma_(x_r, cna, F::fma_(vneg(x_i), sta, y_r));
+          T bi = F::fma_(x_r, sta, F::fma_(x_i, cna, y_i));
+          if (!cone) { ar = ar * c; ai = ai * c; br = br * c; bi = bi * c; }
+          if (perm) { Yr[i] = ar; Yi[i] = ai; Xr[i] = br; Xi[i] = bi; }
+          else { Xr[i] = ar; Xi[i] = ai; Yr[i] = br; Yi[i] = bi; }
+          if (!mat || TRACKV) { amax(mm, ar); amax(mm, ai); amax(mm, br); amax(mm, bi); }
+        }
+      }
+      chp = chq = true;
+      vtouch = true;
+    }
+  }
+  (void)vtouch;
+  (void)tVneg;
+  // block max of |G| and |V| updates
+  mG = warp_max_u64(mG);
+  mV = warp_max_u64(mV);
+  if ((tid & 31) == 0) {
+    red[warp][0] = mG;
+    red[warp][1] = mV;
+  }
+  __syncthreads();
+  if (tid == 0) {
+    unsigned long long bg = 0ull, bv = 0ull;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+      bg = (red[w][0] > bg) ? red[w][0] : bg;
+      bv = (red[w][1] > bv) ? red[w][1] : bv;
+    }
+    const T tG = bitst<T>(bg), tV = bitst<T>(bv);
+    if (!visfinite(tG))
+      atomicMin((long long *)&g->err, a.e_appg);
+    else if (!visfinite(tV))
+      atomicMin((long long *)&g->err, a.e_appv);
+    else {
+      if (bg)
+        atomicMax(&nxt.nMG, bg);
+      if (bv)
+        atomicMax(&nxt.nMV, bv);
+    }
+  }
+  // ---- 5. norms of the changed columns, for the next step ----
+  if (chp || chq) {
+    if ((warp == 0 && chp) || (warp == 1 && chq)) {
+      const T nv = col_norm<T, CPLX>(a, warp ? q : p);
+      if (((tid & 31) == 0) && !(nv <= svdc<T>::RMAX))
+        atomicOr(&nxt.ovf, 1);
+    }
+  }
+}
+
+// norms of all columns before the first step (src/dvjsvd.c:174-180 sets w1 = 1)
+template <typename T, bool CPLX> __global__ void k_norms(SvdArgs<T> a)
+{
+  const long long c = (long long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (c >= a.n)
+    return;
+  const T nv = col_norm<T, CPLX>(a, c);
+  if (((threadIdx.x & 31) == 0) && !(nv <= svdc<T>::RMAX))
+    atomicOr(&a.g->ctl[0].ovf, 1);
+}
+
+// max |a_ij| with min(., inf) (src/dnormx.c); result as bits in *out (atomicMax)
+template <typename T>
+__global__ void k_normx(const T *A, long long ld, long long rows, long long cols, unsigned long long *out)
+{
+  unsigned long long m = 0ull;
+  const unsigned long long inf = absbits(fp<T>::inf());
+  for (long long j = blockIdx.y; j < cols; j += gridDim.y)
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < rows; i += (long long)gridDim.x * blockDim.x) {
+      unsigned long long b = absbits(A[j * ld + i]);
+      b = (b > inf) ? inf : b;  // VMINPD(|x|, inf) maps a NaN to inf
+      m = (b > m) ? b : m;
+    }
+  m = warp_max_u64(m);
+  if ((threadIdx.x & 31) == 0 && m)
+    atomicMax(out, m);
+}
+
+template <typename T> __global__ void k_scale(T *A, long long ld, long long rows, long long cols, int e)
+{
+  for (long long j = blockIdx.y; j < cols; j += gridDim.y)
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < rows; i += (long long)gridDim.x * blockDim.x)
+      A[j * ld + i] = scale2(A[j * ld + i], e);
+}
+
+template <typename T> __global__ void k_eye(T *V, long long ld, long long n, int diag)
+{
+  for (long long j = blockIdx.y; j < n; j += gridDim.y)
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+      V[j * ld + i] = (diag && i == j) ? (T)1 : (T)0;
+}
+
+template <typename T> __global__ void k_initS(T *eS, T *fS, long long n)
+{
+  for (long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += (long long)gridDim.x * blockDim.x) {
+    eS[j] = vneg(fp<T>::inf());
+    fS[j] = (T)1;
+  }
+}
+
+// U = G diag(1/f) 2^-e, eS -= sT (src/dvjsvd.c:604-631); V * 2^-sV
+template <typename T, bool CPLX> __global__ void k_final(SvdArgs<T> a, int g3)
+{
+  const Ctl &c = a.g->ctl[g3];
+  const long long j = blockIdx.y;
+  const T f = a.fS[j];
+  const T s = vneg(a.eS[j]);
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < a.m; i += (long long)gridDim.x * blockDim.x) {
+    a.G[j * a.ldG + i] = scalef(fp<T>::div(a.G[j * a.ldG + i], f), s);
+    if (CPLX)
+      a.Gi[j * a.ldGi + i] = scalef(fp<T>::div(a.Gi[j * a.ldGi + i], f), s);
+  }
+  if (c.sV) {
+    const T sv = (T)(-c.sV);
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += (long long)gridDim.x * blockDim.x) {
+      a.V[j * a.ldV + i] = scalef(a.V[j * a.ldV + i], sv);
+      if (CPLX)
+        a.Vi[j * a.ldVi + i] = scalef(a.Vi[j * a.ldVi + i], sv);
+    }
+  }
+}
+
+template <typename T> __global__ void k_final_e(T *eS, long long n, const SvdGlobal *g, int g3)
+{
+  const T sT = (T)g->ctl[g3].sT;
+  for (long long j = (long long)blockIdx.x * blockDim.x + threadIdx.x; j < n; j += (long long)gridDim.x * blockDim.x)
+    eS[j] = eS[j] - sT;
+}
+
+// host-side (e, f) exponent of a positive finite value
+template <typename T> static int h_exp(T x)
+{
+  int e = 0;
+  (void)std::frexp((double)x, &e);
+  return e - 1;
+}
+template <typename T> static T h_scale2(T x, int n)
+{
+  return (T)std::ldexp((double)x, n);
+}
+
+static inline bool is_al(const void *p)
+{
+  return !((uintptr_t)p & 63u);
+}
+
+template <typename T, bool CPLX>
+static vj_fint svd_dev(vj_fnat m_, vj_fnat n_, T *G, vj_fnat ldG, T *Gi, vj_fnat ldGi, T *V, vj_fnat ldV, T *Vi,
+                       vj_fnat ldVi, T *eS, T *fS, const unsigned *js, unsigned stp, unsigned swp, int preset,
+                       cudaStream_t s)
+{
+  constexpr int L = svdc<T>::LANES;
+  const long long m = (long long)m_, n = (long long)n_;
+  const long long n_2 = n >> 1;
+  if (!n)
+    return 0;
+  if (m_ < n_ || (m % L))
+    return -1;
+  if ((n & 1) || (n_2 % L))
+    return -2;
+  if (!is_al(G))
+    return -3;
+  if (ldG < m_ || (ldG % L))
+    return -4;
+  if (CPLX) {
+    if (!is_al(Gi)) return -5;
+    if (ldGi < m_ || (ldGi % L)) return -6;
+    if (!is_al(V)) return -7;
+    if (ldV < n_ || (ldV % L)) return -8;
+    if (!is_al(Vi)) return -9;
+    if (ldVi < n_ || (ldVi % L)) return -10;
+  }
+  else {
+    if (!is_al(V)) return -5;
+    if (ldV < n_ || (ldV % L)) return -6;
+  }
+  if (!host::gpu_ready())
+    return VJ_ERR_NO_GPU;
+  const long long E_MG = CPLX ? -92 : -80, E_MV = CPLX ? -104 : -92, E_MVZ = CPLX ? -17 : -13;
+  host::Staging &stg = host::staging2();
+  if (!stg.reserve(sizeof(SvdGlobal) + 256))
+    return VJ_ERR_NOMEM;
+  SvdGlobal *dg = reinterpret_cast<SvdGlobal *>(stg.ptr);
+  unsigned long long *dmx = reinterpret_cast<unsigned long long *>(stg.ptr + sizeof(SvdGlobal) + 64);
+  const dim3 blk(256);
+  auto grid2 = [](long long rows, long long cols) {
+    long long gx = (rows + 255) / 256;
+    if (gx > 64) gx = 64;
+    long long gy = cols < 65535 ? cols : 65535;
+    return dim3((unsigned)gx, (unsigned)(gy > 0 ? gy : 1));
+  };
+  auto normx = [&](const T *A, long long lda, long long rows, long long cols, const T *Ai, long long ldai,
+                   T &out) -> bool {
+    if (cudaMemsetAsync(dmx, 0, 8, s) != cudaSuccess) return false;
+    k_normx<T><<<grid2(rows, cols), blk, 0, s>>>(A, lda, rows, cols, dmx);
+    if (CPLX)
+      k_normx<T><<<grid2(rows, cols), blk, 0, s>>>(Ai, ldai, rows, cols, dmx);
+    unsigned long long b = 0;
+    if (cudaMemcpyAsync(&b, dmx, 8, cudaMemcpyDeviceToHost, s) != cudaSuccess) return false;
+    if (cudaStreamSynchronize(s) != cudaSuccess) return false;
+    typename fp<T>::U u = (typename fp<T>::U)b;
+    T v;
+    memcpy(&v, &u, sizeof(T));
+    out = v;
+    return true;
+  };
+  T MG = 0, MV = 1;
+  if (!normx(G, (long long)ldG, m, n, Gi, (long long)ldGi, MG))
+    return VJ_ERR_CUDA;
+  if (!(MG <= svdc<T>::RMAX))
+    return E_MG;
+  if (preset) {
+    if (!normx(V, (long long)ldV, n, n, Vi, (long long)ldVi, MV))
+      return VJ_ERR_CUDA;
+    if (!(MV <= svdc<T>::RMAX))
+      return E_MV;
+    if (MV <= (T)0)
+      return E_MVZ;
+  }
+  else {
+    k_eye<T><<<grid2(n, n), blk, 0, s>>>(V, (long long)ldV, n, 1);
+    if (CPLX)
+      k_eye<T><<<grid2(n, n), blk, 0, s>>>(Vi, (long long)ldVi, n, 0);
+  }
+  k_initS<T><<<(unsigned)((n + 255) / 256), blk, 0, s>>>(eS, fS, n);
+  if (MG == (T)0) {
+    if (cudaStreamSynchronize(s) != cudaSuccess)
+      return VJ_ERR_CUDA;
+    return 0;
+  }
+  // setup of src/dvjsvd.c:120-156 (src/zvjsvd.c:135-171)
+  const int ROT = CPLX ? (svdc<T>::ROT_C - 1) : svdc<T>::ROT_R;
+  const T M_m = CPLX ? (svdc<T>::RMAX / ((T)((unsigned long long)m << 2u) * (T)M_SQRT2))
+                     : (svdc<T>::RMAX / (T)((unsigned long long)m << 1u));
+  const int NRM = h_exp(M_m);
+  int eM = h_exp(MG);
+  int sN = NRM - eM - 1;
+  if (sN) {
+    k_scale<T><<<grid2(m, n), blk, 0, s>>>(G, (long long)ldG, m, n, sN);
+    if (CPLX)
+      k_scale<T><<<grid2(m, n), blk, 0, s>>>(Gi, (long long)ldGi, m, n, sN);
+    MG = h_scale2(MG, sN);
+  }
+  const int sT = sN;
+  int sV = 0;
+  if (preset) {
+    eM = h_exp(MV);
+    const int sR = ROT - eM;
+    if (sR) {
+      k_scale<T><<<grid2(n, n), blk, 0, s>>>(V, (long long)ldV, n, n, sR);
+      if (CPLX)
+        k_scale<T><<<grid2(n, n), blk, 0, s>>>(Vi, (long long)ldVi, n, n, sR);
+      MV = h_scale2(MV, sR);
+    }
+    sV = sR;
+  }
+  SvdGlobal hg;
+  memset(&hg, 0, sizeof(hg));
+  hg.ctl[0].MGbase = (double)MG;
+  hg.ctl[0].MVbase = (double)MV;
+  hg.ctl[0].sT = sT;
+  hg.ctl[0].sV = sV;
+  if (cudaMemcpyAsync(dg, &hg, sizeof(hg), cudaMemcpyHostToDevice, s) != cudaSuccess)
+    return VJ_ERR_CUDA;
+  SvdArgs<T> a;
+  a.m = m; a.n = n; a.ldG = (long long)ldG; a.ldGi = (long long)ldGi; a.ldV = (long long)ldV;
+  a.ldVi = (long long)ldVi;
+  a.G = G; a.Gi = Gi; a.V = V; a.Vi = Vi; a.eS = eS; a.fS = fS; a.js = js; a.g = dg;
+  a.tol = (T)(std::sqrt((T)m) * h_scale2(svdc<T>::EPS, -1));
+  if (sizeof(T) == 4)
+    a.tol = sqrtf((float)m) * h_scale2(svdc<T>::EPS, -1);
+  a.gst = h_scale2(a.tol, (int)svdc<T>::MAX_FIN_EXP);
+  a.nrm_exp = NRM;
+  a.rot = ROT;
+  a.e_dot = CPLX ? -345 : -320;
+  a.e_doti = -347;
+  a.e_appg = CPLX ? -630 : -580;
+  a.e_appv = CPLX ? -638 : -588;
+  if (swp)
+    k_norms<T, CPLX><<<(unsigned)((n + 7) / 8), blk, 0, s>>>(a);
+  if (cudaGetLastError() != cudaSuccess)
+    return VJ_ERR_CUDA;
+  unsigned sw = 0;
+  long long gstep = 0;
+  while (sw < swp) {
+    if (cudaMemsetAsync(&dg->swt, 0, 8, s) != cudaSuccess)
+      return VJ_ERR_CUDA;
+    for (unsigned st = 0; st < stp; ++st, ++gstep) {
+      if (preset)
+        k_step<T, CPLX, true><<<(unsigned)n_2, blk, 0, s>>>(a, (int)st, (int)(gstep % 3));
+      else
+        k_step<T, CPLX, false><<<(unsigned)n_2, blk, 0, s>>>(a, (int)st, (int)(gstep % 3));
+    }
+    if (cudaGetLastError() != cudaSuccess)
+      return VJ_ERR_CUDA;
+    long long hv[2];
+    if (cudaMemcpyAsync(hv, dg, 16, cudaMemcpyDeviceToHost, s) != cudaSuccess)
+      return VJ_ERR_CUDA;
+    if (cudaStreamSynchronize(s) != cudaSuccess)
+      return VJ_ERR_CUDA;
+    if (hv[0])
+      return hv[0];
+    host::trace_sweep(sw, (unsigned long long)hv[1]);
+    if (!hv[1])
+      break;
+    ++sw;
+  }
+  if (sw < swp) {
+    dim3 gf((unsigned)((m + 255) / 256 < 16 ? (m + 255) / 256 : 16), (unsigned)n);
+    k_final<T, CPLX><<<gf, blk, 0, s>>>(a, (int)(gstep % 3));
+    k_final_e<T><<<(unsigned)((n + 255) / 256), blk, 0, s>>>(eS, n, dg, (int)(gstep % 3));
+  }
+  if (cudaStreamSynchronize(s) != cudaSuccess)
+    return VJ_ERR_CUDA;
+  return (vj_fint)sw;
+}
+
+// host-pointer form: copy in, compute, copy out (G, V, eS, fS)
+template <typename T, bool CPLX>
+static vj_fint svd_host(const vj_fnat *m, const vj_fnat *n, T *G, const vj_fnat *ldG, T *Gi, const vj_fnat *ldGi,
+                        T *V, const vj_fnat *ldV, T *Vi, const vj_fnat *ldVi, T *eS, T *fS, const unsigned *js,
+                        const unsigned *stp, const unsigned *swp, T *work, unsigned *iwork)
+{
+  constexpr int L = svdc<T>::LANES;
+  const long long mm = (long long)*m, nn = (long long)*n;
+  // the reference's argument checks, in its order (src/dvjsvd.c:43-68, src/zvjsvd.c:43-80)
+  if (!nn)
+    return 0;
+  if (*m < *n || (mm % L))
+    return -1;
+  if ((nn & 1) || ((nn >> 1) % L))
+    return -2;
+  if (!is_al(G))
+    return -3;
+  if (*ldG < *m || (*ldG % L))
+    return -4;
+  if (CPLX) {
+    if (!is_al(Gi)) return -5;
+    if (*ldGi < *m || (*ldGi % L)) return -6;
+    if (!is_al(V)) return -7;
+    if (*ldV < *n || (*ldV % L)) return -8;
+    if (!is_al(Vi)) return -9;
+    if (*ldVi < *n || (*ldVi % L)) return -10;
+    if (!is_al(work)) return -16;
+  }
+  else {
+    if (!is_al(V)) return -5;
+    if (*ldV < *n || (*ldV % L)) return -6;
+    if (!is_al(work)) return -12;
+  }
+  if (!host::gpu_ready())
+    return VJ_ERR_NO_GPU;
+  const int preset = (*iwork != 0u);
+  cudaStream_t st2[2];
+  if (!host::streams2(st2))
+    return VJ_ERR_CUDA;
+  cudaStream_t s = st2[0];
+  // device copies: G (m x n), Gi, V (n x n), Vi, eS, fS, js; compact leading dimensions
+  const size_t gsz = (size_t)mm * nn * sizeof(T), vsz = (size_t)nn * nn * sizeof(T);
+  const size_t jsz = (size_t)(*stp) * nn * sizeof(unsigned);
+  const size_t al = 256;
+  auto up = [&](size_t x) { return (x + al - 1) & ~(al - 1); };
+  const size_t total = up(gsz) * (CPLX ? 2 : 1) + up(vsz) * (CPLX ? 2 : 1) + 2 * up(nn * sizeof(T)) + up(jsz);
+  host::Staging &stg = host::staging();
+  if (!stg.reserve(total))
+    return VJ_ERR_NOMEM;
+  char *b = stg.ptr;
+  T *dG = (T *)b; b += up(gsz);
+  T *dGi = CPLX ? (T *)b : nullptr; if (CPLX) b += up(gsz);
+  T *dV = (T *)b; b += up(vsz);
+  T *dVi = CPLX ? (T *)b : nullptr; if (CPLX) b += up(vsz);
+  T *deS = (T *)b; b += up(nn * sizeof(T));
+  T *dfS = (T *)b; b += up(nn * sizeof(T));
+  unsigned *djs = (unsigned *)b;
+  const size_t ms = (size_t)mm * sizeof(T), ns = (size_t)nn * sizeof(T);
+  if (cudaMemcpy2DAsync(dG, ms, G, (size_t)*ldG * sizeof(T), ms, (size_t)nn, cudaMemcpyHostToDevice, s) != cudaSuccess)
+    return VJ_ERR_CUDA;
+  if (CPLX && cudaMemcpy2DAsync(dGi, ms, Gi, (size_t)*ldGi * sizeof(T), ms, (size_t)nn, cudaMemcpyHostToDevice, s) != cudaSuccess)
+    return VJ_ERR_CUDA;
+  if (preset) {
+    if (cudaMemcpy2DAsync(dV, ns, V, (size_t)*ldV * sizeof(T), ns, (size_t)nn, cudaMemcpyHostToDevice, s) != cudaSuccess)
+      return VJ_ERR_CUDA;
+    if (CPLX && cudaMemcpy2DAsync(dVi, ns, Vi, (size_t)*ldVi * sizeof(T), ns, (size_t)nn, cudaMemcpyHostToDevice, s) != cudaSuccess)
+      return VJ_ERR_CUDA;
+  }
+  if (jsz && cudaMemcpyAsync(djs, js, jsz, cudaMemcpyHostToDevice, s) != cudaSuccess)
+    return VJ_ERR_CUDA;
+  host::trace_reset();
+  const vj_fint r = svd_dev<T, CPLX>(*m, *n, dG, (vj_fnat)mm, dGi, (vj_fnat)mm, dV, (vj_fnat)nn, dVi, (vj_fnat)nn,
+                                     deS, dfS, djs, *stp, *swp, preset, s);
+  if (r == VJ_ERR_CUDA || r == VJ_ERR_NO_GPU || r == VJ_ERR_NOMEM)
+    return r;
+  // results (also on numerical errors: G and V then hold intermediate values)
+  if (cudaMemcpy2DAsync(G, (size_t)*ldG * sizeof(T), dG, ms, ms, (size_t)nn, cudaMemcpyDeviceToHost, s) != cudaSuccess)
+    return VJ_ERR_CUDA;
+  if (CPLX && cudaMemcpy2DAsync(Gi, (size_t)*ldGi * sizeof(T), dGi, ms, ms, (size_t)nn, cudaMemcpyDeviceToHost, s) != cudaSuccess)
+    return VJ_ERR_CUDA;
+  if (cudaMemcpy2DAsync(V, (size_t)*ldV * sizeof(T), dV, ns, ns, (size_t)nn, cudaMemcpyDeviceToHost, s) != cudaSuccess)
+    return VJ_ERR_CUDA;
+  if (CPLX && cudaMemcpy2DAsync(Vi, (size_t)*ldVi * sizeof(T), dVi, ns, ns, (size_t)nn, cudaMemcpyDeviceToHost, s) != cudaSuccess)
+    return VJ_ERR_CUDA;
+  if (cudaMemcpyAsync(eS, deS, ns, cudaMemcpyDeviceToHost, s) != cudaSuccess)
+    return VJ_ERR_CUDA;
+  if (cudaMemcpyAsync(fS, dfS, ns, cudaMemcpyDeviceToHost, s) != cudaSuccess)
+    return VJ_ERR_CUDA;
+  if (cudaStreamSynchronize(s) != cudaSuccess)
+    return VJ_ERR_CUDA;
+  return r;
+}
+
+}  // namespace vj
+
+using namespace vj;
+
+extern "C" {
+
+vj_fint dvjsvd_(const vj_fnat m[1], const vj_fnat n[1], double G[], const vj_fnat ldG[1], double V[],
+                const vj_fnat ldV[1], double eS[], double fS[], const unsigned js[], const unsigned stp[1],
+                const unsigned swp[1], double work[], unsigned iwork[])
+{
+  return svd_host<double, false>(m, n, G, ldG, nullptr, ldG, V, ldV, nullptr, ldV, eS, fS, js, stp, swp, work,
+                                 iwork);
+}
+vj_fint zvjsvd_(const vj_fnat m[1], const vj_fnat n[1], double Gr[], const vj_fnat ldGr[1], double Gi[],
+                const vj_fnat ldGi[1], double Vr[], const vj_fnat ldVr[1], double Vi[], const vj_fnat ldVi[1],
+                double eS[], double fS[], const unsigned js[], const unsigned stp[1], const unsigned swp[1],
+                double work[], unsigned iwork[])
+{
+  return svd_host<double, true>(m, n, Gr, ldGr, Gi, ldGi, Vr, ldVr, Vi, ldVi, eS, fS, js, stp, swp, work, iwork);
+}
+vj_fint svjsvd_(const vj_fnat m[1], const vj_fnat n[1], float G[], const vj_fnat ldG[1], float V[],
+                const vj_fnat ldV[1], float eS[], float fS[], const unsigned js[], const unsigned stp[1],
+                const unsigned swp[1], float work[], unsigned iwork[])
+{
+  return svd_host<float, false>(m, n, G, ldG, nullptr, ldG, V, ldV, nullptr, ldV, eS, fS, js, stp, swp, work,
+                                iwork);
+}
+vj_fint cvjsvd_(const vj_fnat m[1], const vj_fnat n[1], float Gr[], const vj_fnat ldGr[1], float Gi[],
+                const vj_fnat ldGi[1], float Vr[], const vj_fnat ldVr[1], float Vi[], const vj_fnat ldVi[1],
+                float eS[], float fS[], const unsigned js[], const unsigned stp[1], const unsigned swp[1],
+                float work[], unsigned iwork[])
+{
+  return svd_host<float, true>(m, n, Gr, ldGr, Gi, ldGi, Vr, ldVr, Vi, ldVi, eS, fS, js, stp, swp, work, iwork);
+}
+
+vj_fint vj_dvjsvd_dev(vj_fnat m, vj_fnat n, double *G, vj_fnat ldG, double *V, vj_fnat ldV, double *eS, double *fS,
+                      const unsigned *js, unsigned stp, unsigned swp, int preset, void *stream)
+{
+  return svd_dev<double, false>(m, n, G, ldG, nullptr, ldG, V, ldV, nullptr, ldV, eS, fS, js, stp, swp, preset,
+                                (cudaStream_t)stream);
+}
+vj_fint vj_zvjsvd_dev(vj_fnat m, vj_fnat n, double *Gr, vj_fnat ldGr, double *Gi, vj_fnat ldGi, double *Vr,
+                      vj_fnat ldVr, double *Vi, vj_fnat ldVi, double *eS, double *fS, const unsigned *js,
+                      unsigned stp, unsigned swp, int preset, void *stream)
+{
+  return svd_dev<double, true>(m, n, Gr, ldGr, Gi, ldGi, Vr, ldVr, Vi, ldVi, eS, fS, js, stp, swp, preset,
+                               (cudaStream_t)stream);
+}
+vj_fint vj_svjsvd_dev(vj_fnat m, vj_fnat n, float *G, vj_fnat ldG, float *V, vj_fnat ldV, float *eS, float *fS,
+                      const unsigned *js, unsigned stp, unsigned swp, int preset, void *stream)
+{
+  return svd_dev<float, false>(m, n, G, ldG, nullptr, ldG, V, ldV, nullptr, ldV, eS, fS, js, stp, swp, preset,
+                               (cudaStream_t)stream);
+}
+vj_fint vj_cvjsvd_dev(vj_fnat m, vj_fnat n, float *Gr, vj_fnat ldGr, float *Gi, vj_fnat ldGi, float *Vr,
+                      vj_fnat ldVr, float *Vi, vj_fnat ldVi, float *eS, float *fS, const unsigned *js,
+                      unsigned stp, unsigned swp, int preset, void *stream)
+{
+  return svd_dev<float, true>(m, n, Gr, ldGr, Gi, ldGi, Vr, ldVr, Vi, ldVi, eS, fS, js, stp, swp, preset,
+                              (cudaStream_t)stream);
+}
+
+}  // extern "C"

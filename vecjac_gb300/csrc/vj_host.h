@@ -1,0 +1,36 @@
+// Host-side services shared by the entry points: device discovery, a growable device
+// staging buffer for the host-pointer forms, and a pair of library-owned streams.
+#pragma once
+#include <cstddef>
+#include <cuda_runtime.h>
+
+#include "../../include/vecjac_gb300.h"
+
+namespace vj {
+namespace host {
+
+// true when a CUDA device is usable (checked once; the current device is used)
+bool gpu_ready();
+int sm_count();
+
+// device memory reused across host-API calls; grows on demand, never shrinks
+struct Staging {
+  char *ptr = nullptr;
+  size_t size = 0;
+  bool reserve(size_t bytes);
+};
+Staging &staging();
+Staging &staging2();
+
+// two non-blocking streams owned by the library
+bool streams2(cudaStream_t s[2]);
+
+// per-sweep statistics of the last SVD (transformed pairs per sweep)
+void trace_reset();
+void trace_sweep(unsigned sweep, unsigned long long rotations);
+
+// elements per chunk of a host-pointer 2x2 call (a multiple of `lanes`)
+long long bjac2_chunk(long long n, size_t elem, bool cplx, int lanes);
+
+}  // namespace host
+}  // namespace vj
