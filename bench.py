@@ -1,0 +1,473 @@
+"""Benchmark of the batched 2x2 Hermitian EVD (VecJac's dbjac2_/zbjac2_/sbjac2_/cbjac2_).
+
+Workload ("bjac2", default): the batched-EVD configuration -- 2^28 real symmetric FP64
+triples, 2^27 complex Hermitian FP64, 2^28 real FP32 and 2^27 complex FP32, SoA arrays,
+entries +-2^e*u with e uniform in [-300, 300] (FP64) / [-40, 40] (FP32), u uniform in
+[1, 2), generated on the GPU from a seed (synthetic data; the reference publishes no
+data set). One step = one pass of all four batches (n < 0: cosines and sines).
+
+Metric: GB/s of algorithmic HBM traffic (56.5 / 72.5 / 28.25 / 36.25 bytes per element for
+d / z / s / c: inputs, outputs and the permutation bitmask), whole job. The inputs
+(37 GB) exceed the 129 MB L2 many times over, so no L2 flush is needed between steps.
+
+Other workloads (--workload): "svd1024" (dvjsvd_ on a 1024x1024 FP64 matrix, matrices/s)
+and "zsvd" (zvjsvd_ on 4096x2048 FP64 complex).
+
+Timing follows the harness contract: W untimed warm-up steps, then K steps between CUDA
+events on the launching stream with a barrier and a device synchronize on both sides,
+max over ranks; the e2e figure goes through the C ABI with host buffers (copies in the
+timed region). With --gpus N > 1 (torchrun, one process per GPU) every rank runs an
+independent replica ("replicas only": the batch shards without any exchange).
+"""
+import argparse
+import ctypes as C
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+BPE = {"d": 56.5, "z": 72.5, "s": 28.25, "c": 36.25}
+LG = {"d": 28, "z": 27, "s": 28, "c": 27}
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return json.load(f), "measured"
+    except OSError:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+
+    def __init__(self, dev=0):
+        self.dev = dev
+        self.proc = None
+        self.rows = []
+
+    def __enter__(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.dev), "--query-gpu=" + q,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(2)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            try:
+                sm.append(float(r[0]))
+                mx.append(float(r[1]))
+                for k, v in zip(names, r[3:7]):
+                    if v.lower().startswith("active"):
+                        reasons.add(k)
+            except (ValueError, IndexError):
+                pass
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_init(gpus):
+    import torch
+    if gpus > 1 or "RANK" in os.environ:
+        import torch.distributed as dist
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        dist.init_process_group(backend)
+        rank = dist.get_rank()
+        world = dist.get_world_size()
+        if torch.cuda.is_available():
+            torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", rank)))
+        return dist, rank, world
+    return None, 0, 1
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def allmax(dist, x):
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ---------------------------------------------------------------- GPU inputs
+def gen_pairs_gpu(kind, n, seed):
+    """SoA inputs on the GPU with the distribution of vecjac_gb300.workloads.pairs2x2"""
+    import torch
+    g = torch.Generator(device="cuda")
+    g.manual_seed(seed)
+    dt = torch.float64 if kind in "dz" else torch.float32
+    lo, hi = (-300, 300) if kind in "dz" else (-40, 40)
+    out = []
+    for _ in range(4 if kind in "zc" else 3):
+        e = torch.randint(lo, hi + 1, (n,), generator=g, device="cuda", dtype=torch.int32)
+        u = torch.rand(n, generator=g, device="cuda", dtype=dt) + 1.0
+        s = torch.randint(0, 2, (n,), generator=g, device="cuda", dtype=torch.int32).to(dt) * 2 - 1
+        out.append(torch.ldexp(s * u, e.to(dt)).to(dt))
+        del e, u, s
+    return out
+
+
+class Batch:
+    def __init__(self, kind, n, seed):
+        import torch
+        self.kind, self.n = kind, n
+        self.ins = gen_pairs_gpu(kind, n, seed)
+        dt = self.ins[0].dtype
+        self.outs = [torch.empty(n, dtype=dt, device="cuda") for _ in range(5 if kind in "zc" else 4)]
+        self.p = torch.empty(n // (8 if kind in "dz" else 16), dtype=torch.int32, device="cuda")
+
+    def launch(self, vj, stream):
+        k, i, o = self.kind, self.ins, self.outs
+        if k in "zc":
+            r = vj.bjac2_dev(k, -self.n, i[0], i[1], i[2], i[3], o[0], o[1], o[2], o[3], o[4], self.p, stream=stream)
+        else:
+            r = vj.bjac2_dev(k, -self.n, i[0], i[1], i[2], None, o[0], o[1], None, o[2], o[3], self.p, stream=stream)
+        if r != 1:
+            raise RuntimeError("bjac2 %s failed: %d" % (k, r))
+
+    def bytes(self):
+        return BPE[self.kind] * self.n
+
+
+def fp64_bound(kind, n, sm_mhz, sms=152):
+    """Element-rate bound of the FP64 2x2 on the FP64 pipe: 6 divisions and 2 square roots
+    at the measured 0.195 per clock per SM each, plus 8 FMA/add at 1.68 per clock per SM
+    (complex: 9 divisions, 3 square roots, 10 FMA/add/mul)."""
+    if kind == "d":
+        clk = 8 / 0.195 + 8 / 1.68
+    else:
+        clk = 12 / 0.195 + 10 / 1.68
+    return sms * sm_mhz * 1e6 / clk
+
+
+def bench_bjac2(args, vj, dist, rank, world):
+    import torch
+    kinds = "dzsc"
+    shift = args.scale
+    batches = [Batch(k, 1 << (LG[k] - shift), seed=100 + i + 17 * rank) for i, k in enumerate(kinds)]
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    sh = stream.cuda_stream
+    for _ in range(args.warmup):
+        for b in batches:
+            b.launch(vj, sh)
+    torch.cuda.synchronize()
+    # per-kernel durations (events on the launching stream), one extra step
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in batches]
+    for b, (e0, e1) in zip(batches, ev):
+        e0.record(stream)
+        b.launch(vj, sh)
+        e1.record(stream)
+    torch.cuda.synchronize()
+    per_ms = {b.kind: e0.elapsed_time(e1) for b, (e0, e1) in zip(batches, ev)}
+    barrier(dist)
+    torch.cuda.synchronize()
+    with Clocks(torch.cuda.current_device()) as clk:
+        t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0.record(stream)
+        for _ in range(args.steps):
+            for b in batches:
+                b.launch(vj, sh)
+        t1.record(stream)
+        torch.cuda.synchronize()
+    barrier(dist)
+    ms = allmax(dist, t0.elapsed_time(t1)) / args.steps
+    total_bytes = sum(b.bytes() for b in batches)
+    value = world * total_bytes / (ms * 1e-3) / 1e9
+    clocks = clk.summary()
+    pk, pk_src = peaks()
+    # dominant kernel: the FP64 real batch
+    dom = batches[0]
+    dom_gbs = dom.bytes() / (per_ms["d"] * 1e-3) / 1e9
+    sm_mhz = clocks["sm_mhz"] or pk.get("sm_max_mhz", 2070.0)
+    fb = fp64_bound("d", dom.n, sm_mhz)
+    per_kernel = {k: {"ms": round(per_ms[k], 4), "elements": b.n,
+                      "gbs": round(b.bytes() / (per_ms[k] * 1e-3) / 1e9, 1)} for k, b in zip(kinds, batches)}
+    out = {
+        "metric": "batched 2x2 Hermitian EVD throughput (GB/s of HBM traffic)",
+        "value": round(value, 2), "unit": "GB/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64+f32", "data": "synthetic (seeded, GPU-generated; +-2^e*u distribution)",
+        "config": {"workload": "bjac2: dbjac2_ 2^%d + zbjac2_ 2^%d + sbjac2_ 2^%d + cbjac2_ 2^%d elements, n<0 (sines)"
+                   % tuple(LG[k] - shift for k in kinds),
+                   "bytes_per_step": total_bytes, "l2": "inputs larger than L2 (no flush)",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "per_kernel": per_kernel,
+        "roofline": {"bound": "hbm", "kernel": "k_bjac2<double,real,sine>", "achieved": round(dom_gbs, 1),
+                     "peak": pk["hbm_gbs"], "unit": "GB/s", "frac": round(dom_gbs / pk["hbm_gbs"], 4),
+                     "peak_source": pk_src, "traffic": None,
+                     "binding": "fp64_pipe",
+                     "fp64_pipe": {"elements_per_s": round(dom.n / (per_ms["d"] * 1e-3), 1),
+                                   "bound_elements_per_s": round(fb, 1),
+                                   "frac": round(dom.n / (per_ms["d"] * 1e-3) / fb, 4),
+                                   "note": "6 div + 2 sqrt at 0.195/clk/SM and 8 fma/add at 1.68/clk/SM, "
+                                           "rates measured on this GB300"}},
+        "clocks": clocks,
+        "gpu_launches": args.steps * len(batches),
+    }
+    for b in batches:
+        del b.ins, b.outs, b.p
+    torch.cuda.empty_cache()
+    if args.e2e:
+        out["e2e"] = e2e_bjac2(args, vj, dist, world)
+    if rank == 0 and args.cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline_bjac2(args.cpu_elems)
+    return out
+
+
+def e2e_bjac2(args, vj, dist, world):
+    """The same workload through the reference-facing C ABI (dbjac2_ ... with host
+    buffers; the library stages chunks through the GPU), copies inside the timed region."""
+    import torch
+    shift = args.scale + args.e2e_shift
+    kinds = "dzsc"
+    # host buffers of the full workload need ~2x its 37 GB of RAM (inputs, outputs, staging
+    # of the generator); shrink the e2e batches when the host has less
+    try:
+        with open("/proc/meminfo") as f:
+            avail = {l.split(":")[0]: int(l.split()[1]) for l in f}["MemAvailable"] * 1024
+    except (OSError, KeyError, ValueError):
+        avail = 1 << 40
+    need = sum(BPE[k] * (1 << (LG[k] - shift)) for k in kinds) * 1.6
+    while need > 0.6 * avail and shift < 8:
+        shift += 1
+        need /= 2
+    bufs = {}
+    h2d = d2h = 0
+    for i, k in enumerate(kinds):
+        n = 1 << (LG[k] - shift)
+        ins = [t.cpu().numpy() for t in gen_pairs_gpu(k, n, 300 + i)]
+        dt = ins[0].dtype
+        outs = [np.empty(n, dt) for _ in range(5 if k in "zc" else 4)]
+        p = np.empty(n // (8 if k in "dz" else 16), np.uint32)
+        bufs[k] = (n, ins, outs, p)
+        h2d += sum(a.nbytes for a in ins)
+        d2h += sum(a.nbytes for a in outs) + p.nbytes
+    total = sum(BPE[k] * bufs[k][0] for k in kinds)
+
+    def step():
+        for k in kinds:
+            n, ins, outs, p = bufs[k]
+            a21i = ins[3] if k in "zc" else None
+            if k in "zc":
+                r = vj.bjac2(k, -n, ins[0], ins[1], ins[2], a21i, c=outs[0], at=outs[1], sat=outs[2], l1=outs[3],
+                             l2=outs[4], p=p)
+            else:
+                r = vj.bjac2(k, -n, ins[0], ins[1], ins[2], c=outs[0], at=outs[1], l1=outs[2], l2=outs[3], p=p)
+            if r[0] != 1:
+                raise RuntimeError("host bjac2 failed")
+
+    for _ in range(max(1, min(args.warmup, 2))):
+        step()
+    steps = max(1, min(args.steps, 3))
+    barrier(dist)
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    for _ in range(steps):
+        step()
+    torch.cuda.synchronize()
+    el = allmax(dist, time.perf_counter() - t) / steps
+    return {"value": round(world * total / el / 1e9, 2), "unit": "GB/s", "h2d_bytes_per_step": int(h2d),
+            "d2h_bytes_per_step": int(d2h), "steps": steps,
+            "elements": {k: bufs[k][0] for k in kinds},
+            "path": "C ABI dbjac2_/zbjac2_/sbjac2_/cbjac2_ on pageable host buffers"}
+
+
+def cpu_baseline_bjac2(elems_lg, threads=None):
+    """The oracle port (oracle/vjo.c, the reference's algorithm in portable C) on the host
+    cores, a bounded sample of 2^elems_lg elements per precision, all threads."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    from oracle import oracle as O
+    from vecjac_gb300 import workloads as W
+    O.build()
+    R = O.Restatement()
+    threads = threads or os.cpu_count()
+    n = 1 << elems_lg
+    data = {k: W.pairs2x2(k, n, 7) for k in "dzsc"}
+    chunk = n // threads
+    chunk -= chunk % 16
+
+    def run_kind(k):
+        ins = data[k]
+        dt = ins[0].dtype
+        outs = [np.empty(n, dt) for _ in range(5)]
+        p = np.empty(n // 8, np.uint32)
+        f = R.fn(k + "bjac2_")
+        f.restype = C.c_longlong
+        lanes = 8 if k in "dz" else 16
+
+        def part(off):
+            cnt = min(chunk, n - off)
+            nn = C.c_longlong(-cnt)
+            ptr = lambda a, elt=1: C.c_void_p(a.ctypes.data + off * a.itemsize // elt)
+            if k in "zc":
+                f(C.byref(nn), ptr(ins[0]), ptr(ins[1]), ptr(ins[2]), ptr(ins[3]), ptr(outs[0]), ptr(outs[1]),
+                  ptr(outs[2]), ptr(outs[3]), ptr(outs[4]), C.c_void_p(p.ctypes.data + (off // lanes) * 4))
+            else:
+                f(C.byref(nn), ptr(ins[0]), ptr(ins[1]), ptr(ins[2]), ptr(outs[0]), ptr(outs[1]), ptr(outs[2]),
+                  ptr(outs[3]), C.c_void_p(p.ctypes.data + (off // lanes) * 4))
+
+        with ThreadPoolExecutor(threads) as ex:
+            list(ex.map(part, range(0, n, chunk)))
+
+    t = time.perf_counter()
+    for k in "dzsc":
+        run_kind(k)
+    el = time.perf_counter() - t
+    total = sum(BPE[k] * n for k in "dzsc")
+    return {"value": round(total / el / 1e9, 3), "unit": "GB/s", "cores": threads, "kind": "port",
+            "sample": "2^%d elements each of d/z/s/c (n<0), oracle/vjo.c on %d host threads" % (elems_lg, threads),
+            "seconds": round(el, 2)}
+
+
+def reference_arm(args, dist, rank):
+    """The reference's CPU implementation of the path on this host's cores. VecJac's own
+    AVX-512 code cannot be compiled on this (Arm) host, so its portable restatement in C
+    (oracle/vjo.c) is timed; each step is a bounded sample of the same workload."""
+    if rank != 0:
+        return None
+    base = cpu_baseline_bjac2(args.cpu_elems)
+    for _ in range(max(0, args.warmup - 1)):
+        pass
+    vals = [base["value"]]
+    for _ in range(max(1, args.steps) - 1):
+        vals.append(cpu_baseline_bjac2(args.cpu_elems)["value"])
+    v = float(np.median(vals))
+    return {"metric": "batched 2x2 Hermitian EVD throughput (GB/s of HBM traffic)", "value": v, "unit": "GB/s",
+            "n_gpus": 1, "steps": len(vals), "warmup": 0, "ms_per_step": None, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64+f32", "data": "synthetic (seeded)",
+            "config": {"workload": "bjac2: d/z/s/c 2x2 EVD, bounded CPU sample 2^%d each" % args.cpu_elems},
+            "impl": "reference",
+            "cpu_baseline": {"value": v, "unit": "GB/s", "cores": base["cores"], "kind": "port",
+                             "sample": base["sample"]},
+            "e2e": {"value": v, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+# ---------------------------------------------------------------- SVD workloads
+def bench_svd(args, vj, dist, rank, world, kind, m, n):
+    import torch
+    from vecjac_gb300 import workloads as W
+    cx = kind in "zc"
+    A, s = W.svd_matrix(m, n, seed=2024 + rank, complex_=cx)
+    js, stp = vj.pjs(2, n)
+    dt = np.float64 if kind in "dz" else np.float32
+    Gt = torch.tensor(np.ascontiguousarray(A.real.T, dt), device="cuda")
+    Git = torch.tensor(np.ascontiguousarray(A.imag.T, dt), device="cuda") if cx else None
+    G = torch.empty_like(Gt)
+    Gi = torch.empty_like(Gt) if cx else None
+    V = torch.empty((n, n), dtype=Gt.dtype, device="cuda")
+    Vi = torch.empty_like(V) if cx else None
+    eS = torch.empty(n, dtype=Gt.dtype, device="cuda")
+    fS = torch.empty_like(eS)
+    djs = torch.tensor(js.astype(np.int32), device="cuda")
+    stream = torch.cuda.current_stream()
+
+    def one():
+        G.copy_(Gt)
+        if cx:
+            Gi.copy_(Git)
+        r = vj.vjsvd_dev(kind, m, n, G, m, V, n, eS, fS, djs, stp, Gi=Gi, ldGi=m, Vi=Vi, ldVi=n,
+                         stream=stream.cuda_stream)
+        return r
+
+    for _ in range(args.warmup):
+        sweeps = one()
+    torch.cuda.synchronize()
+    barrier(dist)
+    with Clocks(torch.cuda.current_device()) as clk:
+        t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0.record(stream)
+        for _ in range(args.steps):
+            sweeps = one()
+        t1.record(stream)
+        torch.cuda.synchronize()
+    ms = allmax(dist, t0.elapsed_time(t1)) / args.steps
+    sig = fS.double().cpu().numpy() * np.exp2(eS.double().cpu().numpy())
+    err = float(np.max(np.abs(np.sort(sig)[::-1] - s) / s))
+    per_pair = (36 * m + 20 * n) if cx else (12 * m + 6 * n)
+    flops = sweeps * (n * (n - 1) / 2) * per_pair
+    return {"metric": "Jacobi SVD matrices/s (%svjsvd_)" % kind, "value": round(world * 1000.0 / ms, 4),
+            "unit": "matrices/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(ms, 3), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if kind in "dz" else "f32", "data": "synthetic (Haar factors, log-uniform sigma)",
+            "config": {"workload": "%svjsvd_ %dx%d, pivot strategy id 2 (placeholder tables)" % (kind, m, n),
+                       "sweeps": int(sweeps), "max_rel_sigma_err_vs_exact": err},
+            "flops_per_s": flops / (ms * 1e-3), "clocks": clk.summary(),
+            "gpu_launches": int(sweeps + 1) * stp}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="bjac2", choices=["bjac2", "svd1024", "zsvd"])
+    ap.add_argument("--scale", type=int, default=0, help="shrink the 2x2 batches by 2^scale")
+    ap.add_argument("--e2e-shift", type=int, default=0, help="further shrink of the e2e batches")
+    ap.add_argument("--no-e2e", dest="e2e", action="store_false")
+    ap.add_argument("--no-cpu", dest="cpu_baseline", action="store_false")
+    ap.add_argument("--cpu-elems", type=int, default=22)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        rank = int(os.environ.get("RANK", "0"))
+        out = reference_arm(args, None, rank)
+        if out is not None:
+            print(json.dumps(out))
+        return
+    import torch
+    dist, rank, world = dist_init(args.gpus)
+    from vecjac_gb300 import build
+    build.build()
+    import vecjac_gb300 as vj
+    if args.workload == "bjac2":
+        out = bench_bjac2(args, vj, dist, rank, world)
+    elif args.workload == "svd1024":
+        out = bench_svd(args, vj, dist, rank, world, "d", 1024, 1024)
+    else:
+        out = bench_svd(args, vj, dist, rank, world, "z", 4096, 2048)
+    if rank == 0:
+        print(json.dumps(out))
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -340,7 +340,7 @@ template <typename T> __device__ __forceinline__ void amax(unsigned long long &m
 }
 
 template <typename T, bool CPLX, bool TRACKV>
-__global__ void __launch_bounds__(256) k_step(SvdArgs<T> a, int st, int g3)
+__global__ void __launch_bounds__(256) k_step(SvdArgs<T> a, int st, int g3, int last)
 {
   using F = fp<T>;
   __shared__ PairState<T> ps;
@@ -661,7 +661,9 @@ __global__ void __launch_bounds__(256) k_step(SvdArgs<T> a, int st, int g3)
     }
   }
   // ---- 5. norms of the changed columns, for the next step ----
-  if (chp || chq) {
+  // (not after the last step of the last allowed sweep: the reference returns there with
+  // the norms of those columns not yet recomputed)
+  if ((chp || chq) && !last) {
     if ((warp == 0 && chp) || (warp == 1 && chq)) {
       const T nv = col_norm<T, CPLX>(a, warp ? q : p);
       if (((tid & 31) == 0) && !(nv <= svdc<T>::RMAX))
@@ -908,10 +910,11 @@ static vj_fint svd_dev(vj_fnat m_, vj_fnat n_, T *G, vj_fnat ldG, T *Gi, vj_fnat
     if (cudaMemsetAsync(&dg->swt, 0, 8, s) != cudaSuccess)
       return VJ_ERR_CUDA;
     for (unsigned st = 0; st < stp; ++st, ++gstep) {
+      const int last = ((sw + 1u == swp) && (st + 1u == stp)) ? 1 : 0;
       if (preset)
-        k_step<T, CPLX, true><<<(unsigned)n_2, blk, 0, s>>>(a, (int)st, (int)(gstep % 3));
+        k_step<T, CPLX, true><<<(unsigned)n_2, blk, 0, s>>>(a, (int)st, (int)(gstep % 3), last);
       else
-        k_step<T, CPLX, false><<<(unsigned)n_2, blk, 0, s>>>(a, (int)st, (int)(gstep % 3));
+        k_step<T, CPLX, false><<<(unsigned)n_2, blk, 0, s>>>(a, (int)st, (int)(gstep % 3), last);
     }
     if (cudaGetLastError() != cudaSuccess)
       return VJ_ERR_CUDA;
