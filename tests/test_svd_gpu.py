@@ -127,7 +127,7 @@ def test_properties_large(vj, kind, m, n):
     from vecjac_gb300 import workloads as W
     cx = kind in "zc"
     A, s = W.svd_matrix(m, n, seed=77, lo=-3.0, complex_=cx)
-    js, stp = vj.pjs(2, n)
+    js, stp = vj.pjs(4, n)
     kw = dict(Gi=A.imag) if cx else {}
     r = vj.vjsvd(kind, A.real, js, stp, **kw)
     assert 0 < r[0] < 999

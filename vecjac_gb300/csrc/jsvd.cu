@@ -102,6 +102,47 @@ __device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long v)
   return v;
 }
 
+// ---- TMA (cp.async.bulk) staging of a column pair into shared memory ----
+__device__ __forceinline__ unsigned smem_u32(const void *p)
+{
+  return (unsigned)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(unsigned long long *bar, unsigned count)
+{
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long *bar, unsigned bytes)
+{
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void tma_load_1d(void *dst, const void *src, unsigned bytes, unsigned long long *bar)
+{
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_u32(dst)),
+               "l"(src), "r"(bytes), "r"(smem_u32(bar))
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long *bar, unsigned phase)
+{
+  unsigned ok;
+  asm volatile(
+      "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(phase)
+      : "memory");
+  return ok != 0u;
+}
+// bounded wait on phase 0 of the barrier; false after the iteration limit
+__device__ __forceinline__ bool mbar_wait_bounded(unsigned long long *bar)
+{
+  for (unsigned it = 0; it < (1u << 22); ++it)
+    if (mbar_try_wait(bar, 0u))
+      return true;
+  return false;
+}
+
 // (e, f) of a norm d: d = f 2^e, f in [1,2) (src/dznrm2.h:4-23)
 template <typename T> __device__ __forceinline__ void ef_split(T d, T &e, T &f)
 {
@@ -164,7 +205,24 @@ template <typename T> __device__ __forceinline__ T vhypot(T x, T y)
   return z * M_;
 }
 
-// norm of column c (real, or complex with planes) by one warp; writes eS/fS; returns d
+// norm of column c (real, or complex with planes) by one warp; writes eS/fS; returns d.
+// xr/xi point to the column (in global or in shared memory).
+template <typename T, bool CPLX> __device__ T col_norm_at(const SvdArgs<T> &a, long long c, const T *xr, const T *xi)
+{
+  T d = warp_nrm2(xr, a.m);
+  if (CPLX) {
+    const T di = warp_nrm2(xi, a.m);
+    d = vhypot(d, di);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    T e, f;
+    ef_split(d, e, f);
+    a.eS[c] = e;
+    a.fS[c] = f;
+  }
+  return d;
+}
+
 template <typename T, bool CPLX> __device__ T col_norm(const SvdArgs<T> &a, long long c)
 {
   T d = warp_nrm2(a.G + c * a.ldG, a.m);
@@ -213,12 +271,11 @@ template <int LANES, typename T> __device__ __forceinline__ T hsum(T v)
 
 // scaled compensated dot products (src/ddpscl.c / src/zdpscl.c) by warp 0; x = G_q, y = G_p
 template <typename T, bool CPLX>
-__device__ void pair_dot(const SvdArgs<T> &a, long long p, long long q, T ex, T ey, T fx, T fy, T &zr, T &zi)
+__device__ void pair_dot(const SvdArgs<T> &a, const T *xr, const T *xi, const T *yr, const T *yi, T ex, T ey, T fx,
+                         T fy, T &zr, T &zi)
 {
   constexpr int L = svdc<T>::LANES;
   const int lane = threadIdx.x & 31;
-  const T *xr = a.G + q * a.ldG, *yr = a.G + p * a.ldG;
-  const T *xi = CPLX ? (a.Gi + q * a.ldGi) : nullptr, *yi = CPLX ? (a.Gi + p * a.ldGi) : nullptr;
   const int nx = -(int)ex, ny = -(int)ey;
   T sr = 0, tr = 0, sr_ = 0, tr_ = 0, si = 0, ti = 0, si_ = 0, ti_ = 0;
   if (lane < L) {
@@ -339,13 +396,15 @@ template <typename T> __device__ __forceinline__ void amax(unsigned long long &m
   m = (b > m) ? b : m;
 }
 
-template <typename T, bool CPLX, bool TRACKV>
+template <typename T, bool CPLX, bool TRACKV, bool STAGE>
 __global__ void __launch_bounds__(256) k_step(SvdArgs<T> a, int st, int g3, int last)
 {
   using F = fp<T>;
+  extern __shared__ __align__(128) unsigned char smem_raw[];
   __shared__ PairState<T> ps;
   __shared__ unsigned long long red[8][4];
   __shared__ int s_err;
+  __shared__ unsigned long long bar;
   SvdGlobal *const g = a.g;
   if (*(volatile long long *)&g->err)
     return;
@@ -367,6 +426,9 @@ __global__ void __launch_bounds__(256) k_step(SvdArgs<T> a, int st, int g3, int 
   }
   if (tid == 0)
     s_err = 0;
+  T *Gp = a.G + p * a.ldG, *Gq = a.G + q * a.ldG, *Vp = a.V + p * a.ldV, *Vq = a.V + q * a.ldV;
+  T *Gip = CPLX ? (a.Gi + p * a.ldGi) : nullptr, *Giq = CPLX ? (a.Gi + q * a.ldGi) : nullptr;
+  T *Vip = CPLX ? (a.Vi + p * a.ldVi) : nullptr, *Viq = CPLX ? (a.Vi + q * a.ldVi) : nullptr;
   // ---- 1. rescaling (rare) ----
   if (d.gres || d.ovf) {
     const int e = d.gres ? d.sNg : d.sNv;
@@ -392,13 +454,46 @@ __global__ void __launch_bounds__(256) k_step(SvdArgs<T> a, int st, int g3, int 
     if (CPLX)
       scale_cols(a.Vi, a.ldVi, a.n, p, q, d.sNv);
   }
+  // ---- stage the two columns of G in shared memory (TMA bulk copies) ----
+  T *rp = Gp, *rq = Gq, *rpi = Gip, *rqi = Giq;
+  if (STAGE) {
+    T *sm = reinterpret_cast<T *>(smem_raw);
+    rp = sm;
+    rq = sm + a.m;
+    if (CPLX) {
+      rpi = sm + 2 * a.m;
+      rqi = sm + 3 * a.m;
+    }
+    if (tid == 0)
+      mbar_init(&bar, 1u);
+    __syncthreads();
+    if (tid == 0) {
+      const unsigned colb = (unsigned)(a.m * (long long)sizeof(T));
+      mbar_expect_tx(&bar, colb * (CPLX ? 4u : 2u));
+      const T *src[4] = {Gp, Gq, Gip, Giq};
+      T *dst[4] = {rp, rq, rpi, rqi};
+      for (int c = 0; c < (CPLX ? 4 : 2); ++c)
+        for (unsigned off = 0; off < colb; off += 32768u) {
+          const unsigned b = (colb - off < 32768u) ? (colb - off) : 32768u;
+          tma_load_1d(reinterpret_cast<char *>(dst[c]) + off, reinterpret_cast<const char *>(src[c]) + off, b, &bar);
+        }
+    }
+    if (!mbar_wait_bounded(&bar)) {
+      // the copies did not land within the limit: flag it, give them another bounded
+      // wait, and leave without touching the matrix
+      if (tid == 0)
+        atomicMin((long long *)&g->err, (long long)VJ_ERR_CUDA);
+      (void)mbar_wait_bounded(&bar);
+      return;
+    }
+  }
   __syncthreads();
   // ---- 2. the scaled dot product (warp 0) ----
   if (warp == 0) {
     const T ep = a.eS[p], fp_ = a.fS[p], eq = a.eS[q], fq = a.fS[q];
     T zr = 0, zi = 0;
     if ((eq >= -svdc<T>::RMAX) && (ep >= -svdc<T>::RMAX))
-      pair_dot<T, CPLX>(a, p, q, eq, ep, fq, fp_, zr, zi);
+      pair_dot<T, CPLX>(a, rq, rqi, rp, rpi, eq, ep, fq, fp_, zr, zi);
     if (tid == 0) {
       ps.ep = ep; ps.fp = fp_; ps.eq = eq; ps.fq = fq;
       ps.a21r = zr;
@@ -475,20 +570,17 @@ __global__ void __launch_bounds__(256) k_step(SvdArgs<T> a, int st, int g3, int 
   __syncthreads();
   if (ps.skip)
     return;
-  // ---- 4. apply ----
+  // ---- 4. apply; G is read from the staged copy, written to HBM (and to the copy) ----
   const int code = ps.code;
-  T *Gp = a.G + p * a.ldG, *Gq = a.G + q * a.ldG, *Vp = a.V + p * a.ldV, *Vq = a.V + q * a.ldV;
-  T *Gip = CPLX ? (a.Gi + p * a.ldGi) : nullptr, *Giq = CPLX ? (a.Gi + q * a.ldGi) : nullptr;
-  T *Vip = CPLX ? (a.Vi + p * a.ldVi) : nullptr, *Viq = CPLX ? (a.Vi + q * a.ldVi) : nullptr;
-  unsigned long long mG = 0ull, mV = 0ull, mp = 0ull, mq = 0ull, mpi = 0ull, mqi = 0ull;
-  bool chp = false, chq = false, vtouch = false;
-  T tVneg = (T)0;  // a negative tV (the reference's "should never happen" codes) only feeds a max
+  unsigned long long mG = 0ull, mV = 0ull, mq = 0ull, mqi = 0ull;
+  bool chp = false, chq = false;
   if (code == 1) {
   }
   else if (code == -1) {
     for (long long i = tid; i < a.m; i += blockDim.x) {
-      T t = Gp[i]; Gp[i] = Gq[i]; Gq[i] = t;
-      if (CPLX) { t = Gip[i]; Gip[i] = Giq[i]; Giq[i] = t; }
+      const T x = rp[i], y = rq[i];
+      Gp[i] = y; Gq[i] = x;
+      if (CPLX) { const T xi = rpi[i], yi = rqi[i]; Gip[i] = yi; Giq[i] = xi; }
     }
     for (long long i = tid; i < a.n; i += blockDim.x) {
       T t = Vp[i]; Vp[i] = Vq[i]; Vq[i] = t;
@@ -506,20 +598,21 @@ __global__ void __launch_bounds__(256) k_step(SvdArgs<T> a, int st, int g3, int 
       const T tfi = CPLX ? (ps.a21i * ff) : (T)0;
       for (long long i = tid; i < a.m; i += blockDim.x) {
         if (CPLX) {
-          const T xri_ = scale2(Gp[i], nx), xii_ = scale2(Gip[i], nx);
-          const T yri_ = scale2(Gq[i], ny), yii_ = scale2(Giq[i], ny);
+          const T xri_ = scale2(rp[i], nx), xii_ = scale2(rpi[i], nx);
+          const T yri_ = scale2(rq[i], ny), yii_ = scale2(rqi[i], ny);
           const T xr = F::fma_(tfr, xri_, F::fma_(vneg(tfi), xii_, yri_));
           const T xi = F::fma_(tfr, xii_, F::fma_(tfi, xri_, yii_));
           const T ur = scale2(xr, py), ui = scale2(xi, py);
-          Gq[i] = ur;
-          Giq[i] = ui;
+          Gq[i] = ur; Giq[i] = ui;
+          rq[i] = ur; rqi[i] = ui;
           amax(mq, ur); amax(mqi, ui);
         }
         else {
-          const T xi = scale2(Gp[i], nx);
-          const T yi = scale2(Gq[i], ny);
+          const T xi = scale2(rp[i], nx);
+          const T yi = scale2(rq[i], ny);
           const T u = scale2(F::fma_(tfr, xi, yi), py);
           Gq[i] = u;
+          rq[i] = u;
           amax(mq, u);
         }
       }
@@ -531,23 +624,25 @@ __global__ void __launch_bounds__(256) k_step(SvdArgs<T> a, int st, int g3, int 
       const T tfi = CPLX ? (vneg(ps.a21i) * ff) : (T)0;
       for (long long i = tid; i < a.m; i += blockDim.x) {
         if (CPLX) {
-          const T yri = Gq[i], yii = Giq[i], xri = Gp[i], xii = Gip[i];
-          Gp[i] = yri;
-          Gip[i] = yii;
+          const T yri = rq[i], yii = rqi[i], xri = rp[i], xii = rpi[i];
+          Gp[i] = yri; Gip[i] = yii;
+          rp[i] = yri; rpi[i] = yii;
           const T yri_ = scale2(yri, ny), yii_ = scale2(yii, ny);
           const T xri_ = scale2(xri, nx), xii_ = scale2(xii, nx);
           const T vr = F::fma_(tfr, yri_, F::fma_(vneg(tfi), yii_, xri_));
           const T vi = F::fma_(tfr, yii_, F::fma_(tfi, yri_, xii_));
           const T ur = scale2(vr, px), ui = scale2(vi, px);
-          Gq[i] = ur;
-          Giq[i] = ui;
+          Gq[i] = ur; Giq[i] = ui;
+          rq[i] = ur; rqi[i] = ui;
           amax(mq, ur); amax(mqi, ui);
         }
         else {
-          const T xi = Gp[i], yi = Gq[i];
+          const T xi = rp[i], yi = rq[i];
           Gp[i] = yi;
+          rp[i] = yi;
           const T u = scale2(F::fma_(tfr, scale2(yi, ny), scale2(xi, nx)), px);
           Gq[i] = u;
+          rq[i] = u;
           amax(mq, u);
         }
       }
@@ -575,26 +670,26 @@ __global__ void __launch_bounds__(256) k_step(SvdArgs<T> a, int st, int g3, int 
       // c == 1: identity (or a swap when permuting); c != 1 "never happens" (-4 / -10)
       if (cone && perm) {
         for (long long i = tid; i < a.m; i += blockDim.x) {
-          T t = Gp[i]; Gp[i] = Gq[i]; Gq[i] = t;
-          if (CPLX) { t = Gip[i]; Gip[i] = Giq[i]; Giq[i] = t; }
+          const T x = rp[i], y = rq[i];
+          Gp[i] = y; Gq[i] = x; rp[i] = y; rq[i] = x;
+          if (CPLX) { const T xi = rpi[i], yi = rqi[i]; Gip[i] = yi; Giq[i] = xi; rpi[i] = yi; rqi[i] = xi; }
         }
         for (long long i = tid; i < a.n; i += blockDim.x) {
           T t = Vp[i]; Vp[i] = Vq[i]; Vq[i] = t;
           if (CPLX) { t = Vip[i]; Vip[i] = Viq[i]; Viq[i] = t; }
         }
       }
-      else if (!cone)
-        tVneg = (T)-4;
     }
     else if (real_rot) {
       for (int pl = 0; pl < (CPLX ? 2 : 1); ++pl) {
-        T *X = pl ? Gip : Gp, *Y = pl ? Giq : Gq;
+        T *X = pl ? Gip : Gp, *Y = pl ? Giq : Gq, *RX = pl ? rpi : rp, *RY = pl ? rqi : rq;
         for (long long i = tid; i < a.m; i += blockDim.x) {
-          const T x = X[i], y = Y[i];
+          const T x = RX[i], y = RY[i];
           T xr = perm ? F::fma_(vneg(x), at, y) : F::fma_(y, at, x);
           T yr = perm ? F::fma_(y, at, x) : F::fma_(vneg(x), at, y);
           if (!cone) { xr = xr * c; yr = yr * c; }
           X[i] = xr; Y[i] = yr;
+          RX[i] = xr; RY[i] = yr;
           amax(mG, xr); amax(mG, yr);
         }
         T *XV = pl ? Vip : Vp, *YV = pl ? Viq : Vq;
@@ -607,17 +702,16 @@ __global__ void __launch_bounds__(256) k_step(SvdArgs<T> a, int st, int g3, int 
           if (TRACKV) { amax(mV, xr); amax(mV, yr); }
         }
       }
-      chp = chq = true;
-      vtouch = true;
     }
     else {
       const T cta = at, sta = sat, cna = vneg(at);
       for (int mat = 0; mat < 2; ++mat) {
         T *Xr = mat ? Vp : Gp, *Xi = mat ? Vip : Gip, *Yr = mat ? Vq : Gq, *Yi = mat ? Viq : Giq;
+        const T *Rxr = mat ? Vp : rp, *Rxi = mat ? Vip : rpi, *Ryr = mat ? Vq : rq, *Ryi = mat ? Viq : rqi;
         const long long rows = mat ? a.n : a.m;
         unsigned long long &mm = mat ? mV : mG;
         for (long long i = tid; i < rows; i += blockDim.x) {
-          const T x_r = Xr[i], x_i = Xi[i], y_r = Yr[i], y_i = Yi[i];
+          const T x_r = Rxr[i], x_i = Rxi[i], y_r = Ryr[i], y_i = Ryi[i];
           T ar = F::fma_(y_r, cta, F::fma_(vneg(y_i), sta, x_r));
           T ai = F::fma_(y_r, sta, F::fma_(y_i, cta, x_i));
           T br = F::fma_(x_r, cna, F::fma_(vneg(x_i), sta, y_r));
@@ -625,15 +719,15 @@ __global__ void __launch_bounds__(256) k_step(SvdArgs<T> a, int st, int g3, int 
           if (!cone) { ar = ar * c; ai = ai * c; br = br * c; bi = bi * c; }
           if (perm) { Yr[i] = ar; Yi[i] = ai; Xr[i] = br; Xi[i] = bi; }
           else { Xr[i] = ar; Xi[i] = ai; Yr[i] = br; Yi[i] = bi; }
+          if (!mat) {
+            if (perm) { rq[i] = ar; rqi[i] = ai; rp[i] = br; rpi[i] = bi; }
+            else { rp[i] = ar; rpi[i] = ai; rq[i] = br; rqi[i] = bi; }
+          }
           if (!mat || TRACKV) { amax(mm, ar); amax(mm, ai); amax(mm, br); amax(mm, bi); }
         }
       }
-      chp = chq = true;
-      vtouch = true;
     }
   }
-  (void)vtouch;
-  (void)tVneg;
   // block max of |G| and |V| updates
   mG = warp_max_u64(mG);
   mV = warp_max_u64(mV);
@@ -665,7 +759,7 @@ __global__ void __launch_bounds__(256) k_step(SvdArgs<T> a, int st, int g3, int 
   // the norms of those columns not yet recomputed)
   if ((chp || chq) && !last) {
     if ((warp == 0 && chp) || (warp == 1 && chq)) {
-      const T nv = col_norm<T, CPLX>(a, warp ? q : p);
+      const T nv = warp ? col_norm_at<T, CPLX>(a, q, rq, rqi) : col_norm_at<T, CPLX>(a, p, rp, rpi);
       if (((tid & 31) == 0) && !(nv <= svdc<T>::RMAX))
         atomicOr(&nxt.ovf, 1);
     }
@@ -904,6 +998,13 @@ static vj_fint svd_dev(vj_fnat m_, vj_fnat n_, T *G, vj_fnat ldG, T *Gi, vj_fnat
     k_norms<T, CPLX><<<(unsigned)((n + 7) / 8), blk, 0, s>>>(a);
   if (cudaGetLastError() != cudaSuccess)
     return VJ_ERR_CUDA;
+  // stage each pair's columns of G in shared memory when they fit (160 KiB per CTA)
+  const size_t smem = (size_t)m * sizeof(T) * (CPLX ? 4u : 2u);
+  const bool stage = (smem <= (size_t)160 * 1024);
+  if (stage && smem > 48 * 1024) {
+    cudaFuncSetAttribute(k_step<T, CPLX, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(k_step<T, CPLX, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  }
   unsigned sw = 0;
   long long gstep = 0;
   while (sw < swp) {
@@ -911,10 +1012,19 @@ static vj_fint svd_dev(vj_fnat m_, vj_fnat n_, T *G, vj_fnat ldG, T *Gi, vj_fnat
       return VJ_ERR_CUDA;
     for (unsigned st = 0; st < stp; ++st, ++gstep) {
       const int last = ((sw + 1u == swp) && (st + 1u == stp)) ? 1 : 0;
-      if (preset)
-        k_step<T, CPLX, true><<<(unsigned)n_2, blk, 0, s>>>(a, (int)st, (int)(gstep % 3), last);
-      else
-        k_step<T, CPLX, false><<<(unsigned)n_2, blk, 0, s>>>(a, (int)st, (int)(gstep % 3), last);
+      const int g3 = (int)(gstep % 3);
+      if (stage) {
+        if (preset)
+          k_step<T, CPLX, true, true><<<(unsigned)n_2, blk, smem, s>>>(a, (int)st, g3, last);
+        else
+          k_step<T, CPLX, false, true><<<(unsigned)n_2, blk, smem, s>>>(a, (int)st, g3, last);
+      }
+      else {
+        if (preset)
+          k_step<T, CPLX, true, false><<<(unsigned)n_2, blk, 0, s>>>(a, (int)st, g3, last);
+        else
+          k_step<T, CPLX, false, false><<<(unsigned)n_2, blk, 0, s>>>(a, (int)st, g3, last);
+      }
     }
     if (cudaGetLastError() != cudaSuccess)
       return VJ_ERR_CUDA;
