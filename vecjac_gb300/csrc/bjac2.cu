@@ -132,9 +132,10 @@ static vj_fint bjac2_dev(vj_fint n, int internal, const T *a11, const T *a22, co
   return (e == cudaSuccess) ? 1 : VJ_ERR_CUDA;
 }
 
-// Host-pointer form: chunks of the batch are staged through device buffers on two
-// streams (copy in, compute, copy out), so that the copies of one chunk overlap the
-// kernel of the other.
+// Host-pointer form. Where the GPU can address pageable host memory the kernel runs on
+// the caller's arrays; otherwise chunks of the batch are staged through device buffers on
+// two streams (copy in, compute, copy out), so that the copies of one chunk overlap the
+// kernel of the other. VJ_STAGED=1 in the environment forces the staged form.
 template <typename T, bool CPLX>
 static vj_fint bjac2_host(vj_fint n, int internal, const T *a11, const T *a22, const T *a21r, const T *a21i, T *c,
                           T *cat, T *sat, T *l1, T *l2, unsigned *p)
@@ -147,6 +148,20 @@ static vj_fint bjac2_host(vj_fint n, int internal, const T *a11, const T *a22, c
   const long long nn = (n < 0) ? -n : n;
   if (!nn)
     return 1;
+  // On a GPU that reads and writes pageable host memory coherently (Grace-Blackwell:
+  // NVLink-C2C with address translation), the kernel streams the caller's arrays
+  // directly: no staging copies, and the link is the only bound.
+  auto al16 = [](const void *q) { return q == nullptr || !((uintptr_t)q & 15u); };
+  if (host::pageable_access() && al16(a11) && al16(a22) && al16(a21r) && al16(a21i) && al16(c) && al16(cat) &&
+      al16(sat) && al16(l1) && al16(l2)) {
+    cudaStream_t st[2];
+    if (!host::streams2(st))
+      return VJ_ERR_CUDA;
+    const vj_fint r = bjac2_dev<T, CPLX>(n, internal, a11, a22, a21r, a21i, c, cat, sat, l1, l2, p, st[0]);
+    if (r < 0)
+      return r;
+    return (cudaStreamSynchronize(st[0]) == cudaSuccess) ? 1 : VJ_ERR_CUDA;
+  }
   const long long chunk = host::bjac2_chunk(nn, sizeof(T), CPLX, LANES);
   const int nin = CPLX ? 4 : 3, nout = CPLX ? 5 : 4;
   const T *hin[4] = {a11, a22, a21r, a21i};

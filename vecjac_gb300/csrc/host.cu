@@ -1,3 +1,4 @@
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 
@@ -26,6 +27,22 @@ int sm_count()
       n = 1;
   }
   return n;
+}
+
+bool pageable_access()
+{
+  static int v = -1;
+  if (v < 0) {
+    int dev = 0, a = 0;
+    cudaGetDevice(&dev);
+    if (cudaDeviceGetAttribute(&a, cudaDevAttrPageableMemoryAccess, dev) != cudaSuccess)
+      a = 0;
+    const char *e = getenv("VJ_STAGED");
+    if (e && *e == '1')
+      a = 0;
+    v = a ? 1 : 0;
+  }
+  return v == 1;
 }
 
 bool Staging::reserve(size_t bytes)

@@ -251,13 +251,27 @@ template <typename T> __device__ __forceinline__ void two_sum(T a, T b, T &s, T 
   t = a_ + b_;
 }
 
+// The same (s, t) as 2Sum with half the floating-point operations: for |a| >= |b|,
+// Dekker's Fast2Sum (s = a + b, t = b - (s - a)) also yields the exact rounding error, and
+// the error of a rounded sum is unique, so both transformations agree bit for bit while
+// the accumulators stay finite (they are bounded by 4m here). The magnitude test and the
+// operand swap run on the integer pipes.
+template <typename T> __device__ __forceinline__ void fast_two_sum(T a, T b, T &s, T &t)
+{
+  const bool sw = absbits(b) > absbits(a);
+  const T hi = sw ? b : a, lo = sw ? a : b;
+  const T s_ = hi + lo;
+  s = s_;
+  t = lo - (s_ - hi);
+}
+
 // one compensated product-accumulate step (src/ddpscl.c:51-60, MUL2SUM src/zdpscl.c)
 template <typename T> __device__ __forceinline__ void mul2sum(T x, T y, T &s, T &t, T &s_, T &t_)
 {
   const T xy = fp<T>::mul_rd(x, y);
   const T xy_ = fp<T>::fma_(x, y, vneg(xy));
-  two_sum(s, xy + t, s, t);
-  two_sum(s_, xy_ + t_, s_, t_);
+  fast_two_sum(s, xy + t, s, t);
+  fast_two_sum(s_, xy_ + t_, s_, t_);
 }
 
 // halving tree over the LANES lanes of warp 0 (GCC's _mm512_reduce_add order); lane 0 has it
@@ -681,25 +695,29 @@ __global__ void __launch_bounds__(256) k_step(SvdArgs<T> a, int st, int g3, int 
       }
     }
     else if (real_rot) {
+      // the permuted form writes (y - t x) c to x and (x + t y) c to y: the same two
+      // products with the destinations exchanged
       for (int pl = 0; pl < (CPLX ? 2 : 1); ++pl) {
         T *X = pl ? Gip : Gp, *Y = pl ? Giq : Gq, *RX = pl ? rpi : rp, *RY = pl ? rqi : rq;
+        T *DX = perm ? Y : X, *DY = perm ? X : Y, *RDX = perm ? RY : RX, *RDY = perm ? RX : RY;
         for (long long i = tid; i < a.m; i += blockDim.x) {
           const T x = RX[i], y = RY[i];
-          T xr = perm ? F::fma_(vneg(x), at, y) : F::fma_(y, at, x);
-          T yr = perm ? F::fma_(y, at, x) : F::fma_(vneg(x), at, y);
-          if (!cone) { xr = xr * c; yr = yr * c; }
-          X[i] = xr; Y[i] = yr;
-          RX[i] = xr; RY[i] = yr;
-          amax(mG, xr); amax(mG, yr);
+          T u = F::fma_(y, at, x);
+          T w = F::fma_(vneg(x), at, y);
+          if (!cone) { u = u * c; w = w * c; }
+          DX[i] = u; DY[i] = w;
+          RDX[i] = u; RDY[i] = w;
+          amax(mG, u); amax(mG, w);
         }
         T *XV = pl ? Vip : Vp, *YV = pl ? Viq : Vq;
+        T *DXV = perm ? YV : XV, *DYV = perm ? XV : YV;
         for (long long i = tid; i < a.n; i += blockDim.x) {
           const T x = XV[i], y = YV[i];
-          T xr = perm ? F::fma_(vneg(x), at, y) : F::fma_(y, at, x);
-          T yr = perm ? F::fma_(y, at, x) : F::fma_(vneg(x), at, y);
-          if (!cone) { xr = xr * c; yr = yr * c; }
-          XV[i] = xr; YV[i] = yr;
-          if (TRACKV) { amax(mV, xr); amax(mV, yr); }
+          T u = F::fma_(y, at, x);
+          T w = F::fma_(vneg(x), at, y);
+          if (!cone) { u = u * c; w = w * c; }
+          DXV[i] = u; DYV[i] = w;
+          if (TRACKV) { amax(mV, u); amax(mV, w); }
         }
       }
     }

@@ -12,6 +12,8 @@ namespace host {
 // true when a CUDA device is usable (checked once; the current device is used)
 bool gpu_ready();
 int sm_count();
+// the device can read and write pageable host memory (and VJ_STAGED is not set)
+bool pageable_access();
 
 // device memory reused across host-API calls; grows on demand, never shrinks
 struct Staging {
