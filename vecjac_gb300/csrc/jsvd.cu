@@ -286,13 +286,13 @@ template <int LANES, typename T> __device__ __forceinline__ T hsum(T v)
 // scaled compensated dot products (src/ddpscl.c / src/zdpscl.c) by warp 0; x = G_q, y = G_p
 template <typename T, bool CPLX>
 __device__ void pair_dot(const SvdArgs<T> &a, const T *xr, const T *xi, const T *yr, const T *yi, T ex, T ey, T fx,
-                         T fy, T &zr, T &zi)
+                         T fy, bool live, T &zr, T &zi)
 {
   constexpr int L = svdc<T>::LANES;
-  const int lane = threadIdx.x & 31;
+  const int lane = (threadIdx.x & 31) % L;
   const int nx = -(int)ex, ny = -(int)ey;
   T sr = 0, tr = 0, sr_ = 0, tr_ = 0, si = 0, ti = 0, si_ = 0, ti_ = 0;
-  if (lane < L) {
+  if (live) {
     for (long long i = lane; i < a.m; i += L) {
       const T xri = scale2(xr[i], nx);
       const T yri = scale2(yr[i], ny);
@@ -410,13 +410,20 @@ template <typename T> __device__ __forceinline__ void amax(unsigned long long &m
   m = (b > m) ? b : m;
 }
 
+// pairs handled by one CTA: the LANES-wide dot of each pair runs on LANES lanes of warp 0,
+// so that one warp instruction serves 32/LANES pairs
+template <typename T> struct ppc { static constexpr int P = 32 / svdc<T>::LANES; };
+
 template <typename T, bool CPLX, bool TRACKV, bool STAGE>
 __global__ void __launch_bounds__(256) k_step(SvdArgs<T> a, int st, int g3, int last)
 {
   using F = fp<T>;
+  constexpr int P = ppc<T>::P;
+  constexpr int L = svdc<T>::LANES;
+  constexpr int NC = CPLX ? 4 : 2;   // staged columns per pair (real and imaginary planes)
   extern __shared__ __align__(128) unsigned char smem_raw[];
-  __shared__ PairState<T> ps;
-  __shared__ unsigned long long red[8][4];
+  __shared__ PairState<T> ps[P];
+  __shared__ unsigned long long red[8][2];
   __shared__ int s_err;
   __shared__ unsigned long long bar;
   SvdGlobal *const g = a.g;
@@ -426,8 +433,10 @@ __global__ void __launch_bounds__(256) k_step(SvdArgs<T> a, int st, int g3, int 
   Ctl &nxt = g->ctl[(g3 + 1) % 3];
   Ctl &nn = g->ctl[(g3 + 2) % 3];
   const unsigned *r = a.js + (size_t)st * (size_t)a.n;
-  const long long p = r[2 * blockIdx.x], q = r[2 * blockIdx.x + 1];
-  const int tid = threadIdx.x, warp = tid >> 5;
+  const long long n_2 = a.n >> 1;
+  const long long pair0 = (long long)blockIdx.x * P;
+  const int np = (int)((n_2 - pair0 < P) ? (n_2 - pair0) : P);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const Decision<T> d = decide(a, cur);
   if (blockIdx.x == 0 && tid == 0) {
     nxt.MGbase = (double)d.MG;
@@ -440,19 +449,20 @@ __global__ void __launch_bounds__(256) k_step(SvdArgs<T> a, int st, int g3, int 
   }
   if (tid == 0)
     s_err = 0;
-  T *Gp = a.G + p * a.ldG, *Gq = a.G + q * a.ldG, *Vp = a.V + p * a.ldV, *Vq = a.V + q * a.ldV;
-  T *Gip = CPLX ? (a.Gi + p * a.ldGi) : nullptr, *Giq = CPLX ? (a.Gi + q * a.ldGi) : nullptr;
-  T *Vip = CPLX ? (a.Vi + p * a.ldVi) : nullptr, *Viq = CPLX ? (a.Vi + q * a.ldVi) : nullptr;
+  auto colp = [&](int j) { return (long long)r[2 * (pair0 + j)]; };
+  auto colq = [&](int j) { return (long long)r[2 * (pair0 + j) + 1]; };
   // ---- 1. rescaling (rare) ----
   if (d.gres || d.ovf) {
     const int e = d.gres ? d.sNg : d.sNv;
-    scale_cols(a.G, a.ldG, a.m, p, q, e);
-    if (CPLX)
-      scale_cols(a.Gi, a.ldGi, a.m, p, q, e);
+    for (int j = 0; j < np; ++j) {
+      scale_cols(a.G, a.ldG, a.m, colp(j), colq(j), e);
+      if (CPLX)
+        scale_cols(a.Gi, a.ldGi, a.m, colp(j), colq(j), e);
+    }
     __syncthreads();
-    if (warp < 2) {
-      const T nv = col_norm<T, CPLX>(a, warp ? q : p);
-      if (((tid & 31) == 0) && !(nv <= svdc<T>::RMAX))
+    if (warp < 2 * np) {
+      const T nv = col_norm<T, CPLX>(a, (warp & 1) ? colq(warp >> 1) : colp(warp >> 1));
+      if ((lane == 0) && !(nv <= svdc<T>::RMAX))
         s_err = 1;
     }
     __syncthreads();
@@ -463,33 +473,37 @@ __global__ void __launch_bounds__(256) k_step(SvdArgs<T> a, int st, int g3, int 
       return;
     }
   }
-  if (d.vres) {
-    scale_cols(a.V, a.ldV, a.n, p, q, d.sNv);
-    if (CPLX)
-      scale_cols(a.Vi, a.ldVi, a.n, p, q, d.sNv);
-  }
-  // ---- stage the two columns of G in shared memory (TMA bulk copies) ----
-  T *rp = Gp, *rq = Gq, *rpi = Gip, *rqi = Giq;
-  if (STAGE) {
-    T *sm = reinterpret_cast<T *>(smem_raw);
-    rp = sm;
-    rq = sm + a.m;
-    if (CPLX) {
-      rpi = sm + 2 * a.m;
-      rqi = sm + 3 * a.m;
+  if (d.vres)
+    for (int j = 0; j < np; ++j) {
+      scale_cols(a.V, a.ldV, a.n, colp(j), colq(j), d.sNv);
+      if (CPLX)
+        scale_cols(a.Vi, a.ldVi, a.n, colp(j), colq(j), d.sNv);
     }
+  // ---- stage the columns of G in shared memory (TMA bulk copies) ----
+  // staged layout: pair j, column c (p, q, pi, qi) at sm + (j * NC + c) * m
+  T *const sm = reinterpret_cast<T *>(smem_raw);
+  auto rcol = [&](int j, int c) -> T * {
+    if (STAGE)
+      return sm + ((long long)j * NC + c) * a.m;
+    const long long col = (c & 1) ? colq(j) : colp(j);
+    return (c < 2) ? (a.G + col * a.ldG) : (a.Gi + col * a.ldGi);
+  };
+  if (STAGE) {
     if (tid == 0)
       mbar_init(&bar, 1u);
     __syncthreads();
     if (tid == 0) {
       const unsigned colb = (unsigned)(a.m * (long long)sizeof(T));
-      mbar_expect_tx(&bar, colb * (CPLX ? 4u : 2u));
-      const T *src[4] = {Gp, Gq, Gip, Giq};
-      T *dst[4] = {rp, rq, rpi, rqi};
-      for (int c = 0; c < (CPLX ? 4 : 2); ++c)
-        for (unsigned off = 0; off < colb; off += 32768u) {
-          const unsigned b = (colb - off < 32768u) ? (colb - off) : 32768u;
-          tma_load_1d(reinterpret_cast<char *>(dst[c]) + off, reinterpret_cast<const char *>(src[c]) + off, b, &bar);
+      mbar_expect_tx(&bar, colb * (unsigned)(NC * np));
+      for (int j = 0; j < np; ++j)
+        for (int c = 0; c < NC; ++c) {
+          const long long col = (c & 1) ? colq(j) : colp(j);
+          const T *src = (c < 2) ? (a.G + col * a.ldG) : (a.Gi + col * a.ldGi);
+          T *dst = rcol(j, c);
+          for (unsigned off = 0; off < colb; off += 32768u) {
+            const unsigned b = (colb - off < 32768u) ? (colb - off) : 32768u;
+            tma_load_1d(reinterpret_cast<char *>(dst) + off, reinterpret_cast<const char *>(src) + off, b, &bar);
+          }
         }
     }
     if (!mbar_wait_bounded(&bar)) {
@@ -502,17 +516,27 @@ __global__ void __launch_bounds__(256) k_step(SvdArgs<T> a, int st, int g3, int 
     }
   }
   __syncthreads();
-  // ---- 2. the scaled dot product (warp 0) ----
+  // ---- 2. scaled dot products: pair j on lanes [j L, (j+1) L) of warp 0 ----
   if (warp == 0) {
+    const int j = lane / L;
+    const bool act = (j < np);
+    const int jj = act ? j : 0;
+    const long long p = colp(jj), q = colq(jj);
     const T ep = a.eS[p], fp_ = a.fS[p], eq = a.eS[q], fq = a.fS[q];
     T zr = 0, zi = 0;
-    if ((eq >= -svdc<T>::RMAX) && (ep >= -svdc<T>::RMAX))
-      pair_dot<T, CPLX>(a, rq, rqi, rp, rpi, eq, ep, fq, fp_, zr, zi);
-    if (tid == 0) {
-      ps.ep = ep; ps.fp = fp_; ps.eq = eq; ps.fq = fq;
-      ps.a21r = zr;
-      ps.a21i = zi;
-      ps.skip = 0;
+    const bool live = act && (eq >= -svdc<T>::RMAX) && (ep >= -svdc<T>::RMAX);
+    pair_dot<T, CPLX>(a, rcol(jj, 1), CPLX ? rcol(jj, 3) : nullptr, rcol(jj, 0), CPLX ? rcol(jj, 2) : nullptr, eq,
+                      ep, fq, fp_, live, zr, zi);
+    if (act && (lane % L) == 0) {
+      PairState<T> &s = ps[j];
+      s.ep = ep; s.fp = fp_; s.eq = eq; s.fq = fq;
+      if (!live) {
+        zr = 0;
+        zi = 0;
+      }
+      s.a21r = zr;
+      s.a21i = zi;
+      s.skip = 0;
       long long code = 0;
       if (CPLX) {
         if (!visfinite(zr))
@@ -524,7 +548,7 @@ __global__ void __launch_bounds__(256) k_step(SvdArgs<T> a, int st, int g3, int 
         code = a.e_dot;
       if (code) {
         atomicMin((long long *)&g->err, code);
-        ps.skip = 1;
+        s.skip = 1;
       }
       else {
         // ---- 3. convergence, shear test, prescale, 2x2, classification ----
@@ -559,189 +583,195 @@ __global__ void __launch_bounds__(256) k_step(SvdArgs<T> a, int st, int g3, int 
           }
           else
             perm = rjac2<T, 0>(w11, w22, w21r, cc, at, l1, l2);
-          ps.c = cc;
-          ps.cat = at;
-          ps.sat = sat;
+          s.c = cc;
+          s.cat = at;
+          s.sat = sat;
           if (!ngs && cgs)
-            ps.code = 3;
+            s.code = 3;
           else if (ngs && cgs)
-            ps.code = -3;
+            s.code = -3;
           else if (perm)
-            ps.code = -2;
+            s.code = -2;
           else
-            ps.code = 2;
+            s.code = 2;
         }
         else if (efcmp(ep, fp_, eq, fq) < 0) {
           a.eS[p] = eq; a.eS[q] = ep;
           a.fS[p] = fq; a.fS[q] = fp_;
-          ps.code = -1;
+          s.code = -1;
         }
         else
-          ps.code = 1;
+          s.code = 1;
       }
     }
   }
   __syncthreads();
-  if (ps.skip)
-    return;
-  // ---- 4. apply; G is read from the staged copy, written to HBM (and to the copy) ----
-  const int code = ps.code;
-  unsigned long long mG = 0ull, mV = 0ull, mq = 0ull, mqi = 0ull;
-  bool chp = false, chq = false;
-  if (code == 1) {
-  }
-  else if (code == -1) {
-    for (long long i = tid; i < a.m; i += blockDim.x) {
-      const T x = rp[i], y = rq[i];
-      Gp[i] = y; Gq[i] = x;
-      if (CPLX) { const T xi = rpi[i], yi = rqi[i]; Gip[i] = yi; Giq[i] = xi; }
+  // ---- 4. apply to every pair of the CTA; G is read from the staged copy ----
+  unsigned long long mG = 0ull, mV = 0ull;
+  unsigned chmask = 0u;  // bit 2j: column p of pair j changed, bit 2j+1: column q
+  for (int j = 0; j < np; ++j) {
+    const PairState<T> s = ps[j];
+    if (s.skip)
+      continue;
+    const int code = s.code;
+    const long long p = colp(j), q = colq(j);
+    T *Gp = a.G + p * a.ldG, *Gq = a.G + q * a.ldG, *Vp = a.V + p * a.ldV, *Vq = a.V + q * a.ldV;
+    T *Gip = CPLX ? (a.Gi + p * a.ldGi) : nullptr, *Giq = CPLX ? (a.Gi + q * a.ldGi) : nullptr;
+    T *Vip = CPLX ? (a.Vi + p * a.ldVi) : nullptr, *Viq = CPLX ? (a.Vi + q * a.ldVi) : nullptr;
+    T *rp = rcol(j, 0), *rq = rcol(j, 1), *rpi = CPLX ? rcol(j, 2) : nullptr, *rqi = CPLX ? rcol(j, 3) : nullptr;
+    if (code == 1) {
     }
-    for (long long i = tid; i < a.n; i += blockDim.x) {
-      T t = Vp[i]; Vp[i] = Vq[i]; Vq[i] = t;
-      if (CPLX) { t = Vip[i]; Vip[i] = Viq[i]; Viq[i] = t; }
-    }
-  }
-  else if (code == 3 || code == -3) {
-    // Gram-Schmidt-like shear (src/dgsscl.c:5-85, src/zgsscl.c)
-    const T ex = ps.ep, ey = ps.eq, fx = ps.fp, fy = ps.fq;
-    const int nx = -(int)ex, ny = -(int)ey;
-    const int px = (int)ex, py = (int)ey;
-    if (code == 3) {
-      const T ff = F::div(fy, fx);
-      const T tfr = vneg(ps.a21r) * ff;
-      const T tfi = CPLX ? (ps.a21i * ff) : (T)0;
+    else if (code == -1) {
       for (long long i = tid; i < a.m; i += blockDim.x) {
-        if (CPLX) {
-          const T xri_ = scale2(rp[i], nx), xii_ = scale2(rpi[i], nx);
-          const T yri_ = scale2(rq[i], ny), yii_ = scale2(rqi[i], ny);
-          const T xr = F::fma_(tfr, xri_, F::fma_(vneg(tfi), xii_, yri_));
-          const T xi = F::fma_(tfr, xii_, F::fma_(tfi, xri_, yii_));
-          const T ur = scale2(xr, py), ui = scale2(xi, py);
-          Gq[i] = ur; Giq[i] = ui;
-          rq[i] = ur; rqi[i] = ui;
-          amax(mq, ur); amax(mqi, ui);
-        }
-        else {
-          const T xi = scale2(rp[i], nx);
-          const T yi = scale2(rq[i], ny);
-          const T u = scale2(F::fma_(tfr, xi, yi), py);
-          Gq[i] = u;
-          rq[i] = u;
-          amax(mq, u);
-        }
-      }
-      chq = true;
-    }
-    else {
-      const T ff = F::div(fx, fy);
-      const T tfr = vneg(ps.a21r) * ff;
-      const T tfi = CPLX ? (vneg(ps.a21i) * ff) : (T)0;
-      for (long long i = tid; i < a.m; i += blockDim.x) {
-        if (CPLX) {
-          const T yri = rq[i], yii = rqi[i], xri = rp[i], xii = rpi[i];
-          Gp[i] = yri; Gip[i] = yii;
-          rp[i] = yri; rpi[i] = yii;
-          const T yri_ = scale2(yri, ny), yii_ = scale2(yii, ny);
-          const T xri_ = scale2(xri, nx), xii_ = scale2(xii, nx);
-          const T vr = F::fma_(tfr, yri_, F::fma_(vneg(tfi), yii_, xri_));
-          const T vi = F::fma_(tfr, yii_, F::fma_(tfi, yri_, xii_));
-          const T ur = scale2(vr, px), ui = scale2(vi, px);
-          Gq[i] = ur; Giq[i] = ui;
-          rq[i] = ur; rqi[i] = ui;
-          amax(mq, ur); amax(mqi, ui);
-        }
-        else {
-          const T xi = rp[i], yi = rq[i];
-          Gp[i] = yi;
-          rp[i] = yi;
-          const T u = scale2(F::fma_(tfr, scale2(yi, ny), scale2(xi, nx)), px);
-          Gq[i] = u;
-          rq[i] = u;
-          amax(mq, u);
-        }
+        const T x = rp[i], y = rq[i];
+        Gp[i] = y; Gq[i] = x;
+        if (CPLX) { const T xi = rpi[i], yi = rqi[i]; Gip[i] = yi; Giq[i] = xi; }
       }
       for (long long i = tid; i < a.n; i += blockDim.x) {
         T t = Vp[i]; Vp[i] = Vq[i]; Vq[i] = t;
         if (CPLX) { t = Vip[i]; Vip[i] = Viq[i]; Viq[i] = t; }
       }
-      if (tid == 0) {
-        a.eS[p] = ps.eq; a.eS[q] = ps.ep;
-        a.fS[p] = ps.fq; a.fS[q] = ps.fp;
-      }
-      chq = true;
     }
-    mG = (mq > mqi) ? mq : mqi;
-  }
-  else {
-    // rotation (src/djrot.c, src/djrotf.c, src/zjrot.c, src/zjrotf.c); code -2 permutes
-    const bool perm = (code == -2);
-    const T c = ps.c, at = ps.cat, sat = ps.sat;
-    // the reference marks both columns as changed after any rotation (src/dvjsvd.c:573)
-    chp = chq = true;
-    const bool real_rot = (!CPLX) || (sat == (T)0);
-    const bool cone = (c == (T)1);
-    if (real_rot && at == (T)0) {
-      // c == 1: identity (or a swap when permuting); c != 1 "never happens" (-4 / -10)
-      if (cone && perm) {
+    else if (code == 3 || code == -3) {
+      // Gram-Schmidt-like shear (src/dgsscl.c:5-85, src/zgsscl.c)
+      const T ex = s.ep, ey = s.eq, fx = s.fp, fy = s.fq;
+      const int nx = -(int)ex, ny = -(int)ey;
+      const int px = (int)ex, py = (int)ey;
+      if (code == 3) {
+        const T ff = F::div(fy, fx);
+        const T tfr = vneg(s.a21r) * ff;
+        const T tfi = CPLX ? (s.a21i * ff) : (T)0;
         for (long long i = tid; i < a.m; i += blockDim.x) {
-          const T x = rp[i], y = rq[i];
-          Gp[i] = y; Gq[i] = x; rp[i] = y; rq[i] = x;
-          if (CPLX) { const T xi = rpi[i], yi = rqi[i]; Gip[i] = yi; Giq[i] = xi; rpi[i] = yi; rqi[i] = xi; }
+          if (CPLX) {
+            const T xri_ = scale2(rp[i], nx), xii_ = scale2(rpi[i], nx);
+            const T yri_ = scale2(rq[i], ny), yii_ = scale2(rqi[i], ny);
+            const T xr = F::fma_(tfr, xri_, F::fma_(vneg(tfi), xii_, yri_));
+            const T xi = F::fma_(tfr, xii_, F::fma_(tfi, xri_, yii_));
+            const T ur = scale2(xr, py), ui = scale2(xi, py);
+            Gq[i] = ur; Giq[i] = ui;
+            rq[i] = ur; rqi[i] = ui;
+            amax(mG, ur); amax(mG, ui);
+          }
+          else {
+            const T xi = scale2(rp[i], nx);
+            const T yi = scale2(rq[i], ny);
+            const T u = scale2(F::fma_(tfr, xi, yi), py);
+            Gq[i] = u;
+            rq[i] = u;
+            amax(mG, u);
+          }
+        }
+      }
+      else {
+        const T ff = F::div(fx, fy);
+        const T tfr = vneg(s.a21r) * ff;
+        const T tfi = CPLX ? (vneg(s.a21i) * ff) : (T)0;
+        for (long long i = tid; i < a.m; i += blockDim.x) {
+          if (CPLX) {
+            const T yri = rq[i], yii = rqi[i], xri = rp[i], xii = rpi[i];
+            Gp[i] = yri; Gip[i] = yii;
+            rp[i] = yri; rpi[i] = yii;
+            const T yri_ = scale2(yri, ny), yii_ = scale2(yii, ny);
+            const T xri_ = scale2(xri, nx), xii_ = scale2(xii, nx);
+            const T vr = F::fma_(tfr, yri_, F::fma_(vneg(tfi), yii_, xri_));
+            const T vi = F::fma_(tfr, yii_, F::fma_(tfi, yri_, xii_));
+            const T ur = scale2(vr, px), ui = scale2(vi, px);
+            Gq[i] = ur; Giq[i] = ui;
+            rq[i] = ur; rqi[i] = ui;
+            amax(mG, ur); amax(mG, ui);
+          }
+          else {
+            const T xi = rp[i], yi = rq[i];
+            Gp[i] = yi;
+            rp[i] = yi;
+            const T u = scale2(F::fma_(tfr, scale2(yi, ny), scale2(xi, nx)), px);
+            Gq[i] = u;
+            rq[i] = u;
+            amax(mG, u);
+          }
         }
         for (long long i = tid; i < a.n; i += blockDim.x) {
           T t = Vp[i]; Vp[i] = Vq[i]; Vq[i] = t;
           if (CPLX) { t = Vip[i]; Vip[i] = Viq[i]; Viq[i] = t; }
         }
-      }
-    }
-    else if (real_rot) {
-      // the permuted form writes (y - t x) c to x and (x + t y) c to y: the same two
-      // products with the destinations exchanged
-      for (int pl = 0; pl < (CPLX ? 2 : 1); ++pl) {
-        T *X = pl ? Gip : Gp, *Y = pl ? Giq : Gq, *RX = pl ? rpi : rp, *RY = pl ? rqi : rq;
-        T *DX = perm ? Y : X, *DY = perm ? X : Y, *RDX = perm ? RY : RX, *RDY = perm ? RX : RY;
-        for (long long i = tid; i < a.m; i += blockDim.x) {
-          const T x = RX[i], y = RY[i];
-          T u = F::fma_(y, at, x);
-          T w = F::fma_(vneg(x), at, y);
-          if (!cone) { u = u * c; w = w * c; }
-          DX[i] = u; DY[i] = w;
-          RDX[i] = u; RDY[i] = w;
-          amax(mG, u); amax(mG, w);
-        }
-        T *XV = pl ? Vip : Vp, *YV = pl ? Viq : Vq;
-        T *DXV = perm ? YV : XV, *DYV = perm ? XV : YV;
-        for (long long i = tid; i < a.n; i += blockDim.x) {
-          const T x = XV[i], y = YV[i];
-          T u = F::fma_(y, at, x);
-          T w = F::fma_(vneg(x), at, y);
-          if (!cone) { u = u * c; w = w * c; }
-          DXV[i] = u; DYV[i] = w;
-          if (TRACKV) { amax(mV, u); amax(mV, w); }
+        if (tid == 0) {
+          a.eS[p] = s.eq; a.eS[q] = s.ep;
+          a.fS[p] = s.fq; a.fS[q] = s.fp;
         }
       }
+      chmask |= 2u << (2 * j);
     }
     else {
-      const T cta = at, sta = sat, cna = vneg(at);
-      for (int mat = 0; mat < 2; ++mat) {
-        T *Xr = mat ? Vp : Gp, *Xi = mat ? Vip : Gip, *Yr = mat ? Vq : Gq, *Yi = mat ? Viq : Giq;
-        const T *Rxr = mat ? Vp : rp, *Rxi = mat ? Vip : rpi, *Ryr = mat ? Vq : rq, *Ryi = mat ? Viq : rqi;
-        const long long rows = mat ? a.n : a.m;
-        unsigned long long &mm = mat ? mV : mG;
-        for (long long i = tid; i < rows; i += blockDim.x) {
-          const T x_r = Rxr[i], x_i = Rxi[i], y_r = Ryr[i], y_i = Ryi[i];
-          T ar = F::fma_(y_r, cta, F::fma_(vneg(y_i), sta, x_r));
-          T ai = F::fma_(y_r, sta, F::fma_(y_i, cta, x_i));
-          T br = F::fma_(x_r, cna, F::fma_(vneg(x_i), sta, y_r));
-          T bi = F::fma_(x_r, sta, F::fma_(x_i, cna, y_i));
-          if (!cone) { ar = ar * c; ai = ai * c; br = br * c; bi = bi * c; }
-          if (perm) { Yr[i] = ar; Yi[i] = ai; Xr[i] = br; Xi[i] = bi; }
-          else { Xr[i] = ar; Xi[i] = ai; Yr[i] = br; Yi[i] = bi; }
-          if (!mat) {
-            if (perm) { rq[i] = ar; rqi[i] = ai; rp[i] = br; rpi[i] = bi; }
-            else { rp[i] = ar; rpi[i] = ai; rq[i] = br; rqi[i] = bi; }
+      // rotation (src/djrot.c, src/djrotf.c, src/zjrot.c, src/zjrotf.c); code -2 permutes
+      const bool perm = (code == -2);
+      const T c = s.c, at = s.cat, sat = s.sat;
+      // the reference marks both columns as changed after any rotation (src/dvjsvd.c:573)
+      chmask |= 3u << (2 * j);
+      const bool real_rot = (!CPLX) || (sat == (T)0);
+      const bool cone = (c == (T)1);
+      if (real_rot && at == (T)0) {
+        // c == 1: identity (or a swap when permuting); c != 1 "never happens" (-4 / -10)
+        if (cone && perm) {
+          for (long long i = tid; i < a.m; i += blockDim.x) {
+            const T x = rp[i], y = rq[i];
+            Gp[i] = y; Gq[i] = x; rp[i] = y; rq[i] = x;
+            if (CPLX) { const T xi = rpi[i], yi = rqi[i]; Gip[i] = yi; Giq[i] = xi; rpi[i] = yi; rqi[i] = xi; }
           }
-          if (!mat || TRACKV) { amax(mm, ar); amax(mm, ai); amax(mm, br); amax(mm, bi); }
+          for (long long i = tid; i < a.n; i += blockDim.x) {
+            T t = Vp[i]; Vp[i] = Vq[i]; Vq[i] = t;
+            if (CPLX) { t = Vip[i]; Vip[i] = Viq[i]; Viq[i] = t; }
+          }
+        }
+      }
+      else if (real_rot) {
+        // the permuted form writes (y - t x) c to x and (x + t y) c to y: the same two
+        // products with the destinations exchanged
+        for (int pl = 0; pl < (CPLX ? 2 : 1); ++pl) {
+          T *X = pl ? Gip : Gp, *Y = pl ? Giq : Gq, *RX = pl ? rpi : rp, *RY = pl ? rqi : rq;
+          T *DX = perm ? Y : X, *DY = perm ? X : Y, *RDX = perm ? RY : RX, *RDY = perm ? RX : RY;
+          for (long long i = tid; i < a.m; i += blockDim.x) {
+            const T x = RX[i], y = RY[i];
+            T u = F::fma_(y, at, x);
+            T w = F::fma_(vneg(x), at, y);
+            if (!cone) { u = u * c; w = w * c; }
+            DX[i] = u; DY[i] = w;
+            RDX[i] = u; RDY[i] = w;
+            amax(mG, u); amax(mG, w);
+          }
+          T *XV = pl ? Vip : Vp, *YV = pl ? Viq : Vq;
+          T *DXV = perm ? YV : XV, *DYV = perm ? XV : YV;
+          for (long long i = tid; i < a.n; i += blockDim.x) {
+            const T x = XV[i], y = YV[i];
+            T u = F::fma_(y, at, x);
+            T w = F::fma_(vneg(x), at, y);
+            if (!cone) { u = u * c; w = w * c; }
+            DXV[i] = u; DYV[i] = w;
+            if (TRACKV) { amax(mV, u); amax(mV, w); }
+          }
+        }
+      }
+      else {
+        const T cta = at, sta = sat, cna = vneg(at);
+        for (int mat = 0; mat < 2; ++mat) {
+          T *Xr = mat ? Vp : Gp, *Xi = mat ? Vip : Gip, *Yr = mat ? Vq : Gq, *Yi = mat ? Viq : Giq;
+          const T *Rxr = mat ? Vp : rp, *Rxi = mat ? Vip : rpi, *Ryr = mat ? Vq : rq, *Ryi = mat ? Viq : rqi;
+          const long long rows = mat ? a.n : a.m;
+          unsigned long long &mm = mat ? mV : mG;
+          for (long long i = tid; i < rows; i += blockDim.x) {
+            const T x_r = Rxr[i], x_i = Rxi[i], y_r = Ryr[i], y_i = Ryi[i];
+            T ar = F::fma_(y_r, cta, F::fma_(vneg(y_i), sta, x_r));
+            T ai = F::fma_(y_r, sta, F::fma_(y_i, cta, x_i));
+            T br = F::fma_(x_r, cna, F::fma_(vneg(x_i), sta, y_r));
+            T bi = F::fma_(x_r, sta, F::fma_(x_i, cna, y_i));
+            if (!cone) { ar = ar * c; ai = ai * c; br = br * c; bi = bi * c; }
+            if (perm) { Yr[i] = ar; Yi[i] = ai; Xr[i] = br; Xi[i] = bi; }
+            else { Xr[i] = ar; Xi[i] = ai; Yr[i] = br; Yi[i] = bi; }
+            if (!mat) {
+              if (perm) { rq[i] = ar; rqi[i] = ai; rp[i] = br; rpi[i] = bi; }
+              else { rp[i] = ar; rpi[i] = ai; rq[i] = br; rqi[i] = bi; }
+            }
+            if (!mat || TRACKV) { amax(mm, ar); amax(mm, ai); amax(mm, br); amax(mm, bi); }
+          }
         }
       }
     }
@@ -749,7 +779,7 @@ __global__ void __launch_bounds__(256) k_step(SvdArgs<T> a, int st, int g3, int 
   // block max of |G| and |V| updates
   mG = warp_max_u64(mG);
   mV = warp_max_u64(mV);
-  if ((tid & 31) == 0) {
+  if (lane == 0) {
     red[warp][0] = mG;
     red[warp][1] = mV;
   }
@@ -772,15 +802,15 @@ __global__ void __launch_bounds__(256) k_step(SvdArgs<T> a, int st, int g3, int 
         atomicMax(&nxt.nMV, bv);
     }
   }
-  // ---- 5. norms of the changed columns, for the next step ----
+  // ---- 5. norms of the changed columns (warp w: pair w/2, column p or q), for the next step ----
   // (not after the last step of the last allowed sweep: the reference returns there with
   // the norms of those columns not yet recomputed)
-  if ((chp || chq) && !last) {
-    if ((warp == 0 && chp) || (warp == 1 && chq)) {
-      const T nv = warp ? col_norm_at<T, CPLX>(a, q, rq, rqi) : col_norm_at<T, CPLX>(a, p, rp, rpi);
-      if (((tid & 31) == 0) && !(nv <= svdc<T>::RMAX))
-        atomicOr(&nxt.ovf, 1);
-    }
+  if (!last && warp < 2 * np && ((chmask >> warp) & 1u)) {
+    const int j = warp >> 1, c = warp & 1;
+    const long long col = c ? colq(j) : colp(j);
+    const T nv = col_norm_at<T, CPLX>(a, col, rcol(j, c), CPLX ? rcol(j, 2 + c) : nullptr);
+    if ((lane == 0) && !(nv <= svdc<T>::RMAX))
+      atomicOr(&nxt.ovf, 1);
   }
 }
 
@@ -1017,8 +1047,10 @@ static vj_fint svd_dev(vj_fnat m_, vj_fnat n_, T *G, vj_fnat ldG, T *Gi, vj_fnat
   if (cudaGetLastError() != cudaSuccess)
     return VJ_ERR_CUDA;
   // stage each pair's columns of G in shared memory when they fit (160 KiB per CTA)
-  const size_t smem = (size_t)m * sizeof(T) * (CPLX ? 4u : 2u);
+  constexpr int P = ppc<T>::P;
+  const size_t smem = (size_t)m * sizeof(T) * (CPLX ? 4u : 2u) * P;
   const bool stage = (smem <= (size_t)160 * 1024);
+  const unsigned grid = (unsigned)((n_2 + P - 1) / P);
   if (stage && smem > 48 * 1024) {
     cudaFuncSetAttribute(k_step<T, CPLX, true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     cudaFuncSetAttribute(k_step<T, CPLX, false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -1033,15 +1065,15 @@ static vj_fint svd_dev(vj_fnat m_, vj_fnat n_, T *G, vj_fnat ldG, T *Gi, vj_fnat
       const int g3 = (int)(gstep % 3);
       if (stage) {
         if (preset)
-          k_step<T, CPLX, true, true><<<(unsigned)n_2, blk, smem, s>>>(a, (int)st, g3, last);
+          k_step<T, CPLX, true, true><<<grid, blk, smem, s>>>(a, (int)st, g3, last);
         else
-          k_step<T, CPLX, false, true><<<(unsigned)n_2, blk, smem, s>>>(a, (int)st, g3, last);
+          k_step<T, CPLX, false, true><<<grid, blk, smem, s>>>(a, (int)st, g3, last);
       }
       else {
         if (preset)
-          k_step<T, CPLX, true, false><<<(unsigned)n_2, blk, 0, s>>>(a, (int)st, g3, last);
+          k_step<T, CPLX, true, false><<<grid, blk, 0, s>>>(a, (int)st, g3, last);
         else
-          k_step<T, CPLX, false, false><<<(unsigned)n_2, blk, 0, s>>>(a, (int)st, g3, last);
+          k_step<T, CPLX, false, false><<<grid, blk, 0, s>>>(a, (int)st, g3, last);
       }
     }
     if (cudaGetLastError() != cudaSuccess)
