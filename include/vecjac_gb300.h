@@ -128,12 +128,15 @@ unsigned *pjs(long id, unsigned n, unsigned stp[1]);
 vj_fint vj_pjs_dev(long id, unsigned n, unsigned *table, void *stream);
 
 /* ---------------- library ---------------- */
-/* Number of sweeps-per-phase statistics of the last host-API SVD call (the JTRACE
- * equivalent): total rotations per sweep and per-phase GPU times in seconds. */
+/* Statistics of the last host-API SVD call, the counterpart of the reference's JTRACE
+ * log (src/dvjsvd.c:596,635): transformed pairs per sweep (first 64 sweeps) and, when
+ * VJ_TRACE=1 is set in the environment, SM cycles spent by one CTA in each phase of the
+ * pivot steps: 0 control/rescaling, 1 staging, 2 dot products, 3 2x2 and classification,
+ * 4 rotations, 5 norms. */
 typedef struct vj_trace {
   unsigned sweeps;
   unsigned long long rotations[64];
-  double t_total;
+  unsigned long long phase_cycles[8];
 } vj_trace;
 vj_fint vj_last_trace(vj_trace *out);
 const char *vj_version(void);

@@ -169,3 +169,19 @@ def pjs_dev(sid, n, table, stream=None):
     L = lib()
     s = C.c_void_p(stream) if stream else None
     return L.vj_pjs_dev(C.c_long(int(sid)), C.c_uint(int(n)), _p(table), s)
+
+
+class _Trace(C.Structure):
+    _fields_ = [("sweeps", C.c_uint), ("rotations", C.c_ulonglong * 64), ("phase_cycles", C.c_ulonglong * 8)]
+
+
+PHASES = ("control", "staging", "dots", "2x2", "rotations", "norms")
+
+
+def last_trace():
+    """Statistics of the last host-API SVD: transformed pairs per sweep and, with VJ_TRACE=1,
+    SM cycles of one CTA per step phase (summed over all steps)."""
+    t = _Trace()
+    lib().vj_last_trace(C.byref(t))
+    return {"sweeps": t.sweeps, "rotations": list(t.rotations[:min(t.sweeps, 64)]),
+            "phase_cycles": dict(zip(PHASES, list(t.phase_cycles[:len(PHASES)])))}

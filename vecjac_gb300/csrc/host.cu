@@ -110,6 +110,18 @@ void trace_reset()
   memset(&g_trace, 0, sizeof(g_trace));
 }
 
+bool trace_enabled()
+{
+  const char *e = getenv("VJ_TRACE");
+  return e && *e == '1';
+}
+
+void trace_phases(const unsigned long long *cycles, int count)
+{
+  for (int i = 0; i < count && i < 8; ++i)
+    g_trace.phase_cycles[i] = cycles[i];
+}
+
 void trace_sweep(unsigned sweep, unsigned long long rotations)
 {
   if (sweep < 64)

@@ -7,9 +7,15 @@
 // Finite inputs take a path whose exponent logic (getexp, min, scalef by an integer)
 // runs on the integer pipes; inputs with an inf or NaN take the literal transcription.
 #pragma once
+#include "idiv.cuh"
 #include "vj_fp.cuh"
 
 namespace vj {
+
+// correctly rounded division: FP64 quotients are formed on the integer pipes (ddiv_int),
+// FP32 ones by the FP32 unit
+__device__ __forceinline__ double qdiv(double a, double b) { return ddiv_int(a, b); }
+__device__ __forceinline__ float qdiv(float a, float b) { return fp<float>::div(a, b); }
 
 template <typename T> __device__ __forceinline__ bool all_finite3(T a, T b, T c)
 {
@@ -46,8 +52,8 @@ template <typename T> __device__ __forceinline__ angle<T> jac_angle(T a1, T a2, 
   const T one = (T)1;
   const T ad = a1 - a2;
   ad_out = ad;
-  const T t2 = vor(clamp_t2(F::div(ab, vabs(ad))), vsgn(ad));
-  const T t1 = F::div(t2, one + F::sqrt_(F::fma_(t2, t2, one)));
+  const T t2 = vor(clamp_t2(qdiv(ab, vabs(ad))), vsgn(ad));
+  const T t1 = qdiv(t2, one + F::sqrt_(F::fma_(t2, t2, one)));
   const T s2 = F::fma_(t1, t1, one);
   return angle<T>{t1, s2, F::sqrt_(s2)};
 }
@@ -69,8 +75,8 @@ __device__ __forceinline__ unsigned rjac2(T a1, T a2, T ar, T &c, T &at, T &l1, 
     T ad;
     const angle<T> g = jac_angle(a1, a2, ab, ad);
     t1 = g.t1; s2 = g.s2; s1 = g.s1;
-    L1 = F::div(F::fma_(t1, F::fma_(a2, t1, ab), a1), s2);
-    L2 = F::div(F::fma_(t1, F::fma_(a1, t1, vneg(ab)), a2), s2);
+    L1 = qdiv(F::fma_(t1, F::fma_(a2, t1, ab), a1), s2);
+    L2 = qdiv(F::fma_(t1, F::fma_(a1, t1, vneg(ab)), a2), s2);
     l1 = scale2(L1, -es);
     l2 = scale2(L2, -es);
   }
@@ -100,8 +106,8 @@ __device__ __forceinline__ unsigned rjac2(T a1, T a2, T ar, T &c, T &at, T &l1, 
     c = s1;
   }
   else {
-    c = F::div(one, s1);
-    at = ((KIND == 1) ? F::div(vxor(t1, as), s1) : vxor(t1, as));
+    c = qdiv(one, s1);
+    at = ((KIND == 1) ? qdiv(vxor(t1, as), s1) : vxor(t1, as));
   }
   return (L1 < L2) ? 1u : 0u;
 }
@@ -123,16 +129,16 @@ __device__ __forceinline__ unsigned cjac2(T a1, T a2, T ar, T ai, T &c, T &cat, 
     const T as = vsgn(ar);
     const T am = vmin(ar_, ai_);
     const T aM = vmax(ar_, ai_);
-    T aa = vmax(F::div(am, aM), zero);
+    T aa = vmax(qdiv(am, aM), zero);
     aa = F::sqrt_(F::fma_(aa, aa, one)) * aM;
-    ar_ = vor(vmin(F::div(ar_, aa), one), as);
-    ai_ = F::div(ai, vmax(aa, F::true_min()));
+    ar_ = vor(vmin(qdiv(ar_, aa), one), as);
+    ai_ = qdiv(ai, vmax(aa, F::true_min()));
     const T ab = scale2(aa, 1);
     T ad;
     const angle<T> g = jac_angle(a1, a2, ab, ad);
     t1 = g.t1; s2 = g.s2; s1 = g.s1;
-    L1 = F::div(F::fma_(t1, F::fma_(a2, t1, ab), a1), s2);
-    L2 = F::div(F::fma_(t1, F::fma_(a1, t1, vneg(ab)), a2), s2);
+    L1 = qdiv(F::fma_(t1, F::fma_(a2, t1, ab), a1), s2);
+    L2 = qdiv(F::fma_(t1, F::fma_(a1, t1, vneg(ab)), a2), s2);
     l1 = scale2(L1, -es);
     l2 = scale2(L2, -es);
   }
@@ -172,12 +178,12 @@ __device__ __forceinline__ unsigned cjac2(T a1, T a2, T ar, T ai, T &c, T &cat, 
     ai_ = xmul(ai_, t1);
   }
   else if (KIND == 1) {
-    c = F::div(one, s1);
-    ar_ = F::div(ar_ * t1, s1);
+    c = qdiv(one, s1);
+    ar_ = qdiv(ar_ * t1, s1);
     ai_ = xdiv(xmul(ai_, t1), s1);
   }
   else {
-    c = F::div(one, s1);
+    c = qdiv(one, s1);
     ar_ = ar_ * t1;
     ai_ = xmul(ai_, t1);
   }

@@ -65,9 +65,13 @@ struct SvdGlobal {
   long long err;                // 0 or the (negative) error code, atomicMin
   unsigned long long swt;       // transformed pairs in the current sweep
   Ctl ctl[3];
+  // per-phase SM cycles of CTA 0 (the JTRACE split of src/dvjsvd.c:635), when tracing:
+  // 0 control + rescaling, 1 staging, 2 dot products, 3 2x2 + classification, 4 rotations, 5 norms
+  unsigned long long phase[8];
 };
 
 template <typename T> struct SvdArgs {
+  int trace;                    // record per-phase cycles (VJ_TRACE=1)
   long long m, n, ldG, ldGi, ldV, ldVi;
   T *G, *Gi, *V, *Vi, *eS, *fS;
   const unsigned *js;
@@ -437,6 +441,15 @@ __global__ void __launch_bounds__(256) k_step(SvdArgs<T> a, int st, int g3, int 
   const long long pair0 = (long long)blockIdx.x * P;
   const int np = (int)((n_2 - pair0 < P) ? (n_2 - pair0) : P);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const bool tr = a.trace && blockIdx.x == 0 && tid == 0;
+  long long tmark = tr ? clock64() : 0;
+  auto tphase = [&](int ph) {
+    if (tr) {
+      const long long t = clock64();
+      atomicAdd(&g->phase[ph], (unsigned long long)(t - tmark));
+      tmark = t;
+    }
+  };
   const Decision<T> d = decide(a, cur);
   if (blockIdx.x == 0 && tid == 0) {
     nxt.MGbase = (double)d.MG;
@@ -479,6 +492,7 @@ __global__ void __launch_bounds__(256) k_step(SvdArgs<T> a, int st, int g3, int 
       if (CPLX)
         scale_cols(a.Vi, a.ldVi, a.n, colp(j), colq(j), d.sNv);
     }
+  tphase(0);
   // ---- stage the columns of G in shared memory (TMA bulk copies) ----
   // staged layout: pair j, column c (p, q, pi, qi) at sm + (j * NC + c) * m
   T *const sm = reinterpret_cast<T *>(smem_raw);
@@ -516,6 +530,7 @@ __global__ void __launch_bounds__(256) k_step(SvdArgs<T> a, int st, int g3, int 
     }
   }
   __syncthreads();
+  tphase(1);
   // ---- 2. scaled dot products: pair j on lanes [j L, (j+1) L) of warp 0 ----
   if (warp == 0) {
     const int j = lane / L;
@@ -527,6 +542,7 @@ __global__ void __launch_bounds__(256) k_step(SvdArgs<T> a, int st, int g3, int 
     const bool live = act && (eq >= -svdc<T>::RMAX) && (ep >= -svdc<T>::RMAX);
     pair_dot<T, CPLX>(a, rcol(jj, 1), CPLX ? rcol(jj, 3) : nullptr, rcol(jj, 0), CPLX ? rcol(jj, 2) : nullptr, eq,
                       ep, fq, fp_, live, zr, zi);
+    tphase(2);
     if (act && (lane % L) == 0) {
       PairState<T> &s = ps[j];
       s.ep = ep; s.fp = fp_; s.eq = eq; s.fq = fq;
@@ -606,6 +622,7 @@ __global__ void __launch_bounds__(256) k_step(SvdArgs<T> a, int st, int g3, int 
     }
   }
   __syncthreads();
+  tphase(3);
   // ---- 4. apply to every pair of the CTA; G is read from the staged copy ----
   unsigned long long mG = 0ull, mV = 0ull;
   unsigned chmask = 0u;  // bit 2j: column p of pair j changed, bit 2j+1: column q
@@ -776,6 +793,7 @@ __global__ void __launch_bounds__(256) k_step(SvdArgs<T> a, int st, int g3, int 
       }
     }
   }
+  tphase(4);
   // block max of |G| and |V| updates
   mG = warp_max_u64(mG);
   mV = warp_max_u64(mV);
@@ -812,6 +830,7 @@ __global__ void __launch_bounds__(256) k_step(SvdArgs<T> a, int st, int g3, int 
     if ((lane == 0) && !(nv <= svdc<T>::RMAX))
       atomicOr(&nxt.ovf, 1);
   }
+  tphase(5);
 }
 
 // norms of all columns before the first step (src/dvjsvd.c:174-180 sets w1 = 1)
@@ -1029,6 +1048,7 @@ static vj_fint svd_dev(vj_fnat m_, vj_fnat n_, T *G, vj_fnat ldG, T *Gi, vj_fnat
   if (cudaMemcpyAsync(dg, &hg, sizeof(hg), cudaMemcpyHostToDevice, s) != cudaSuccess)
     return VJ_ERR_CUDA;
   SvdArgs<T> a;
+  a.trace = host::trace_enabled() ? 1 : 0;
   a.m = m; a.n = n; a.ldG = (long long)ldG; a.ldGi = (long long)ldGi; a.ldV = (long long)ldV;
   a.ldVi = (long long)ldVi;
   a.G = G; a.Gi = Gi; a.V = V; a.Vi = Vi; a.eS = eS; a.fS = fS; a.js = js; a.g = dg;
@@ -1097,6 +1117,11 @@ static vj_fint svd_dev(vj_fnat m_, vj_fnat n_, T *G, vj_fnat ldG, T *Gi, vj_fnat
   }
   if (cudaStreamSynchronize(s) != cudaSuccess)
     return VJ_ERR_CUDA;
+  if (a.trace) {
+    unsigned long long ph[8];
+    if (cudaMemcpy(ph, dg->phase, sizeof(ph), cudaMemcpyDeviceToHost) == cudaSuccess)
+      host::trace_phases(ph, 6);
+  }
   return (vj_fint)sw;
 }
 

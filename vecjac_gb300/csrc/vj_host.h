@@ -30,6 +30,9 @@ bool streams2(cudaStream_t s[2]);
 // per-sweep statistics of the last SVD (transformed pairs per sweep)
 void trace_reset();
 void trace_sweep(unsigned sweep, unsigned long long rotations);
+// per-phase cycle counts (VJ_TRACE=1 in the environment enables their collection)
+bool trace_enabled();
+void trace_phases(const unsigned long long *cycles, int count);
 
 // elements per chunk of a host-pointer 2x2 call (a multiple of `lanes`)
 long long bjac2_chunk(long long n, size_t elem, bool cplx, int lanes);
