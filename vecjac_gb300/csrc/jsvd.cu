@@ -269,15 +269,6 @@ template <typename T> __device__ __forceinline__ void fast_two_sum(T a, T b, T &
   t = lo - (s_ - hi);
 }
 
-// one compensated product-accumulate step (src/ddpscl.c:51-60, MUL2SUM src/zdpscl.c)
-template <typename T> __device__ __forceinline__ void mul2sum(T x, T y, T &s, T &t, T &s_, T &t_)
-{
-  const T xy = fp<T>::mul_rd(x, y);
-  const T xy_ = fp<T>::fma_(x, y, vneg(xy));
-  fast_two_sum(s, xy + t, s, t);
-  fast_two_sum(s_, xy_ + t_, s_, t_);
-}
-
 // halving tree over the LANES lanes of warp 0 (GCC's _mm512_reduce_add order); lane 0 has it
 template <int LANES, typename T> __device__ __forceinline__ T hsum(T v)
 {
@@ -287,7 +278,44 @@ template <int LANES, typename T> __device__ __forceinline__ T hsum(T v)
   return v;
 }
 
-// scaled compensated dot products (src/ddpscl.c / src/zdpscl.c) by warp 0; x = G_q, y = G_p
+// scaled compensated dot products (src/ddpscl.c / src/zdpscl.c) by warp 0; x = G_q, y = G_p.
+// Only the two (four for complex data) 2Sum accumulations carry a dependency from one
+// element to the next; the loads, the power-of-two scaling and the exact product split
+// (round-down product and its error by an FMA) of element i + LANES are issued before the
+// accumulation of element i, so that their FP64 latency overlaps the accumulator chain.
+template <typename T, bool CPLX> struct DotTerms {
+  T pd[CPLX ? 4 : 1], dn[CPLX ? 4 : 1];
+};
+
+template <typename T, bool CPLX>
+__device__ __forceinline__ void dot_terms(const T *xr, const T *xi, const T *yr, const T *yi, long long i, int nx,
+                                          int ny, DotTerms<T, CPLX> &d)
+{
+  const T xri = scale2(xr[i], nx);
+  const T yri = scale2(yr[i], ny);
+  if (CPLX) {
+    const T yii = scale2(yi[i], ny);
+    const T xii = scale2(xi[i], nx);
+    const T xs[4] = {xri, xii, xri, vneg(xii)}, ys[4] = {yri, yii, yii, yri};
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      d.pd[k] = fp<T>::mul_rd(xs[k], ys[k]);
+      d.dn[k] = fp<T>::fma_(xs[k], ys[k], vneg(d.pd[k]));
+    }
+  }
+  else {
+    d.pd[0] = fp<T>::mul_rd(xri, yri);
+    d.dn[0] = fp<T>::fma_(xri, yri, vneg(d.pd[0]));
+  }
+}
+
+template <typename T>
+__device__ __forceinline__ void dot_acc(T pd, T dn, T &s, T &t, T &s_, T &t_)
+{
+  fast_two_sum(s, pd + t, s, t);
+  fast_two_sum(s_, dn + t_, s_, t_);
+}
+
 template <typename T, bool CPLX>
 __device__ void pair_dot(const SvdArgs<T> &a, const T *xr, const T *xi, const T *yr, const T *yi, T ex, T ey, T fx,
                          T fy, bool live, T &zr, T &zi)
@@ -296,21 +324,23 @@ __device__ void pair_dot(const SvdArgs<T> &a, const T *xr, const T *xi, const T 
   const int lane = (threadIdx.x & 31) % L;
   const int nx = -(int)ex, ny = -(int)ey;
   T sr = 0, tr = 0, sr_ = 0, tr_ = 0, si = 0, ti = 0, si_ = 0, ti_ = 0;
-  if (live) {
+  if (live && lane < a.m) {
+    DotTerms<T, CPLX> cur, nxt;
+    dot_terms<T, CPLX>(xr, xi, yr, yi, lane, nx, ny, cur);
     for (long long i = lane; i < a.m; i += L) {
-      const T xri = scale2(xr[i], nx);
-      const T yri = scale2(yr[i], ny);
+      const bool more = (i + L < a.m);
+      if (more)
+        dot_terms<T, CPLX>(xr, xi, yr, yi, i + L, nx, ny, nxt);
       if (CPLX) {
-        const T yii = scale2(yi[i], ny);
-        T xii = scale2(xi[i], nx);
-        mul2sum(xri, yri, sr, tr, sr_, tr_);
-        mul2sum(xii, yii, sr, tr, sr_, tr_);
-        xii = vneg(xii);
-        mul2sum(xri, yii, si, ti, si_, ti_);
-        mul2sum(xii, yri, si, ti, si_, ti_);
+        dot_acc(cur.pd[0], cur.dn[0], sr, tr, sr_, tr_);
+        dot_acc(cur.pd[1], cur.dn[1], sr, tr, sr_, tr_);
+        dot_acc(cur.pd[2], cur.dn[2], si, ti, si_, ti_);
+        dot_acc(cur.pd[3], cur.dn[3], si, ti, si_, ti_);
       }
       else
-        mul2sum(xri, yri, sr, tr, sr_, tr_);
+        dot_acc(cur.pd[0], cur.dn[0], sr, tr, sr_, tr_);
+      if (more)
+        cur = nxt;
     }
   }
   const T nur = hsum<L>(sr) + (hsum<L>(tr) + (hsum<L>(sr_) + hsum<L>(tr_)));
@@ -623,13 +653,20 @@ __global__ void __launch_bounds__(256) k_step(SvdArgs<T> a, int st, int g3, int 
   }
   __syncthreads();
   tphase(3);
-  // ---- 4. apply to every pair of the CTA; G is read from the staged copy ----
+  // ---- 4. apply: the CTA's pairs concurrently, blockDim/P threads each; G is read from
+  // the staged copy ----
   unsigned long long mG = 0ull, mV = 0ull;
   unsigned chmask = 0u;  // bit 2j: column p of pair j changed, bit 2j+1: column q
   for (int j = 0; j < np; ++j) {
+    const int cj = ps[j].code;
+    if (!ps[j].skip)
+      chmask |= ((cj == 3 || cj == -3) ? 2u : ((cj == 2 || cj == -2) ? 3u : 0u)) << (2 * j);
+  }
+  const int TPP = (int)blockDim.x / P;
+  const int j = tid / TPP;
+  const int ltid = tid - j * TPP;
+  if (j < np && !ps[j].skip) {
     const PairState<T> s = ps[j];
-    if (s.skip)
-      continue;
     const int code = s.code;
     const long long p = colp(j), q = colq(j);
     T *Gp = a.G + p * a.ldG, *Gq = a.G + q * a.ldG, *Vp = a.V + p * a.ldV, *Vq = a.V + q * a.ldV;
@@ -639,12 +676,12 @@ __global__ void __launch_bounds__(256) k_step(SvdArgs<T> a, int st, int g3, int 
     if (code == 1) {
     }
     else if (code == -1) {
-      for (long long i = tid; i < a.m; i += blockDim.x) {
+      for (long long i = ltid; i < a.m; i += TPP) {
         const T x = rp[i], y = rq[i];
         Gp[i] = y; Gq[i] = x;
         if (CPLX) { const T xi = rpi[i], yi = rqi[i]; Gip[i] = yi; Giq[i] = xi; }
       }
-      for (long long i = tid; i < a.n; i += blockDim.x) {
+      for (long long i = ltid; i < a.n; i += TPP) {
         T t = Vp[i]; Vp[i] = Vq[i]; Vq[i] = t;
         if (CPLX) { t = Vip[i]; Vip[i] = Viq[i]; Viq[i] = t; }
       }
@@ -658,7 +695,7 @@ __global__ void __launch_bounds__(256) k_step(SvdArgs<T> a, int st, int g3, int 
         const T ff = F::div(fy, fx);
         const T tfr = vneg(s.a21r) * ff;
         const T tfi = CPLX ? (s.a21i * ff) : (T)0;
-        for (long long i = tid; i < a.m; i += blockDim.x) {
+        for (long long i = ltid; i < a.m; i += TPP) {
           if (CPLX) {
             const T xri_ = scale2(rp[i], nx), xii_ = scale2(rpi[i], nx);
             const T yri_ = scale2(rq[i], ny), yii_ = scale2(rqi[i], ny);
@@ -683,7 +720,7 @@ __global__ void __launch_bounds__(256) k_step(SvdArgs<T> a, int st, int g3, int 
         const T ff = F::div(fx, fy);
         const T tfr = vneg(s.a21r) * ff;
         const T tfi = CPLX ? (vneg(s.a21i) * ff) : (T)0;
-        for (long long i = tid; i < a.m; i += blockDim.x) {
+        for (long long i = ltid; i < a.m; i += TPP) {
           if (CPLX) {
             const T yri = rq[i], yii = rqi[i], xri = rp[i], xii = rpi[i];
             Gp[i] = yri; Gip[i] = yii;
@@ -707,34 +744,32 @@ __global__ void __launch_bounds__(256) k_step(SvdArgs<T> a, int st, int g3, int 
             amax(mG, u);
           }
         }
-        for (long long i = tid; i < a.n; i += blockDim.x) {
+        for (long long i = ltid; i < a.n; i += TPP) {
           T t = Vp[i]; Vp[i] = Vq[i]; Vq[i] = t;
           if (CPLX) { t = Vip[i]; Vip[i] = Viq[i]; Viq[i] = t; }
         }
-        if (tid == 0) {
+        if (ltid == 0) {
           a.eS[p] = s.eq; a.eS[q] = s.ep;
           a.fS[p] = s.fq; a.fS[q] = s.fp;
         }
       }
-      chmask |= 2u << (2 * j);
     }
     else {
       // rotation (src/djrot.c, src/djrotf.c, src/zjrot.c, src/zjrotf.c); code -2 permutes
       const bool perm = (code == -2);
       const T c = s.c, at = s.cat, sat = s.sat;
       // the reference marks both columns as changed after any rotation (src/dvjsvd.c:573)
-      chmask |= 3u << (2 * j);
       const bool real_rot = (!CPLX) || (sat == (T)0);
       const bool cone = (c == (T)1);
       if (real_rot && at == (T)0) {
         // c == 1: identity (or a swap when permuting); c != 1 "never happens" (-4 / -10)
         if (cone && perm) {
-          for (long long i = tid; i < a.m; i += blockDim.x) {
+          for (long long i = ltid; i < a.m; i += TPP) {
             const T x = rp[i], y = rq[i];
             Gp[i] = y; Gq[i] = x; rp[i] = y; rq[i] = x;
             if (CPLX) { const T xi = rpi[i], yi = rqi[i]; Gip[i] = yi; Giq[i] = xi; rpi[i] = yi; rqi[i] = xi; }
           }
-          for (long long i = tid; i < a.n; i += blockDim.x) {
+          for (long long i = ltid; i < a.n; i += TPP) {
             T t = Vp[i]; Vp[i] = Vq[i]; Vq[i] = t;
             if (CPLX) { t = Vip[i]; Vip[i] = Viq[i]; Viq[i] = t; }
           }
@@ -746,7 +781,7 @@ __global__ void __launch_bounds__(256) k_step(SvdArgs<T> a, int st, int g3, int 
         for (int pl = 0; pl < (CPLX ? 2 : 1); ++pl) {
           T *X = pl ? Gip : Gp, *Y = pl ? Giq : Gq, *RX = pl ? rpi : rp, *RY = pl ? rqi : rq;
           T *DX = perm ? Y : X, *DY = perm ? X : Y, *RDX = perm ? RY : RX, *RDY = perm ? RX : RY;
-          for (long long i = tid; i < a.m; i += blockDim.x) {
+          for (long long i = ltid; i < a.m; i += TPP) {
             const T x = RX[i], y = RY[i];
             T u = F::fma_(y, at, x);
             T w = F::fma_(vneg(x), at, y);
@@ -757,7 +792,7 @@ __global__ void __launch_bounds__(256) k_step(SvdArgs<T> a, int st, int g3, int 
           }
           T *XV = pl ? Vip : Vp, *YV = pl ? Viq : Vq;
           T *DXV = perm ? YV : XV, *DYV = perm ? XV : YV;
-          for (long long i = tid; i < a.n; i += blockDim.x) {
+          for (long long i = ltid; i < a.n; i += TPP) {
             const T x = XV[i], y = YV[i];
             T u = F::fma_(y, at, x);
             T w = F::fma_(vneg(x), at, y);
@@ -774,7 +809,7 @@ __global__ void __launch_bounds__(256) k_step(SvdArgs<T> a, int st, int g3, int 
           const T *Rxr = mat ? Vp : rp, *Rxi = mat ? Vip : rpi, *Ryr = mat ? Vq : rq, *Ryi = mat ? Viq : rqi;
           const long long rows = mat ? a.n : a.m;
           unsigned long long &mm = mat ? mV : mG;
-          for (long long i = tid; i < rows; i += blockDim.x) {
+          for (long long i = ltid; i < rows; i += TPP) {
             const T x_r = Rxr[i], x_i = Rxi[i], y_r = Ryr[i], y_i = Ryi[i];
             T ar = F::fma_(y_r, cta, F::fma_(vneg(y_i), sta, x_r));
             T ai = F::fma_(y_r, sta, F::fma_(y_i, cta, x_i));
