@@ -149,3 +149,32 @@ def test_special_golden(vj, kind, tag, sgn):
     assert r[0] == 1
     for name, arr in zip(NAMES["c" if kind in "zc" else "r"], r[1:]):
         assert same(arr, g[f"{tag}_{name}"]), (kind, tag, name)
+
+
+def test_host_paths_agree(vj, tmp_path):
+    """the staged host path (VJ_STAGED=1) and the direct-read host path give the same bits"""
+    import subprocess
+    import sys
+    script = (
+        "import sys, numpy as np\n"
+        "sys.path.insert(0, %r)\n"
+        "import vecjac_gb300 as vj\n"
+        "from vecjac_gb300 import workloads as W\n"
+        "for k in 'dzsc':\n"
+        "    ins = W.pairs2x2(k, 1 << 20, seed=21)\n"
+        "    r = vj.bjac2(k, -(1 << 20), *ins)\n"
+        "    assert r[0] == 1\n"
+        "    np.savez(%r + '/' + k + '.npz', *r[1:])\n") 
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    outs = {}
+    for mode in ("0", "1"):
+        d = tmp_path / mode
+        d.mkdir()
+        env = dict(os.environ, VJ_STAGED=mode)
+        subprocess.run([sys.executable, "-c", script % (root, str(d))], check=True, env=env)
+        outs[mode] = d
+    for k in "dzsc":
+        a = np.load(outs["0"] / (k + ".npz"))
+        b = np.load(outs["1"] / (k + ".npz"))
+        for name in a.files:
+            assert same(a[name], b[name]), (k, name)

@@ -132,10 +132,10 @@ static vj_fint bjac2_dev(vj_fint n, int internal, const T *a11, const T *a22, co
   return (e == cudaSuccess) ? 1 : VJ_ERR_CUDA;
 }
 
-// Host-pointer form. Where the GPU can address pageable host memory the kernel runs on
-// the caller's arrays; otherwise chunks of the batch are staged through device buffers on
-// two streams (copy in, compute, copy out), so that the copies of one chunk overlap the
-// kernel of the other. VJ_STAGED=1 in the environment forces the staged form.
+// Host-pointer form. Where the GPU can read pageable host memory the kernel reads the
+// caller's inputs in place; otherwise chunks of the batch are staged through device
+// buffers on two streams (copy in, compute, copy out), so that the copies of one chunk
+// overlap the kernel of the other. VJ_STAGED=1 in the environment forces the staged form.
 template <typename T, bool CPLX>
 static vj_fint bjac2_host(vj_fint n, int internal, const T *a11, const T *a22, const T *a21r, const T *a21i, T *c,
                           T *cat, T *sat, T *l1, T *l2, unsigned *p)
@@ -148,19 +148,63 @@ static vj_fint bjac2_host(vj_fint n, int internal, const T *a11, const T *a22, c
   const long long nn = (n < 0) ? -n : n;
   if (!nn)
     return 1;
-  // On a GPU that reads and writes pageable host memory coherently (Grace-Blackwell:
-  // NVLink-C2C with address translation), the kernel streams the caller's arrays
-  // directly: no staging copies, and the link is the only bound.
+  // On a GPU that reads pageable host memory coherently (Grace-Blackwell: NVLink-C2C with
+  // address translation), the kernel reads the caller's inputs in place and writes its
+  // outputs to device buffers, whose copies back to the caller's arrays overlap the
+  // kernel of the next chunk. (GPU stores into pageable host memory are slower than the
+  // copy engines, so outputs are not written in place.) The masked i-variant keeps the
+  // caller's outputs for unprocessed groups and takes the fully staged path below.
   auto al16 = [](const void *q) { return q == nullptr || !((uintptr_t)q & 15u); };
-  if (host::pageable_access() && al16(a11) && al16(a22) && al16(a21r) && al16(a21i) && al16(c) && al16(cat) &&
-      al16(sat) && al16(l1) && al16(l2)) {
+  if (!internal && host::pageable_access() && al16(a11) && al16(a22) && al16(a21r) && al16(a21i)) {
+    const long long chunk = host::bjac2_chunk(nn, sizeof(T), CPLX, LANES);
+    const int nout = CPLX ? 5 : 4;
+    T *hout[5] = {c, cat, CPLX ? sat : l1, CPLX ? l1 : l2, CPLX ? l2 : nullptr};
+    const size_t per = (size_t)chunk * sizeof(T);
+    const size_t pwords = (size_t)(chunk / LANES) * sizeof(unsigned);
+    const size_t slot = ((nout * per + pwords) + 255u) & ~(size_t)255u;
+    host::Staging &stg = host::staging();
+    if (!stg.reserve(2 * slot))
+      return VJ_ERR_NOMEM;
     cudaStream_t st[2];
     if (!host::streams2(st))
       return VJ_ERR_CUDA;
-    const vj_fint r = bjac2_dev<T, CPLX>(n, internal, a11, a22, a21r, a21i, c, cat, sat, l1, l2, p, st[0]);
-    if (r < 0)
-      return r;
-    return (cudaStreamSynchronize(st[0]) == cudaSuccess) ? 1 : VJ_ERR_CUDA;
+    auto copy_back = [&](int b, long long off, long long cnt) -> bool {
+      char *base = stg.ptr + (size_t)b * slot;
+      const size_t bytes = (size_t)cnt * sizeof(T);
+      for (int k = 0; k < nout; ++k)
+        if (cudaMemcpyAsync(hout[k] + off, base + k * per, bytes, cudaMemcpyDeviceToHost, st[b]) != cudaSuccess)
+          return false;
+      return cudaMemcpyAsync(p + off / LANES, base + nout * per, (size_t)(cnt / LANES) * sizeof(unsigned),
+                             cudaMemcpyDeviceToHost, st[b]) == cudaSuccess;
+    };
+    long long prev_off = -1, prev_cnt = 0;
+    int prev_b = 0;
+    for (long long off = 0, it = 0; off < nn; off += chunk, ++it) {
+      const long long cnt = (nn - off < chunk) ? (nn - off) : chunk;
+      const int b = (int)(it & 1);
+      char *base = stg.ptr + (size_t)b * slot;
+      T *dout[5];
+      for (int k = 0; k < nout; ++k)
+        dout[k] = reinterpret_cast<T *>(base + k * per);
+      unsigned *dp = reinterpret_cast<unsigned *>(base + nout * per);
+      const vj_fint sn = (n < 0) ? -cnt : cnt;
+      const vj_fint r = bjac2_dev<T, CPLX>(sn, 0, a11 + off, a22 + off, a21r + off, CPLX ? a21i + off : nullptr,
+                                           dout[0], dout[1], CPLX ? dout[2] : nullptr, CPLX ? dout[3] : dout[2],
+                                           CPLX ? dout[4] : dout[3], dp, st[b]);
+      if (r < 0)
+        return r;
+      // while this chunk computes, copy the previous one back (its stream is in order)
+      if (prev_off >= 0 && !copy_back(prev_b, prev_off, prev_cnt))
+        return VJ_ERR_CUDA;
+      prev_off = off;
+      prev_cnt = cnt;
+      prev_b = b;
+    }
+    if (prev_off >= 0 && !copy_back(prev_b, prev_off, prev_cnt))
+      return VJ_ERR_CUDA;
+    if (cudaStreamSynchronize(st[0]) != cudaSuccess || cudaStreamSynchronize(st[1]) != cudaSuccess)
+      return VJ_ERR_CUDA;
+    return 1;
   }
   const long long chunk = host::bjac2_chunk(nn, sizeof(T), CPLX, LANES);
   const int nin = CPLX ? 4 : 3, nout = CPLX ? 5 : 4;
