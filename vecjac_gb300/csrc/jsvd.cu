@@ -255,20 +255,6 @@ template <typename T> __device__ __forceinline__ void two_sum(T a, T b, T &s, T 
   t = a_ + b_;
 }
 
-// The same (s, t) as 2Sum with half the floating-point operations: for |a| >= |b|,
-// Dekker's Fast2Sum (s = a + b, t = b - (s - a)) also yields the exact rounding error, and
-// the error of a rounded sum is unique, so both transformations agree bit for bit while
-// the accumulators stay finite (they are bounded by 4m here). The magnitude test and the
-// operand swap run on the integer pipes.
-template <typename T> __device__ __forceinline__ void fast_two_sum(T a, T b, T &s, T &t)
-{
-  const bool sw = absbits(b) > absbits(a);
-  const T hi = sw ? b : a, lo = sw ? a : b;
-  const T s_ = hi + lo;
-  s = s_;
-  t = lo - (s_ - hi);
-}
-
 // halving tree over the LANES lanes of warp 0 (GCC's _mm512_reduce_add order); lane 0 has it
 template <int LANES, typename T> __device__ __forceinline__ T hsum(T v)
 {
@@ -309,11 +295,14 @@ __device__ __forceinline__ void dot_terms(const T *xr, const T *xi, const T *yr,
   }
 }
 
+// The accumulation uses branch-free 2Sum: on GB300 a value moving from the FP64 unit to
+// the integer pipes (as Fast2Sum's magnitude test would need) costs several hundred
+// cycles, more than 2Sum's three extra FP64 additions.
 template <typename T>
 __device__ __forceinline__ void dot_acc(T pd, T dn, T &s, T &t, T &s_, T &t_)
 {
-  fast_two_sum(s, pd + t, s, t);
-  fast_two_sum(s_, dn + t_, s_, t_);
+  two_sum(s, pd + t, s, t);
+  two_sum(s_, dn + t_, s_, t_);
 }
 
 template <typename T, bool CPLX>
@@ -679,11 +668,13 @@ __global__ void __launch_bounds__(256) k_step(SvdArgs<T> a, int st, int g3, int 
     if (code == 1) {
     }
     else if (code == -1) {
+      #pragma unroll 4
       for (long long i = ltid; i < a.m; i += TPP) {
         const T x = rp[i], y = rq[i];
         Gp[i] = y; Gq[i] = x;
         if (CPLX) { const T xi = rpi[i], yi = rqi[i]; Gip[i] = yi; Giq[i] = xi; }
       }
+      #pragma unroll 4
       for (long long i = ltid; i < a.n; i += TPP) {
         T t = Vp[i]; Vp[i] = Vq[i]; Vq[i] = t;
         if (CPLX) { t = Vip[i]; Vip[i] = Viq[i]; Viq[i] = t; }
@@ -698,6 +689,7 @@ __global__ void __launch_bounds__(256) k_step(SvdArgs<T> a, int st, int g3, int 
         const T ff = F::div(fy, fx);
         const T tfr = vneg(s.a21r) * ff;
         const T tfi = CPLX ? (s.a21i * ff) : (T)0;
+        #pragma unroll 4
         for (long long i = ltid; i < a.m; i += TPP) {
           if (CPLX) {
             const T xri_ = scale2(rp[i], nx), xii_ = scale2(rpi[i], nx);
@@ -723,6 +715,7 @@ __global__ void __launch_bounds__(256) k_step(SvdArgs<T> a, int st, int g3, int 
         const T ff = F::div(fx, fy);
         const T tfr = vneg(s.a21r) * ff;
         const T tfi = CPLX ? (vneg(s.a21i) * ff) : (T)0;
+        #pragma unroll 4
         for (long long i = ltid; i < a.m; i += TPP) {
           if (CPLX) {
             const T yri = rq[i], yii = rqi[i], xri = rp[i], xii = rpi[i];
@@ -747,6 +740,7 @@ __global__ void __launch_bounds__(256) k_step(SvdArgs<T> a, int st, int g3, int 
             amax(mG, u);
           }
         }
+        #pragma unroll 4
         for (long long i = ltid; i < a.n; i += TPP) {
           T t = Vp[i]; Vp[i] = Vq[i]; Vq[i] = t;
           if (CPLX) { t = Vip[i]; Vip[i] = Viq[i]; Viq[i] = t; }
@@ -767,11 +761,13 @@ __global__ void __launch_bounds__(256) k_step(SvdArgs<T> a, int st, int g3, int 
       if (real_rot && at == (T)0) {
         // c == 1: identity (or a swap when permuting); c != 1 "never happens" (-4 / -10)
         if (cone && perm) {
+          #pragma unroll 4
           for (long long i = ltid; i < a.m; i += TPP) {
             const T x = rp[i], y = rq[i];
             Gp[i] = y; Gq[i] = x; rp[i] = y; rq[i] = x;
             if (CPLX) { const T xi = rpi[i], yi = rqi[i]; Gip[i] = yi; Giq[i] = xi; rpi[i] = yi; rqi[i] = xi; }
           }
+          #pragma unroll 4
           for (long long i = ltid; i < a.n; i += TPP) {
             T t = Vp[i]; Vp[i] = Vq[i]; Vq[i] = t;
             if (CPLX) { t = Vip[i]; Vip[i] = Viq[i]; Viq[i] = t; }
@@ -784,6 +780,7 @@ __global__ void __launch_bounds__(256) k_step(SvdArgs<T> a, int st, int g3, int 
         for (int pl = 0; pl < (CPLX ? 2 : 1); ++pl) {
           T *X = pl ? Gip : Gp, *Y = pl ? Giq : Gq, *RX = pl ? rpi : rp, *RY = pl ? rqi : rq;
           T *DX = perm ? Y : X, *DY = perm ? X : Y, *RDX = perm ? RY : RX, *RDY = perm ? RX : RY;
+          #pragma unroll 4
           for (long long i = ltid; i < a.m; i += TPP) {
             const T x = RX[i], y = RY[i];
             T u = F::fma_(y, at, x);
@@ -795,6 +792,7 @@ __global__ void __launch_bounds__(256) k_step(SvdArgs<T> a, int st, int g3, int 
           }
           T *XV = pl ? Vip : Vp, *YV = pl ? Viq : Vq;
           T *DXV = perm ? YV : XV, *DYV = perm ? XV : YV;
+          #pragma unroll 4
           for (long long i = ltid; i < a.n; i += TPP) {
             const T x = XV[i], y = YV[i];
             T u = F::fma_(y, at, x);
@@ -812,6 +810,7 @@ __global__ void __launch_bounds__(256) k_step(SvdArgs<T> a, int st, int g3, int 
           const T *Rxr = mat ? Vp : rp, *Rxi = mat ? Vip : rpi, *Ryr = mat ? Vq : rq, *Ryi = mat ? Viq : rqi;
           const long long rows = mat ? a.n : a.m;
           unsigned long long &mm = mat ? mV : mG;
+          #pragma unroll 4
           for (long long i = ltid; i < rows; i += TPP) {
             const T x_r = Rxr[i], x_i = Rxi[i], y_r = Ryr[i], y_i = Ryi[i];
             T ar = F::fma_(y_r, cta, F::fma_(vneg(y_i), sta, x_r));
