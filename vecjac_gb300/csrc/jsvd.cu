@@ -433,12 +433,11 @@ template <typename T> __device__ __forceinline__ void amax(unsigned long long &m
   m = (b > m) ? b : m;
 }
 
-// Pairs handled by one CTA. The dot product of pair j runs on the first LANES lanes of
-// warp j: an SM executes FP64 instructions on four sub-partition units (warps 0-3 of a
-// CTA land on different ones), each taking about four cycles per active lane, so one
-// dot warp per sub-partition uses the whole SM's FP64 rate while the accumulation chains
-// of the four pairs run concurrently.
-template <typename T> struct ppc { static constexpr int P = 4; };
+// Pairs handled by one CTA: the LANES-wide dot of pair j runs on lanes [j LANES,
+// (j+1) LANES) of warp 0. GB300's FP64 unit accepts about one warp instruction every 19
+// cycles per SM whatever the number of active lanes, so the four FP64 dot products of a
+// CTA share every FP64 instruction (32 active lanes) instead of issuing four.
+template <typename T> struct ppc { static constexpr int P = 32 / svdc<T>::LANES; };
 
 template <typename T, bool CPLX, bool TRACKV, bool STAGE>
 __global__ void __launch_bounds__(256) k_step(SvdArgs<T> a, int st, int g3, int last)
@@ -553,10 +552,10 @@ __global__ void __launch_bounds__(256) k_step(SvdArgs<T> a, int st, int g3, int 
   }
   __syncthreads();
   tphase(1);
-  // ---- 2. scaled dot products: pair j on lanes [0, L) of warp j ----
-  if (warp < P) {
-    const int j = warp;
-    const bool act = (j < np) && (lane < L);
+  // ---- 2. scaled dot products: pair j on lanes [j L, (j+1) L) of warp 0 ----
+  if (warp == 0) {
+    const int j = lane / L;
+    const bool act = (j < np);
     const int jj = act ? j : 0;
     const long long p = colp(jj), q = colq(jj);
     const T ep = a.eS[p], fp_ = a.fS[p], eq = a.eS[q], fq = a.fS[q];
@@ -565,7 +564,7 @@ __global__ void __launch_bounds__(256) k_step(SvdArgs<T> a, int st, int g3, int 
     pair_dot<T, CPLX>(a, rcol(jj, 1), CPLX ? rcol(jj, 3) : nullptr, rcol(jj, 0), CPLX ? rcol(jj, 2) : nullptr, eq,
                       ep, fq, fp_, live, zr, zi);
     tphase(2);
-    if (act && lane == 0) {
+    if (act && (lane % L) == 0) {
       PairState<T> &s = ps[j];
       s.ep = ep; s.fp = fp_; s.eq = eq; s.fq = fq;
       if (!live) {
