@@ -76,7 +76,7 @@ __device__ __forceinline__ unsigned rjac2(T a1, T a2, T ar, T &c, T &at, T &l1, 
     const angle<T> g = jac_angle(a1, a2, ab, ad);
     t1 = g.t1; s2 = g.s2; s1 = g.s1;
     L1 = qdiv(F::fma_(t1, F::fma_(a2, t1, ab), a1), s2);
-    L2 = qdiv(F::fma_(t1, F::fma_(a1, t1, vneg(ab)), a2), s2);
+    L2 = qdiv(F::fma_(t1, F::fma_(a1, t1, -ab), a2), s2);
     l1 = scale2(L1, -es);
     l2 = scale2(L2, -es);
   }
@@ -138,7 +138,7 @@ __device__ __forceinline__ unsigned cjac2(T a1, T a2, T ar, T ai, T &c, T &cat, 
     const angle<T> g = jac_angle(a1, a2, ab, ad);
     t1 = g.t1; s2 = g.s2; s1 = g.s1;
     L1 = qdiv(F::fma_(t1, F::fma_(a2, t1, ab), a1), s2);
-    L2 = qdiv(F::fma_(t1, F::fma_(a1, t1, vneg(ab)), a2), s2);
+    L2 = qdiv(F::fma_(t1, F::fma_(a1, t1, -ab), a2), s2);
     l1 = scale2(L1, -es);
     l2 = scale2(L2, -es);
   }

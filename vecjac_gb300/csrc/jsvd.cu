@@ -282,16 +282,17 @@ __device__ __forceinline__ void dot_terms(const T *xr, const T *xi, const T *yr,
   if (CPLX) {
     const T yii = scale2(yi[i], ny);
     const T xii = scale2(xi[i], nx);
-    const T xs[4] = {xri, xii, xri, vneg(xii)}, ys[4] = {yri, yii, yii, yri};
+    // (negations are written as FP negations: the FMA folds them, with the same bits)
+    const T xs[4] = {xri, xii, xri, -xii}, ys[4] = {yri, yii, yii, yri};
 #pragma unroll
     for (int k = 0; k < 4; ++k) {
       d.pd[k] = fp<T>::mul_rd(xs[k], ys[k]);
-      d.dn[k] = fp<T>::fma_(xs[k], ys[k], vneg(d.pd[k]));
+      d.dn[k] = fp<T>::fma_(xs[k], ys[k], -d.pd[k]);
     }
   }
   else {
     d.pd[0] = fp<T>::mul_rd(xri, yri);
-    d.dn[0] = fp<T>::fma_(xri, yri, vneg(d.pd[0]));
+    d.dn[0] = fp<T>::fma_(xri, yri, -d.pd[0]);
   }
 }
 
@@ -317,9 +318,10 @@ __device__ void pair_dot(const SvdArgs<T> &a, const T *xr, const T *xi, const T 
     DotTerms<T, CPLX> cur, nxt;
     dot_terms<T, CPLX>(xr, xi, yr, yi, lane, nx, ny, cur);
     for (long long i = lane; i < a.m; i += L) {
-      const bool more = (i + L < a.m);
-      if (more)
-        dot_terms<T, CPLX>(xr, xi, yr, yi, i + L, nx, ny, nxt);
+      // the terms of the next element (of this one again on the last pass, unused), with
+      // no branch so that they interleave with the accumulation below
+      const long long inx = (i + L < a.m) ? (i + L) : i;
+      dot_terms<T, CPLX>(xr, xi, yr, yi, inx, nx, ny, nxt);
       if (CPLX) {
         dot_acc(cur.pd[0], cur.dn[0], sr, tr, sr_, tr_);
         dot_acc(cur.pd[1], cur.dn[1], sr, tr, sr_, tr_);
@@ -328,8 +330,7 @@ __device__ void pair_dot(const SvdArgs<T> &a, const T *xr, const T *xi, const T 
       }
       else
         dot_acc(cur.pd[0], cur.dn[0], sr, tr, sr_, tr_);
-      if (more)
-        cur = nxt;
+      cur = nxt;
     }
   }
   const T nur = hsum<L>(sr) + (hsum<L>(tr) + (hsum<L>(sr_) + hsum<L>(tr_)));
@@ -686,14 +687,14 @@ __global__ void __launch_bounds__(256) k_step(SvdArgs<T> a, int st, int g3, int 
       const int px = (int)ex, py = (int)ey;
       if (code == 3) {
         const T ff = F::div(fy, fx);
-        const T tfr = vneg(s.a21r) * ff;
+        const T tfr = -s.a21r * ff;
         const T tfi = CPLX ? (s.a21i * ff) : (T)0;
         #pragma unroll 4
         for (long long i = ltid; i < a.m; i += TPP) {
           if (CPLX) {
             const T xri_ = scale2(rp[i], nx), xii_ = scale2(rpi[i], nx);
             const T yri_ = scale2(rq[i], ny), yii_ = scale2(rqi[i], ny);
-            const T xr = F::fma_(tfr, xri_, F::fma_(vneg(tfi), xii_, yri_));
+            const T xr = F::fma_(tfr, xri_, F::fma_(-tfi, xii_, yri_));
             const T xi = F::fma_(tfr, xii_, F::fma_(tfi, xri_, yii_));
             const T ur = scale2(xr, py), ui = scale2(xi, py);
             Gq[i] = ur; Giq[i] = ui;
@@ -712,8 +713,8 @@ __global__ void __launch_bounds__(256) k_step(SvdArgs<T> a, int st, int g3, int 
       }
       else {
         const T ff = F::div(fx, fy);
-        const T tfr = vneg(s.a21r) * ff;
-        const T tfi = CPLX ? (vneg(s.a21i) * ff) : (T)0;
+        const T tfr = -s.a21r * ff;
+        const T tfi = CPLX ? (-s.a21i * ff) : (T)0;
         #pragma unroll 4
         for (long long i = ltid; i < a.m; i += TPP) {
           if (CPLX) {
@@ -722,7 +723,7 @@ __global__ void __launch_bounds__(256) k_step(SvdArgs<T> a, int st, int g3, int 
             rp[i] = yri; rpi[i] = yii;
             const T yri_ = scale2(yri, ny), yii_ = scale2(yii, ny);
             const T xri_ = scale2(xri, nx), xii_ = scale2(xii, nx);
-            const T vr = F::fma_(tfr, yri_, F::fma_(vneg(tfi), yii_, xri_));
+            const T vr = F::fma_(tfr, yri_, F::fma_(-tfi, yii_, xri_));
             const T vi = F::fma_(tfr, yii_, F::fma_(tfi, yri_, xii_));
             const T ur = scale2(vr, px), ui = scale2(vi, px);
             Gq[i] = ur; Giq[i] = ui;
@@ -783,7 +784,7 @@ __global__ void __launch_bounds__(256) k_step(SvdArgs<T> a, int st, int g3, int 
           for (long long i = ltid; i < a.m; i += TPP) {
             const T x = RX[i], y = RY[i];
             T u = F::fma_(y, at, x);
-            T w = F::fma_(vneg(x), at, y);
+            T w = F::fma_(-x, at, y);
             if (!cone) { u = u * c; w = w * c; }
             DX[i] = u; DY[i] = w;
             RDX[i] = u; RDY[i] = w;
@@ -795,7 +796,7 @@ __global__ void __launch_bounds__(256) k_step(SvdArgs<T> a, int st, int g3, int 
           for (long long i = ltid; i < a.n; i += TPP) {
             const T x = XV[i], y = YV[i];
             T u = F::fma_(y, at, x);
-            T w = F::fma_(vneg(x), at, y);
+            T w = F::fma_(-x, at, y);
             if (!cone) { u = u * c; w = w * c; }
             DXV[i] = u; DYV[i] = w;
             if (TRACKV) { amax(mV, u); amax(mV, w); }
@@ -803,7 +804,7 @@ __global__ void __launch_bounds__(256) k_step(SvdArgs<T> a, int st, int g3, int 
         }
       }
       else {
-        const T cta = at, sta = sat, cna = vneg(at);
+        const T cta = at, sta = sat, cna = -at;
         for (int mat = 0; mat < 2; ++mat) {
           T *Xr = mat ? Vp : Gp, *Xi = mat ? Vip : Gip, *Yr = mat ? Vq : Gq, *Yi = mat ? Viq : Giq;
           const T *Rxr = mat ? Vp : rp, *Rxi = mat ? Vip : rpi, *Ryr = mat ? Vq : rq, *Ryi = mat ? Viq : rqi;
@@ -812,9 +813,9 @@ __global__ void __launch_bounds__(256) k_step(SvdArgs<T> a, int st, int g3, int 
           #pragma unroll 4
           for (long long i = ltid; i < rows; i += TPP) {
             const T x_r = Rxr[i], x_i = Rxi[i], y_r = Ryr[i], y_i = Ryi[i];
-            T ar = F::fma_(y_r, cta, F::fma_(vneg(y_i), sta, x_r));
+            T ar = F::fma_(y_r, cta, F::fma_(-y_i, sta, x_r));
             T ai = F::fma_(y_r, sta, F::fma_(y_i, cta, x_i));
-            T br = F::fma_(x_r, cna, F::fma_(vneg(x_i), sta, y_r));
+            T br = F::fma_(x_r, cna, F::fma_(-x_i, sta, y_r));
             T bi = F::fma_(x_r, sta, F::fma_(x_i, cna, y_i));
             if (!cone) { ar = ar * c; ai = ai * c; br = br * c; bi = bi * c; }
             if (perm) { Yr[i] = ar; Yi[i] = ai; Xr[i] = br; Xi[i] = bi; }
