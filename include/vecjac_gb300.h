@@ -117,6 +117,19 @@ vj_fint vj_cvjsvd_dev(vj_fnat m, vj_fnat n, float *Gr, vj_fnat ldGr, float *Gi, 
                       vj_fnat ldVr, float *Vi, vj_fnat ldVi, float *eS, float *fS, const unsigned *js,
                       unsigned stp, unsigned swp, int preset, void *stream);
 
+/* Allocation-free FP64 SVD. No counterpart in the reference. For callers that must not
+ * allocate GPU memory while they run -- for example code that is being captured into a
+ * CUDA graph, or an application whose memory pool owns the whole device -- this form
+ * takes only the matrices and the outputs: the pivot table (strategy 2 or 4, generated on
+ * the GPU) and the control block live in a fixed 1 MiB + 512 B device array inside the
+ * library, present on every GPU that loads it until the process exits. n must not exceed
+ * 512 (VJ_ERR_ARG otherwise); the other arguments and the result are those of
+ * vj_dvjsvd_dev. The first call on a device looks up that array's address (do it before
+ * any stream capture). Every call shares the array: calls that overlap on the GPU, on any
+ * stream or thread, race and must be serialised by the caller. */
+vj_fint vj_dvjsvd_dev_noalloc(vj_fnat m, vj_fnat n, double *G, vj_fnat ldG, double *V, vj_fnat ldV, double *eS,
+                              double *fS, long strategy, unsigned swp, int preset, void *stream);
+
 /* ---------------- pivot strategy tables ----------------
  * replaces pjs() src/pjs.h:21, src/pjs.c:9: returns a malloc'ed table of *stp rows of n
  * unsigned (n/2 pairs per row, p < q inside a pair), generated on the GPU, or NULL.

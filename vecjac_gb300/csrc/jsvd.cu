@@ -27,6 +27,7 @@
 #include <cfloat>
 #include <cmath>
 #include <cstdio>
+#include <mutex>
 #include <vector>
 
 #include <cuda_runtime.h>
@@ -969,7 +970,7 @@ static inline bool is_al(const void *p)
 template <typename T, bool CPLX>
 static vj_fint svd_dev(vj_fnat m_, vj_fnat n_, T *G, vj_fnat ldG, T *Gi, vj_fnat ldGi, T *V, vj_fnat ldV, T *Vi,
                        vj_fnat ldVi, T *eS, T *fS, const unsigned *js, unsigned stp, unsigned swp, int preset,
-                       cudaStream_t s)
+                       cudaStream_t s, unsigned char *scratch = nullptr)
 {
   constexpr int L = svdc<T>::LANES;
   const long long m = (long long)m_, n = (long long)n_;
@@ -999,11 +1000,15 @@ static vj_fint svd_dev(vj_fnat m_, vj_fnat n_, T *G, vj_fnat ldG, T *Gi, vj_fnat
   if (!host::gpu_ready())
     return VJ_ERR_NO_GPU;
   const long long E_MG = CPLX ? -92 : -80, E_MV = CPLX ? -104 : -92, E_MVZ = CPLX ? -17 : -13;
-  host::Staging &stg = host::staging2();
-  if (!stg.reserve(sizeof(SvdGlobal) + 256))
-    return VJ_ERR_NOMEM;
-  SvdGlobal *dg = reinterpret_cast<SvdGlobal *>(stg.ptr);
-  unsigned long long *dmx = reinterpret_cast<unsigned long long *>(stg.ptr + sizeof(SvdGlobal) + 64);
+  unsigned char *ctlmem = scratch;
+  if (!ctlmem) {
+    host::Staging &stg = host::staging2();
+    if (!stg.reserve(sizeof(SvdGlobal) + 256))
+      return VJ_ERR_NOMEM;
+    ctlmem = reinterpret_cast<unsigned char *>(stg.ptr);
+  }
+  SvdGlobal *dg = reinterpret_cast<SvdGlobal *>(ctlmem);
+  unsigned long long *dmx = reinterpret_cast<unsigned long long *>(ctlmem + sizeof(SvdGlobal) + 64);
   const dim3 blk(256);
   auto grid2 = [](long long rows, long long cols) {
     long long gx = (rows + 255) / 256;
@@ -1318,3 +1323,67 @@ vj_fint vj_cvjsvd_dev(vj_fnat m, vj_fnat n, float *Gr, vj_fnat ldGr, float *Gi, 
 }
 
 }  // extern "C"
+
+// ---------------- allocation-free FP64 SVD ----------------
+// Callers that cannot allocate device memory at run time (code running inside a stream
+// being captured into a CUDA graph, or an application that owns every byte of the GPU
+// through its own pool and forbids library allocations) can still run the SVD through
+// vj_dvjsvd_dev_noalloc. It needs no table and no scratch from the caller: its scratch --
+// the control block of the call, the max |a_ij| cell and the pivot table it generates on
+// the GPU -- lives in the file-scope device array below, 1 MiB + 512 bytes that every GPU
+// loading this library holds until the process exits. The table limits it to n <= 512
+// columns (stp * n <= 262144 entries); larger n is rejected with VJ_ERR_ARG.
+namespace vj {
+
+constexpr size_t NOALLOC_CTL = 512;
+constexpr size_t NOALLOC_JS = 262144;  // unsigned entries of the pivot table
+static_assert(sizeof(SvdGlobal) + 64 + 8 <= NOALLOC_CTL, "control block does not fit");
+static __device__ __align__(256) unsigned char vj_noalloc_scratch[NOALLOC_CTL + NOALLOC_JS * sizeof(unsigned)];
+
+// device address of the scratch array, looked up once per device with that device current
+static unsigned char *noalloc_scratch()
+{
+  static std::mutex mu;
+  static unsigned char *addr[64] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64)
+    return nullptr;
+  std::lock_guard<std::mutex> lk(mu);
+  if (!addr[dev]) {
+    void *p = nullptr;
+    if (cudaGetSymbolAddress(&p, vj_noalloc_scratch) != cudaSuccess) {
+      cudaGetLastError();
+      return nullptr;
+    }
+    addr[dev] = static_cast<unsigned char *>(p);
+  }
+  return addr[dev];
+}
+
+}  // namespace vj
+
+extern "C" vj_fint vj_dvjsvd_dev_noalloc(vj_fnat m, vj_fnat n, double *G, vj_fnat ldG, double *V, vj_fnat ldV,
+                                         double *eS, double *fS, long strategy, unsigned swp, int preset,
+                                         void *stream)
+{
+  using namespace vj;
+  if (strategy != 2l && strategy != 4l)
+    return VJ_ERR_ARG;
+  const unsigned long long stp = (strategy == 2l) ? (n ? n - 1ull : 0ull) : n;
+  if (n > 512ull || stp * n > NOALLOC_JS)
+    return VJ_ERR_ARG;
+  if (!host::gpu_ready())
+    return VJ_ERR_NO_GPU;
+  unsigned char *sc = noalloc_scratch();
+  if (!sc)
+    return VJ_ERR_CUDA;
+  unsigned *js = reinterpret_cast<unsigned *>(sc + NOALLOC_CTL);
+  // (odd or tiny n: no table; the SVD's own argument checks report it)
+  if (n >= 2 && !(n & 1ull)) {
+    const vj_fint r = vj_pjs_dev(strategy, (unsigned)n, js, stream);
+    if (r < 0)
+      return r;
+  }
+  return svd_dev<double, false>(m, n, G, ldG, nullptr, ldG, V, ldV, nullptr, ldV, eS, fS, js, (unsigned)stp, swp,
+                                preset, (cudaStream_t)stream, sc);
+}
