@@ -117,6 +117,24 @@ vj_fint vj_cvjsvd_dev(vj_fnat m, vj_fnat n, float *Gr, vj_fnat ldGr, float *Gi, 
                       vj_fnat ldVr, float *Vi, vj_fnat ldVi, float *eS, float *fS, const unsigned *js,
                       unsigned stp, unsigned swp, int preset, void *stream);
 
+/* Batched SVD of `count` independent real matrices in one persistent launch (FP64 d,
+ * FP32 s), each with the result dvjsvd_/svjsvd_ give for it (V := I, pivot strategy 2 or 4
+ * generated on the fly, sweep cap swp). All arrays are on the device: matrix b is
+ * m[b] x n[b] (the reference's rules: m >= n, m % 8 / % 16, (n/2) % 8 / % 16, n <= 512),
+ * column-major with leading dimension m[b] at G + offG[b]; V at V + offV[b] (n x n,
+ * leading dimension n); eS/fS at offS[b]. order (optional, NULL = 0..count-1) is the order
+ * in which CTAs take matrices (largest first balances the tail). info[b] receives the sweep
+ * count or the error code of matrix b. block: 64, 128 or 256 threads per CTA (chosen by
+ * the package's autotuner). Asynchronous on `stream`. No counterpart in the reference
+ * (whose callers loop over dvjsvd_); the per-matrix arithmetic is dvjsvd_'s
+ * (src/dvjsvd.c:40-638). */
+vj_fint vj_dvjsvd_batch_dev(vj_fint count, const long long *m, const long long *n, double *G, const long long *offG,
+                            double *V, const long long *offV, double *eS, double *fS, const long long *offS,
+                            const int *order, long strategy, unsigned swp, long long *info, int block, void *stream);
+vj_fint vj_svjsvd_batch_dev(vj_fint count, const long long *m, const long long *n, float *G, const long long *offG,
+                            float *V, const long long *offV, float *eS, float *fS, const long long *offS,
+                            const int *order, long strategy, unsigned swp, long long *info, int block, void *stream);
+
 /* Allocation-free FP64 SVD. No counterpart in the reference. For callers that must not
  * allocate GPU memory while they run -- for example code that is being captured into a
  * CUDA graph, or an application whose memory pool owns the whole device -- this form

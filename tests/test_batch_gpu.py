@@ -1,0 +1,92 @@
+"""Batched SVD of uneven matrices in one persistent launch (vj_?vjsvd_batch_dev).
+
+Every matrix of the batch must give bit for bit what the oracle restatement gives for
+that matrix padded to the reference's shape rules -- sweep count, U, V, eS, fS -- whatever
+its neighbours in the batch; a zero matrix and a non-finite matrix inside the batch get
+the reference's return values without disturbing the others; the autotuned block size
+and a CUDA-graph replay give the same bits.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def env():
+    from vecjac_gb300 import build
+    build.build()
+    O.build()
+    return O.Restatement()
+
+
+def same(a, b):
+    a, b = np.ascontiguousarray(a), np.ascontiguousarray(b)
+    na, nb = np.isnan(a), np.isnan(b)
+    return a.shape == b.shape and np.array_equal(na, nb) and np.array_equal(a[~na].view(np.uint8),
+                                                                             b[~nb].view(np.uint8))
+
+
+def uneven(count, seed, mmax=96):
+    from vecjac_gb300 import workloads as W
+    rng = np.random.default_rng(seed)
+    mats = []
+    for i in range(count):
+        m = int(rng.integers(16, mmax + 1))
+        n = int(rng.integers(8, m + 1))
+        A, _ = W.svd_matrix(m, n, seed=seed * 1000 + i, lo=-4.0)
+        mats.append(A)
+    return mats
+
+
+@pytest.mark.parametrize("kind", ["d", "s"])
+@pytest.mark.parametrize("strategy", [4, 2])
+def test_batch_vs_oracle(env, kind, strategy):
+    from vecjac_gb300 import batch as B
+    rst = env
+    mats = uneven(24, seed=7 if kind == "d" else 8)
+    mats.append(np.zeros((24, 16)))                        # zero matrix: returns 0
+    bad = np.ones((32, 16))
+    bad[3, 4] = np.inf
+    mats.append(bad)                                         # non-finite: -80
+    res = B.svd_batch(mats, kind, strategy=strategy, block=128)
+    dt = np.float64 if kind == "d" else np.float32
+    for A, r in zip(mats, res):
+        m2, n2 = B.padded_shape(A.shape[0], A.shape[1], kind)
+        P = np.zeros((m2, n2), dt)
+        P[:A.shape[0], :A.shape[1]] = A
+        js, stp = rst.pjs(strategy, n2)
+        o = rst.vjsvd(kind, P, js, stp)
+        assert r[0] == o[0], (A.shape, r[0], o[0])
+        if o[0] < 0:
+            continue
+        for x, y in zip(r[1:], o[1:]):
+            assert same(x, y), A.shape
+
+
+def test_batch_autotune_and_graph(env):
+    import torch
+    from vecjac_gb300 import batch as B
+    mats = uneven(64, seed=11, mmax=160)
+    b = B.Batch(mats, "d")
+    blk = B.autotune(b, 4, sample=32)
+    assert blk in (64, 128, 256)
+    b.run(4, block=blk)
+    torch.cuda.synchronize()
+    first = b.results()
+    ref = B.Batch(mats, "d")
+    ref.run(4, block=64 if blk != 64 else 128)
+    torch.cuda.synchronize()
+    for x, y in zip(first, ref.results()):
+        assert x[0] == y[0]
+        for u, v in zip(x[1:], y[1:]):
+            assert same(u, v)
+    g = B.capture(b, 4, block=blk)
+    g.replay()
+    torch.cuda.synchronize()
+    for x, y in zip(first, b.results()):
+        assert x[0] == y[0]
+        for u, v in zip(x[1:], y[1:]):
+            assert same(u, v)

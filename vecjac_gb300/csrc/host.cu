@@ -70,6 +70,12 @@ Staging &staging()
   return s;
 }
 
+unsigned *batch_queue()
+{
+  static Staging q;
+  return q.reserve(256) ? reinterpret_cast<unsigned *>(q.ptr) : nullptr;
+}
+
 Staging &staging2()
 {
   static Staging s;

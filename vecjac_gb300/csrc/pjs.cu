@@ -16,6 +16,7 @@
 
 #include <cuda_runtime.h>
 
+#include "pjs.cuh"
 #include "vj_host.h"
 
 namespace vj {
@@ -27,24 +28,11 @@ __global__ void k_pjs_rr(unsigned n, unsigned stp, unsigned *t)
   for (unsigned long long w = (unsigned long long)blockIdx.x * blockDim.x + threadIdx.x; w < tot;
        w += (unsigned long long)gridDim.x * blockDim.x) {
     const unsigned s = (unsigned)(w / half), k = (unsigned)(w % half);
-    const unsigned N = n - 1u;
-    unsigned a, b;
-    if (!k) {
-      a = s;
-      b = N;
-    }
-    else {
-      a = (s + k) % N;
-      b = (s + N - k) % N;
-    }
     unsigned *r = t + (size_t)s * n + 2u * k;
-    r[0] = (a < b) ? a : b;
-    r[1] = (a < b) ? b : a;
+    pair_rr(n, s, k, r[0], r[1]);
   }
 }
 
-// modulus ordering: the pairs (i, j), i < j, i + j = s (mod n), in increasing i, then the
-// self-paired couple of an even step
 __global__ void k_pjs_mod(unsigned n, unsigned stp, unsigned *t)
 {
   const unsigned half = n >> 1;
@@ -53,32 +41,7 @@ __global__ void k_pjs_mod(unsigned n, unsigned stp, unsigned *t)
        w += (unsigned long long)gridDim.x * blockDim.x) {
     const unsigned s = (unsigned)(w / half), k = (unsigned)(w % half);
     unsigned *r = t + (size_t)s * n + 2u * k;
-    // the i < j solutions of i + j = s (mod n) in increasing i: for odd s there are n/2 of
-    // them; for even s, n/2 - 1 of them, followed by (s/2, s/2 + n/2)
-    const bool even = !(s & 1u);
-    // enumerate i = 0.. with j = (s - i) mod n, keeping i < j
-    // count of valid i below a bound is computed in closed form: i valid iff i < j(i)
-    // For i <= s: j = s - i, valid iff i < s - i  <=> 2i < s.
-    // For i > s:  j = s + n - i, valid iff 2i < s + n.
-    const unsigned c1 = (s + 1u) >> 1;                   // i in [0, ceil(s/2)) with 2i < s
-    const unsigned lo2 = s + 1u, hi2 = (s + n + 1u) >> 1; // i in [s+1, ceil((s+n)/2))
-    const unsigned c2 = (hi2 > lo2) ? (hi2 - lo2) : 0u;
-    unsigned a, b;
-    if (k < c1) {
-      a = k;
-      b = s - k;
-    }
-    else if (k < c1 + c2) {
-      a = lo2 + (k - c1);
-      b = s + n - a;
-    }
-    else {
-      a = s >> 1;
-      b = a + half;
-      (void)even;
-    }
-    r[0] = a;
-    r[1] = b;
+    pair_mod(n, s, k, r[0], r[1]);
   }
 }
 

@@ -24,6 +24,9 @@ struct Staging {
 Staging &staging();
 Staging &staging2();
 
+// the work-queue counter of the batched SVD (device memory, allocated on first use)
+unsigned *batch_queue();
+
 // two non-blocking streams owned by the library
 bool streams2(cudaStream_t s[2]);
 
