@@ -434,13 +434,91 @@ def bench_svd(args, vj, dist, rank, world, kind, m, n):
             "gpu_launches": int(sweeps + 1) * stp}
 
 
+def gen_uneven(count, seed, kind):
+    """The uneven-batch workload: m ~ U{16..512}, n ~ U{8..m}, A = Q1 diag(sigma) Q2^T with
+    Q1, Q2 from QR of Gaussian matrices and sigma = 10^U(-4, 0) per matrix (host threads)."""
+    from concurrent.futures import ThreadPoolExecutor
+    rng = np.random.default_rng(seed)
+    m = rng.integers(16, 513, count)
+    n = np.array([rng.integers(8, int(mm) + 1) for mm in m])
+    seeds = rng.integers(0, 2 ** 63 - 1, count)
+
+    def one(i):
+        r = np.random.default_rng(int(seeds[i]))
+        q1, _ = np.linalg.qr(r.standard_normal((int(m[i]), int(n[i]))))
+        q2, _ = np.linalg.qr(r.standard_normal((int(n[i]), int(n[i]))))
+        s = 10.0 ** r.uniform(-4.0, 0.0, int(n[i]))
+        return ((q1 * s) @ q2.T).astype(np.float64 if kind == "d" else np.float32)
+
+    with ThreadPoolExecutor(os.cpu_count()) as ex:
+        return list(ex.map(one, range(count)))
+
+
+def bench_batch(args, vj, dist, rank, world, kind):
+    import torch
+    from vecjac_gb300 import batch as B
+    mats = gen_uneven(args.batch_count, 77 + rank, kind)
+    b = B.Batch(mats, kind)
+    blk = B.autotune(b, args.pivot)
+    g = B.capture(b, args.pivot, block=blk)
+    for _ in range(max(0, args.warmup - 1)):
+        g.replay()
+    torch.cuda.synchronize()
+    barrier(dist)
+    with Clocks(torch.cuda.current_device()) as clk:
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(args.steps):
+            g.replay()
+        e1.record()
+        torch.cuda.synchronize()
+    ms = allmax(dist, e0.elapsed_time(e1)) / args.steps
+    info = b.info.cpu().numpy()
+    flops = b.flops(np.maximum(info, 0))
+    # the same matrices one launch sequence per matrix (vj_?vjsvd_dev) on a sample
+    sample = min(args.batch_sample, len(mats))
+    idx = np.random.default_rng(5).choice(len(mats), sample, replace=False)
+    t = 0.0
+    for i in idx:
+        A = mats[i]
+        m2, n2 = B.padded_shape(A.shape[0], A.shape[1], kind)
+        P = np.zeros((m2, n2), A.dtype)
+        P[:A.shape[0], :A.shape[1]] = A
+        js, stp = vj.pjs(args.pivot, n2)
+        Gd = torch.tensor(P.T.copy(), device="cuda")
+        Vd = torch.empty((n2, n2), dtype=Gd.dtype, device="cuda")
+        eS = torch.empty(n2, dtype=Gd.dtype, device="cuda")
+        fS = torch.empty_like(eS)
+        dj = torch.tensor(js.astype(np.int32), device="cuda")
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        vj.vjsvd_dev(kind, m2, n2, Gd, m2, Vd, n2, eS, fS, dj, stp)
+        torch.cuda.synchronize()
+        t += time.perf_counter() - t0
+    per_launch = len(mats) * (t / sample)
+    return {"metric": "batched Jacobi SVD matrices/s (%svjsvd_, uneven sizes)" % kind,
+            "value": round(world * len(mats) / (ms * 1e-3), 2), "unit": "matrices/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 2), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64" if kind == "d" else "f32",
+            "data": "synthetic (m~U[16,512], n~U[8,m], Q1 diag(sigma) Q2^T, sigma=10^U(-4,0))",
+            "config": {"workload": "%d matrices in one persistent launch (CUDA graph), pivot id %d, block %d"
+                       % (len(mats), args.pivot, blk), "errors": int((info < 0).sum()),
+                       "mean_sweeps": float(info[info >= 0].mean())},
+            "flops_per_s": flops / (ms * 1e-3),
+            "one_launch_per_matrix_s_estimate": round(per_launch, 2),
+            "speedup_vs_per_matrix_launches": round(per_launch / (ms * 1e-3), 2),
+            "clocks": clk.summary(), "gpu_launches": 2 * args.steps}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="bjac2", choices=["bjac2", "svd1024", "zsvd"])
+    ap.add_argument("--workload", default="bjac2", choices=["bjac2", "svd1024", "zsvd", "batch_d", "batch_s"])
+    ap.add_argument("--batch-count", type=int, default=20000)
+    ap.add_argument("--batch-sample", type=int, default=40)
     ap.add_argument("--scale", type=int, default=0, help="shrink the 2x2 batches by 2^scale")
     ap.add_argument("--e2e-shift", type=int, default=0, help="further shrink of the e2e batches")
     ap.add_argument("--no-e2e", dest="e2e", action="store_false")
@@ -463,6 +541,8 @@ def main():
         out = bench_bjac2(args, vj, dist, rank, world)
     elif args.workload == "svd1024":
         out = bench_svd(args, vj, dist, rank, world, "d", 1024, 1024)
+    elif args.workload.startswith("batch_"):
+        out = bench_batch(args, vj, dist, rank, world, args.workload[-1])
     else:
         out = bench_svd(args, vj, dist, rank, world, "z", 4096, 2048)
     if rank == 0:
