@@ -93,14 +93,15 @@ class Batch:
 
 
 def autotune(batch, strategy=4, candidates=(64, 128, 256), sample=None):
-    """Pick the CTA size for this batch's size mix: time each candidate on a sample of the
-    largest matrices (CUDA events, after one warm-up) and return the fastest. The choice is
+    """Pick the CTA size for this batch's size mix: time each candidate on a random sample
+    of its matrices (CUDA events, after one warm-up) and return the fastest. The choice is
     cached per (precision, coarse size histogram)."""
     import torch
     key = (batch.kind, tuple(np.histogram(batch.n, bins=[0, 64, 128, 256, 513])[0] > 0))
     if key in _TUNED:
         return _TUNED[key]
-    idx = batch.order_np[:sample or min(batch.count, 1024)]
+    rng = np.random.default_rng(0)
+    idx = rng.choice(batch.count, min(batch.count, sample or 512), replace=False)
     mats = []
     G = batch.G0.cpu().numpy()
     for b in idx:
