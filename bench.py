@@ -10,8 +10,10 @@ Metric: GB/s of algorithmic HBM traffic (56.5 / 72.5 / 28.25 / 36.25 bytes per e
 d / z / s / c: inputs, outputs and the permutation bitmask), whole job. The inputs
 (37 GB) exceed the 129 MB L2 many times over, so no L2 flush is needed between steps.
 
-Other workloads (--workload): "svd1024" (dvjsvd_ on a 1024x1024 FP64 matrix, matrices/s)
-and "zsvd" (zvjsvd_ on 4096x2048 FP64 complex).
+Other workloads (--workload): "svd1024" (dvjsvd_ on a 1024x1024 FP64 matrix, matrices/s),
+"zsvd" (zvjsvd_ on 4096x2048 FP64 complex), "zsvd_mixed"/"dsvd_mixed" (the same matrix
+through the mixed-precision path, with the plain FP64 arm timed beside it), "batch_d"/
+"batch_s" (20,000 uneven real matrices in one persistent launch).
 
 Timing follows the harness contract: W untimed warm-up steps, then K steps between CUDA
 events on the launching stream with a barrier and a device synchronize on both sides,
@@ -434,6 +436,194 @@ def bench_svd(args, vj, dist, rank, world, kind, m, n):
             "gpu_launches": int(sweeps + 1) * stp}
 
 
+def bench_mixed(args, vj, dist, rank, world, kind, m, n):
+    """Mixed-precision SVD (FP32 presweeps, FP64 finish) against the plain FP64 SVD of the
+    same matrix: the mixed path is timed over K steps after W warm-ups, the plain one over
+    --plain-steps runs (it is the slow arm); both sigma sets are compared with the exact
+    sigma of the synthetic matrix."""
+    import torch
+    from vecjac_gb300 import workloads as W
+    cx = kind == "z"
+    A, s = W.svd_matrix(m, n, seed=2024 + rank, complex_=cx)
+    js, stp = vj.pjs(args.pivot, n)
+    Gt = torch.tensor(np.ascontiguousarray(A.real.T), dtype=torch.float64, device="cuda")
+    Git = torch.tensor(np.ascontiguousarray(A.imag.T), dtype=torch.float64, device="cuda") if cx else None
+    G = torch.empty_like(Gt)
+    Gi = torch.empty_like(Gt) if cx else None
+    V = torch.empty((n, n), dtype=torch.float64, device="cuda")
+    Vi = torch.empty_like(V) if cx else None
+    eS = torch.empty(n, dtype=torch.float64, device="cuda")
+    fS = torch.empty_like(eS)
+    djs = torch.tensor(js.astype(np.int32), device="cuda")
+    stream = torch.cuda.current_stream()
+
+    def reset():
+        G.copy_(Gt)
+        if cx:
+            Gi.copy_(Git)
+
+    def mixed():
+        reset()
+        return vj.vjsvd_mixed_dev(kind, m, n, G, m, V, n, eS, fS, djs, stp, Gi=Gi, ldGi=m, Vi=Vi, ldVi=n,
+                                  stream=stream.cuda_stream)
+
+    def plain():
+        reset()
+        return vj.vjsvd_dev(kind, m, n, G, m, V, n, eS, fS, djs, stp, Gi=Gi, ldGi=m, Vi=Vi, ldVi=n,
+                            stream=stream.cuda_stream)
+
+    def sigma_err():
+        sig = fS.cpu().numpy() * np.exp2(eS.cpu().numpy())
+        srt = np.sort(sig)[::-1]
+        return srt, float(np.max(np.abs(srt - s) / s)), float(np.max(np.abs(srt - s)) / s[0])
+
+    def timed(fn, k):
+        torch.cuda.synchronize()
+        barrier(dist)
+        t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0.record(stream)
+        for _ in range(k):
+            r = fn()
+        t1.record(stream)
+        torch.cuda.synchronize()
+        return allmax(dist, t0.elapsed_time(t1)) / k, r
+
+    for _ in range(args.warmup):
+        mixed()
+    with Clocks(torch.cuda.current_device()) as clk:
+        ms, (sw64, sw32) = timed(mixed, args.steps)
+    sig_m, rel_m, nrm_m = sigma_err()
+    out = {"metric": "Jacobi SVD matrices/s (%svjsvd mixed FP32->FP64)" % kind,
+           "value": round(world * 1000.0 / ms, 5), "unit": "matrices/s", "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic (Haar factors, log-uniform sigma in [1e-6, 1])",
+           "config": {"workload": "%svjsvd_ %dx%d mixed precision (FP32 presweeps, 2 Newton-Schulz steps, FP64 "
+                                  "finishing sweeps), pivot strategy id %d" % (kind, m, n, args.pivot),
+                      "sweeps_fp32": int(sw32), "sweeps_fp64": int(sw64),
+                      "max_rel_sigma_err_vs_exact": rel_m, "max_sigma_err_over_sigma_max": nrm_m},
+           "clocks": clk.summary()}
+    if args.plain_steps > 0:
+        pms, psw = timed(plain, args.plain_steps)
+        sig_p, rel_p, nrm_p = sigma_err()
+        out["plain"] = {"ms_per_step": round(pms, 3), "steps": args.plain_steps, "sweeps": int(psw),
+                        "max_rel_sigma_err_vs_exact": rel_p, "max_sigma_err_over_sigma_max": nrm_p,
+                        "max_rel_sigma_diff_mixed_vs_plain": float(np.max(np.abs(sig_m - sig_p) / sig_p))}
+        out["speedup_vs_plain"] = round(pms / ms, 3)
+    return out
+
+
+def bench_diff(args, vj, dist, rank, world):
+    """Differentiable batched SVD: 4096 FP32 matrices 128x64, sigma uniform in [0.1, 10] with
+    relative gaps >= 1e-3, loss = sum_i w_i s_i + <G_U, U_k> + <G_V, V_k>, k = 16. One step =
+    forward (batched SVD in one persistent launch, sort, sign fix, loss) + backward (the
+    adjoint kernel). The adjoint launch is also timed alone (its own CUDA events)."""
+    import torch
+    from vecjac_gb300 import autodiff as AD
+    count, m, n, k = args.diff_count, 128, 64, 16
+    A64, _ = AD.spaced_sigma_matrices(count, m, n, seed=91 + rank)
+    rng = np.random.default_rng(92 + rank)
+    w, GU, GV = rng.standard_normal((count, n)), rng.standard_normal((count, m, k)), rng.standard_normal((count, n, k))
+    t32 = lambda x: torch.tensor(x, dtype=torch.float32, device="cuda")
+    A, w32, GU32, GV32 = t32(A64), t32(w), t32(GU), t32(GV)
+
+    def step():
+        X = A.clone().requires_grad_(True)
+        S, Uk, Vk = AD.svd_k(X, k)
+        L = (w32 * S).sum() + (GU32 * Uk).sum() + (GV32 * Vk).sum()
+        L.backward()
+        return X.grad
+
+    for _ in range(args.warmup):
+        g = step()
+    torch.cuda.synchronize()
+    barrier(dist)
+    with Clocks(torch.cuda.current_device()) as clk:
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(args.steps):
+            g = step()
+        e1.record()
+        torch.cuda.synchronize()
+    ms = allmax(dist, e0.elapsed_time(e1)) / args.steps
+    # the adjoint kernel alone, on the saved factors of one forward
+    with torch.no_grad():
+        S, U, V, _ = AD.svd_batch_dev(A)
+        S, U, V = AD._sort_and_fix(S, U, V)
+    Uc, Vc = U.contiguous(), V.contiguous()
+    for _ in range(3):
+        AD.adjoint(Uc, S, Vc, w32, GU32, GV32)
+    torch.cuda.synchronize()
+    a0, a1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = 20
+    a0.record()
+    for _ in range(reps):
+        AD.adjoint(Uc, S, Vc, w32, GU32, GV32)
+    a1.record()
+    torch.cuda.synchronize()
+    adj_ms = a0.elapsed_time(a1) / reps
+    adj_bytes = count * 4.0 * (m * n + n * n + m * k + n * k + 2 * n + m * n)
+    adj_flops = count * 2.0 * (m * n * k + n * n * k + n ** 3 + m * n * (n + k))
+    pk, src = peaks()
+    achieved = adj_bytes / (adj_ms * 1e-3) / 1e9
+    # gradient error vs torch.linalg.svd (FP64 on the GPU) on a sample of the batch
+    ns = min(count, 256)
+    At = torch.tensor(A64[:ns], dtype=torch.float64, device="cuda", requires_grad=True)
+    Ut, St, Vht = torch.linalg.svd(At, full_matrices=False)
+    Vt = Vht.mT
+    with torch.no_grad():
+        piv = torch.argmax(Vt.abs(), dim=1, keepdim=True)
+        sg = torch.sign(torch.gather(Vt, 1, piv))
+    Ut, Vt = Ut * sg, Vt * sg
+    t64 = lambda x: torch.tensor(x, dtype=torch.float64, device="cuda")
+    Lt = (t64(w[:ns]) * St).sum() + (t64(GU[:ns]) * Ut[:, :, :k]).sum() + (t64(GV[:ns]) * Vt[:, :, :k]).sum()
+    Lt.backward()
+    ref = At.grad
+    err_torch = float(torch.max(torch.amax((g[:ns].double() - ref).abs(), dim=(1, 2)) /
+                                torch.amax(ref.abs(), dim=(1, 2))))
+    # FP64 path against central finite differences (h = 1e-6) on 8 matrices, 2 directions
+    nf = 8
+    A8 = torch.tensor(A64[:nf], dtype=torch.float64, device="cuda", requires_grad=True)
+    w8, GU8, GV8 = t64(w[:nf]), t64(GU[:nf]), t64(GV[:nf])
+    S8, U8, V8 = AD.svd_k(A8, k)
+    ((w8 * S8).sum() + (GU8 * U8).sum() + (GV8 * V8).sum()).backward()
+
+    def losses(X):
+        with torch.no_grad():
+            S_, U_, V_ = AD.svd_k(X, k)
+            return ((w8 * S_).sum(1) + (GU8 * U_).sum((1, 2)) + (GV8 * V_).sum((1, 2))).cpu().numpy()
+
+    h, err_fd = 1e-6, 0.0
+    for _ in range(2):
+        E = torch.tensor(rng.standard_normal((nf, m, n)), dtype=torch.float64, device="cuda")
+        fd = (losses(A8.detach() + h * E) - losses(A8.detach() - h * E)) / (2 * h)
+        an = (A8.grad * E).sum((1, 2)).cpu().numpy()
+        err_fd = max(err_fd, float(np.max(np.abs(fd - an) / np.maximum(1.0, np.abs(an)))))
+    out = {"metric": "differentiable batched SVD matrices/s (forward + adjoint)", "value": round(world * count * 1000.0 / ms, 1),
+           "unit": "matrices/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+           "ms_per_step": round(ms, 3), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "f32", "data": "synthetic (Haar factors, sigma uniform in [0.1, 10], relative gaps >= 1e-3)",
+           "config": {"workload": "%d FP32 matrices %dx%d, loss sum w s + <G_U,U_k> + <G_V,V_k>, k=%d" % (count, m, n, k),
+                      "l2": "inputs larger than L2 (A alone is %d MB), no flush" % (count * m * n * 4 // 10 ** 6)},
+           "adjoint": {"ms": round(adj_ms, 4), "gflops": round(adj_flops / (adj_ms * 1e-3) / 1e9, 1),
+                       "max_rel_grad_err_vs_torch_fp64": err_torch, "max_rel_grad_err_fp64_vs_fd": err_fd},
+           "roofline": {"kernel": "k_svd_adjoint<float>", "bound": "hbm", "achieved": round(achieved, 1),
+                        "peak": pk["hbm_gbs"], "unit": "GB/s", "frac": round(achieved / pk["hbm_gbs"], 4),
+                        "traffic": None, "peak_source": src},
+           "clocks": clk.summary(), "gpu_launches": 2 * args.steps}
+    if rank == 0 and args.cpu_baseline:
+        torch.set_num_threads(8)
+        nc = 256
+        Ac = torch.tensor(A64[:nc], dtype=torch.float32, requires_grad=True)
+        wc, GUc, GVc = [torch.tensor(x[:nc], dtype=torch.float32) for x in (w, GU, GV)]
+        t0 = time.perf_counter()
+        Uc_, Sc_, Vhc_ = torch.linalg.svd(Ac, full_matrices=False)
+        ((wc * Sc_).sum() + (GUc * Uc_[:, :, :k]).sum() + (GVc * Vhc_.mT[:, :, :k]).sum()).backward()
+        dt = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": round(nc / dt, 1), "unit": "matrices/s", "cores": 8, "kind": "torch",
+                               "sample": "torch.linalg.svd forward + backward, %d of the FP32 matrices, CPU" % nc}
+    return out
+
+
 def gen_uneven(count, seed, kind):
     """The uneven-batch workload: m ~ U{16..512}, n ~ U{8..m}, A = Q1 diag(sigma) Q2^T with
     Q1, Q2 from QR of Gaussian matrices and sigma = 10^U(-4, 0) per matrix (host threads)."""
@@ -516,7 +706,12 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="bjac2", choices=["bjac2", "svd1024", "zsvd", "batch_d", "batch_s"])
+    ap.add_argument("--workload", default="bjac2", choices=["bjac2", "svd1024", "zsvd", "zsvd_mixed", "dsvd_mixed",
+                                                             "batch_d", "batch_s", "diff"])
+    ap.add_argument("--diff-count", type=int, default=4096, help="matrices of the differentiable batch")
+    ap.add_argument("--svd-m", type=int, default=0, help="rows of the SVD workloads (0: the workload's own)")
+    ap.add_argument("--svd-n", type=int, default=0, help="columns of the SVD workloads (0: the workload's own)")
+    ap.add_argument("--plain-steps", type=int, default=1, help="timed runs of the plain FP64 arm of *_mixed")
     ap.add_argument("--batch-count", type=int, default=20000)
     ap.add_argument("--batch-sample", type=int, default=40)
     ap.add_argument("--scale", type=int, default=0, help="shrink the 2x2 batches by 2^scale")
@@ -543,8 +738,14 @@ def main():
         out = bench_svd(args, vj, dist, rank, world, "d", 1024, 1024)
     elif args.workload.startswith("batch_"):
         out = bench_batch(args, vj, dist, rank, world, args.workload[-1])
+    elif args.workload == "diff":
+        out = bench_diff(args, vj, dist, rank, world)
+    elif args.workload == "zsvd_mixed":
+        out = bench_mixed(args, vj, dist, rank, world, "z", args.svd_m or 4096, args.svd_n or 2048)
+    elif args.workload == "dsvd_mixed":
+        out = bench_mixed(args, vj, dist, rank, world, "d", args.svd_m or 4096, args.svd_n or 2048)
     else:
-        out = bench_svd(args, vj, dist, rank, world, "z", 4096, 2048)
+        out = bench_svd(args, vj, dist, rank, world, "z", args.svd_m or 4096, args.svd_n or 2048)
     if rank == 0:
         print(json.dumps(out))
     if dist is not None:

@@ -117,6 +117,35 @@ vj_fint vj_cvjsvd_dev(vj_fnat m, vj_fnat n, float *Gr, vj_fnat ldGr, float *Gi, 
                       vj_fnat ldVr, float *Vi, vj_fnat ldVi, float *eS, float *fS, const unsigned *js,
                       unsigned stp, unsigned swp, int preset, void *stream);
 
+/* Mixed-precision SVD (FP64 data, result to FP64 accuracy): FP32 presweeps of the
+ * svjsvd_/cvjsvd_ algorithm on A rounded to FP32, FP64 re-orthogonalisation of their V
+ * (two Newton-Schulz steps), G := A V, then FP64 finishing sweeps of dvjsvd_/zvjsvd_ with
+ * V preset (the reference's iwork[0] != 0 mode, src/dvjsvd.c:88-96, src/zvjsvd.c:100-110).
+ * Shape rules are the FP32 ones: m % 16 == 0, (n/2) % 16 == 0. js/stp is one pivot table
+ * used by both phases; swp caps each phase. Returns the FP64 phase's sweep count (or its
+ * error); *sweeps32 (optional) receives the FP32 phase's. All arrays on the device. */
+vj_fint vj_dvjsvd_mixed_dev(vj_fnat m, vj_fnat n, double *G, vj_fnat ldG, double *V, vj_fnat ldV, double *eS,
+                            double *fS, const unsigned *js, unsigned stp, unsigned swp, unsigned *sweeps32,
+                            void *stream);
+vj_fint vj_zvjsvd_mixed_dev(vj_fnat m, vj_fnat n, double *Gr, vj_fnat ldGr, double *Gi, vj_fnat ldGi, double *Vr,
+                            vj_fnat ldVr, double *Vi, vj_fnat ldVi, double *eS, double *fS, const unsigned *js,
+                            unsigned stp, unsigned swp, unsigned *sweeps32, void *stream);
+
+/* Adjoint of the thin SVD A = U diag(S) V^T (m >= n, V square), batched over `count`
+ * matrices of one shape: given the cotangents dS (n), dU (m x k) and dV (n x k) of S and of
+ * the first k columns of U and V, writes dA (m x n) = the cotangent of A. All arrays on the
+ * device, column-major and packed (matrix b at U + b*m*n, V + b*n*n, S/dS + b*n,
+ * dU + b*m*k, dV + b*n*k, dA + b*m*n). gap >= 0 broadens 1/(s_j^2 - s_i^2) to
+ * d/(d^2 + (gap*max(s_i,s_j)^2)^2) (0: exact; degenerate pairs contribute 0). The working
+ * set of one matrix must fit in 227 KiB of shared memory, else VJ_ERR_ARG.
+ * Returns 0 (asynchronous on `stream`) or a VJ_ERR_* code. */
+vj_fint vj_ssvd_adjoint_batch_dev(vj_fint count, vj_fnat m, vj_fnat n, vj_fnat k, const float *U, const float *S,
+                                  const float *V, const float *dS, const float *dU, const float *dV, float *dA,
+                                  float gap, void *stream);
+vj_fint vj_dsvd_adjoint_batch_dev(vj_fint count, vj_fnat m, vj_fnat n, vj_fnat k, const double *U, const double *S,
+                                  const double *V, const double *dS, const double *dU, const double *dV, double *dA,
+                                  double gap, void *stream);
+
 /* Batched SVD of `count` independent real matrices in one persistent launch (FP64 d,
  * FP32 s), each with the result dvjsvd_/svjsvd_ give for it (V := I, pivot strategy 2 or 4
  * generated on the fly, sweep cap swp). All arrays are on the device: matrix b is

@@ -1,0 +1,109 @@
+"""Mixed-precision SVD (FP32 presweeps + FP64 finishing sweeps) through the C ABI.
+
+The mixed path is not bit-identical to dvjsvd_/zvjsvd_: its FP64 phase is the reference's
+algorithm with a preset V (src/dvjsvd.c:88-96), applied to A V where V comes from FP32
+sweeps and two FP64 Newton-Schulz steps. It is checked against the oracle's FP64 SVD of
+the same matrix (small sizes) and against the matrix's construction (larger sizes):
+  |sigma_mixed - sigma_oracle| <= 32 n eps sigma_max,
+  ||U^H U - I||_max, ||V^H V - I||_max <= 32 n eps,
+  ||A V - U Sigma||_max <= 32 n eps ||A||_max.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+EPS = np.finfo(np.float64).eps
+
+
+@pytest.fixture(scope="module")
+def vj():
+    import vecjac_gb300
+    from vecjac_gb300 import build
+    build.build()
+    return vecjac_gb300
+
+
+@pytest.fixture(scope="module")
+def rst():
+    O.build()
+    return O.Restatement()
+
+
+def run_mixed(vj, kind, A, sid=4, swp=999):
+    import torch
+    m, n = A.shape
+    js, stp = vj.pjs(sid, n)
+    G = torch.tensor(np.ascontiguousarray(A.real.T), dtype=torch.float64, device="cuda")
+    Gi = torch.tensor(np.ascontiguousarray(A.imag.T), dtype=torch.float64, device="cuda") if kind == "z" else None
+    V = torch.empty((n, n), dtype=torch.float64, device="cuda")
+    Vi = torch.empty_like(V) if kind == "z" else None
+    eS = torch.empty(n, dtype=torch.float64, device="cuda")
+    fS = torch.empty_like(eS)
+    djs = torch.tensor(js.astype(np.int32), device="cuda")
+    r, r32 = vj.vjsvd_mixed_dev(kind, m, n, G, m, V, n, eS, fS, djs, stp, swp, Gi=Gi, ldGi=m, Vi=Vi, ldVi=n)
+    torch.cuda.synchronize()
+    U = G.cpu().numpy().T
+    Vm = V.cpu().numpy().T
+    if kind == "z":
+        U = U + 1j * Gi.cpu().numpy().T
+        Vm = Vm + 1j * Vi.cpu().numpy().T
+    sig = fS.cpu().numpy() * np.exp2(eS.cpu().numpy())
+    return r, r32, U, Vm, sig
+
+
+def check_props(A, U, V, sig):
+    n = A.shape[1]
+    tol = 32 * n * EPS
+    assert np.max(np.abs(U.conj().T @ U - np.eye(n))) <= tol
+    assert np.max(np.abs(V.conj().T @ V - np.eye(n))) <= tol
+    assert np.max(np.abs(A @ V - U * sig)) <= tol * np.max(np.abs(A)) * np.sqrt(n)
+
+
+@pytest.mark.parametrize("kind,m,n", [("d", 128, 64), ("d", 96, 96), ("z", 128, 64), ("z", 64, 32)])
+def test_mixed_vs_oracle(vj, rst, kind, m, n):
+    from vecjac_gb300 import workloads as W
+    A, _ = W.svd_matrix(m, n, seed=5 + m + n, complex_=(kind == "z"))
+    r, r32, U, V, sig = run_mixed(vj, kind, A)
+    assert r >= 0 and r32 > 0, (r, r32)
+    js, stp = rst.pjs(4, n)
+    if kind == "z":
+        ro = rst.vjsvd("z", A.real, js, stp, Gi=A.imag)
+    else:
+        ro = rst.vjsvd("d", A, js, stp)
+    assert ro[0] >= 0
+    so = ro[4] * np.exp2(ro[3])
+    assert np.max(np.abs(np.sort(sig) - np.sort(so))) <= 32 * n * EPS * np.max(so)
+    check_props(A, U, V, sig)
+
+
+@pytest.mark.parametrize("kind,m,n", [("d", 1024, 512), ("z", 512, 256)])
+def test_mixed_large(vj, kind, m, n):
+    from vecjac_gb300 import workloads as W
+    A, s = W.svd_matrix(m, n, seed=11, complex_=(kind == "z"))
+    r, r32, U, V, sig = run_mixed(vj, kind, A)
+    assert r >= 0 and r32 > 0
+    # the FP64 phase starts from columns orthogonal to FP32 level: a few sweeps finish it
+    assert r <= 5, r
+    assert np.max(np.abs(np.sort(sig)[::-1] - s)) <= 32 * n * EPS * s[0]
+    check_props(A, U, V, sig)
+
+
+def test_mixed_errors(vj):
+    import torch
+    z = torch.zeros(64 * 32, dtype=torch.float64, device="cuda")
+    v = torch.zeros(32 * 32, dtype=torch.float64, device="cuda")
+    e = torch.zeros(32, dtype=torch.float64, device="cuda")
+    f = torch.zeros(32, dtype=torch.float64, device="cuda")
+    js, stp = vj.pjs(4, 32)
+    djs = torch.tensor(js.astype(np.int32), device="cuda")
+    # m % 16 != 0 is rejected (the FP32 phase's rule)
+    r, _ = vj.vjsvd_mixed_dev("d", 40, 32, z, 40, v, 32, e, f, djs, stp)
+    assert r == -1
+    # a zero matrix: no sweeps, V = I, sigma = 0
+    r, r32 = vj.vjsvd_mixed_dev("d", 64, 32, z, 64, v, 32, e, f, djs, stp)
+    torch.cuda.synchronize()
+    assert r == 0 and r32 == 0
+    assert np.array_equal(v.cpu().numpy().reshape(32, 32), np.eye(32))
+    assert not np.any(f.cpu().numpy() * np.exp2(e.cpu().numpy()))

@@ -39,7 +39,9 @@ def lib():
         for name in ("dbjac2_", "zbjac2_", "sbjac2_", "cbjac2_", "dbjac2i", "zbjac2i", "sbjac2i", "cbjac2i",
                      "vj_dbjac2_dev", "vj_zbjac2_dev", "vj_sbjac2_dev", "vj_cbjac2_dev", "dvjsvd_", "zvjsvd_",
                      "svjsvd_", "cvjsvd_", "vj_dvjsvd_dev", "vj_zvjsvd_dev", "vj_svjsvd_dev", "vj_cvjsvd_dev",
-                     "vj_pjs_dev"):
+                     "vj_pjs_dev", "vj_dvjsvd_mixed_dev", "vj_zvjsvd_mixed_dev",
+                     "vj_ssvd_adjoint_batch_dev", "vj_dsvd_adjoint_batch_dev", "vj_dvjsvd_batch_dev",
+                     "vj_svjsvd_batch_dev"):
             if hasattr(_LIB, name):
                 getattr(_LIB, name).restype = _ll
         if hasattr(_LIB, "pjs"):
@@ -151,6 +153,26 @@ def vjsvd_dev(kind, m, n, G, ldG, V, ldV, eS, fS, js, stp, swp=999, preset=False
                  _p(eS), _p(fS), _p(js), C.c_uint(int(stp)), C.c_uint(int(swp)), C.c_int(int(preset)), s)
     return f(_ull(m), _ull(n), _p(G), _ull(ldG), _p(V), _ull(ldV), _p(eS), _p(fS), _p(js), C.c_uint(int(stp)),
              C.c_uint(int(swp)), C.c_int(int(preset)), s)
+
+
+def vjsvd_mixed_dev(kind, m, n, G, ldG, V, ldV, eS, fS, js, stp, swp=999, Gi=None, ldGi=None, Vi=None, ldVi=None,
+                    stream=None):
+    """Mixed-precision device SVD of FP64 data (kind "d" or "z"): FP32 presweeps, FP64
+    re-orthogonalisation of V, FP64 finishing sweeps with V preset. Returns
+    (FP64 sweeps or error code, FP32 sweeps)."""
+    if kind not in "dz":
+        raise ValueError("the mixed-precision SVD takes FP64 data (kind d or z)")
+    L = lib()
+    f = getattr(L, "vj_%svjsvd_mixed_dev" % kind)
+    s = C.c_void_p(stream) if stream else None
+    sw32 = C.c_uint(0)
+    if kind == "z":
+        r = f(_ull(m), _ull(n), _p(G), _ull(ldG), _p(Gi), _ull(ldGi), _p(V), _ull(ldV), _p(Vi), _ull(ldVi),
+              _p(eS), _p(fS), _p(js), C.c_uint(int(stp)), C.c_uint(int(swp)), C.byref(sw32), s)
+    else:
+        r = f(_ull(m), _ull(n), _p(G), _ull(ldG), _p(V), _ull(ldV), _p(eS), _p(fS), _p(js), C.c_uint(int(stp)),
+              C.c_uint(int(swp)), C.byref(sw32), s)
+    return r, sw32.value
 
 
 def pjs(sid, n):

@@ -3,7 +3,8 @@
 Every translation unit under csrc/ is compiled in parallel with
 ``-gencode arch=compute_103a,code=sm_103a -lineinfo --fmad=false`` (no implicit
 multiply-add contraction: the kernels reproduce the reference's rounding op by op)
-and linked against the CUDA runtime only -- PyTorch is not a dependency of the library.
+and linked against the CUDA runtime and cuBLAS (the plain FP64 GEMMs of the mixed-precision
+SVD) -- PyTorch is not a dependency of the library.
 """
 import concurrent.futures as cf
 import glob
@@ -48,7 +49,7 @@ def build(verbose=False, extra=()):
         objs = list(ex.map(lambda s: _compile(s, list(extra)), srcs))
     if os.path.exists(LIB) and os.path.getmtime(LIB) >= max(os.path.getmtime(o) for o in objs):
         return LIB
-    cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart"]
+    cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart", "-lcublas"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s\n%s" % (" ".join(cmd), r.stderr))

@@ -82,6 +82,12 @@ Staging &staging2()
   return s;
 }
 
+Staging &staging3()
+{
+  static Staging s;
+  return s;
+}
+
 bool streams2(cudaStream_t s[2])
 {
   static cudaStream_t st[2] = {nullptr, nullptr};

@@ -660,6 +660,29 @@ static vj_fint svd_host(const vj_fnat *m, const vj_fnat *n, T *G, const vj_fnat 
 
 using namespace vj;
 
+namespace vj {
+// device-pointer SVD for other translation units (the mixed-precision driver)
+template <typename T, bool CPLX>
+vj_fint svd_dev_entry(vj_fnat m, vj_fnat n, T *G, vj_fnat ldG, T *Gi, vj_fnat ldGi, T *V, vj_fnat ldV, T *Vi,
+                      vj_fnat ldVi, T *eS, T *fS, const unsigned *js, unsigned stp, unsigned swp, int preset,
+                      cudaStream_t s)
+{
+  return svd_dev<T, CPLX>(m, n, G, ldG, Gi, ldGi, V, ldV, Vi, ldVi, eS, fS, js, stp, swp, preset, s);
+}
+template vj_fint svd_dev_entry<double, false>(vj_fnat, vj_fnat, double *, vj_fnat, double *, vj_fnat, double *,
+                                              vj_fnat, double *, vj_fnat, double *, double *, const unsigned *,
+                                              unsigned, unsigned, int, cudaStream_t);
+template vj_fint svd_dev_entry<double, true>(vj_fnat, vj_fnat, double *, vj_fnat, double *, vj_fnat, double *,
+                                             vj_fnat, double *, vj_fnat, double *, double *, const unsigned *,
+                                             unsigned, unsigned, int, cudaStream_t);
+template vj_fint svd_dev_entry<float, false>(vj_fnat, vj_fnat, float *, vj_fnat, float *, vj_fnat, float *,
+                                             vj_fnat, float *, vj_fnat, float *, float *, const unsigned *,
+                                             unsigned, unsigned, int, cudaStream_t);
+template vj_fint svd_dev_entry<float, true>(vj_fnat, vj_fnat, float *, vj_fnat, float *, vj_fnat, float *,
+                                            vj_fnat, float *, vj_fnat, float *, float *, const unsigned *,
+                                            unsigned, unsigned, int, cudaStream_t);
+}  // namespace vj
+
 extern "C" {
 
 vj_fint dvjsvd_(const vj_fnat m[1], const vj_fnat n[1], double G[], const vj_fnat ldG[1], double V[],

@@ -23,6 +23,8 @@ struct Staging {
 };
 Staging &staging();
 Staging &staging2();
+// scratch of the mixed-precision SVD (its inner SVD calls use staging2)
+Staging &staging3();
 
 // the work-queue counter of the batched SVD (device memory, allocated on first use)
 unsigned *batch_queue();
