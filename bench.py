@@ -387,7 +387,7 @@ def bench_svd(args, vj, dist, rank, world, kind, m, n):
     import torch
     from vecjac_gb300 import workloads as W
     cx = kind in "zc"
-    A, s = W.svd_matrix(m, n, seed=2024 + rank, complex_=cx)
+    A, s = W.svd_matrix(m, n, seed=2024 + rank, lo=(-8.0 if cx else -6.0), complex_=cx)
     js, stp = vj.pjs(args.pivot, n)
     dt = np.float64 if kind in "dz" else np.float32
     Gt = torch.tensor(np.ascontiguousarray(A.real.T, dt), device="cuda")
@@ -444,7 +444,7 @@ def bench_mixed(args, vj, dist, rank, world, kind, m, n):
     import torch
     from vecjac_gb300 import workloads as W
     cx = kind == "z"
-    A, s = W.svd_matrix(m, n, seed=2024 + rank, complex_=cx)
+    A, s = W.svd_matrix(m, n, seed=2024 + rank, lo=(-8.0 if cx else -6.0), complex_=cx)
     js, stp = vj.pjs(args.pivot, n)
     Gt = torch.tensor(np.ascontiguousarray(A.real.T), dtype=torch.float64, device="cuda")
     Git = torch.tensor(np.ascontiguousarray(A.imag.T), dtype=torch.float64, device="cuda") if cx else None
@@ -465,7 +465,7 @@ def bench_mixed(args, vj, dist, rank, world, kind, m, n):
     def mixed():
         reset()
         return vj.vjsvd_mixed_dev(kind, m, n, G, m, V, n, eS, fS, djs, stp, Gi=Gi, ldGi=m, Vi=Vi, ldVi=n,
-                                  stream=stream.cuda_stream)
+                                  stream=stream.cuda_stream, stages=args.stages)
 
     def plain():
         reset()
@@ -496,9 +496,10 @@ def bench_mixed(args, vj, dist, rank, world, kind, m, n):
     out = {"metric": "Jacobi SVD matrices/s (%svjsvd mixed FP32->FP64)" % kind,
            "value": round(world * 1000.0 / ms, 5), "unit": "matrices/s", "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": True, "scaling": "weak",
-           "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic (Haar factors, log-uniform sigma in [1e-6, 1])",
-           "config": {"workload": "%svjsvd_ %dx%d mixed precision (FP32 presweeps, 2 Newton-Schulz steps, FP64 "
-                                  "finishing sweeps), pivot strategy id %d" % (kind, m, n, args.pivot),
+           "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic (Haar factors, log-uniform sigma in [%g, 1])" % (1e-8 if cx else 1e-6),
+           "config": {"workload": "%svjsvd_ %dx%d mixed precision (FP32 presweep rounds, each with 2 Newton-Schulz "
+                                  "steps, then FP64 finishing sweeps), pivot strategy id %d" % (kind, m, n, args.pivot),
+                      "stages": args.stages or 3,
                       "sweeps_fp32": int(sw32), "sweeps_fp64": int(sw64),
                       "max_rel_sigma_err_vs_exact": rel_m, "max_sigma_err_over_sigma_max": nrm_m},
            "clocks": clk.summary()}
@@ -712,6 +713,7 @@ def main():
     ap.add_argument("--svd-m", type=int, default=0, help="rows of the SVD workloads (0: the workload's own)")
     ap.add_argument("--svd-n", type=int, default=0, help="columns of the SVD workloads (0: the workload's own)")
     ap.add_argument("--plain-steps", type=int, default=1, help="timed runs of the plain FP64 arm of *_mixed")
+    ap.add_argument("--stages", type=int, default=0, help="FP32 preconditioning rounds of *_mixed (0: library default)")
     ap.add_argument("--batch-count", type=int, default=20000)
     ap.add_argument("--batch-sample", type=int, default=40)
     ap.add_argument("--scale", type=int, default=0, help="shrink the 2x2 batches by 2^scale")

@@ -39,7 +39,7 @@ def grad_ours(ad, A, w, GU, GV, k, dtype):
     t = lambda x: torch.tensor(x, dtype=dtype, device="cuda")
     L = (t(w) * S).sum() + (t(GU) * Uk).sum() + (t(GV) * Vk).sum()
     L.backward()
-    return At.grad.double().cpu().numpy(), S.double().cpu().numpy()
+    return At.grad.double().cpu().numpy(), S.detach().double().cpu().numpy()
 
 
 @pytest.mark.parametrize("dtype_name,m,n,k", [("float64", 32, 16, 4), ("float64", 64, 32, 32), ("float32", 128, 64, 16),

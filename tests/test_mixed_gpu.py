@@ -1,8 +1,8 @@
 """Mixed-precision SVD (FP32 presweeps + FP64 finishing sweeps) through the C ABI.
 
 The mixed path is not bit-identical to dvjsvd_/zvjsvd_: its FP64 phase is the reference's
-algorithm with a preset V (src/dvjsvd.c:88-96), applied to A V where V comes from FP32
-sweeps and two FP64 Newton-Schulz steps. It is checked against the oracle's FP64 SVD of
+algorithm with a preset V (src/dvjsvd.c:88-96), applied to A V where V comes from rounds
+of FP32 sweeps, each re-orthogonalised by two FP64 Newton-Schulz steps. It is checked against the oracle's FP64 SVD of
 the same matrix (small sizes) and against the matrix's construction (larger sizes):
   |sigma_mixed - sigma_oracle| <= 32 n eps sigma_max,
   ||U^H U - I||_max, ||V^H V - I||_max <= 32 n eps,
@@ -98,9 +98,11 @@ def test_mixed_errors(vj):
     f = torch.zeros(32, dtype=torch.float64, device="cuda")
     js, stp = vj.pjs(4, 32)
     djs = torch.tensor(js.astype(np.int32), device="cuda")
-    # m % 16 != 0 is rejected (the FP32 phase's rule)
-    r, _ = vj.vjsvd_mixed_dev("d", 40, 32, z, 40, v, 32, e, f, djs, stp)
+    # the reference's shape rules: m % 8 != 0 -> -1, (n/2) % 8 != 0 -> -2
+    r, _ = vj.vjsvd_mixed_dev("d", 36, 32, z, 36, v, 32, e, f, djs, stp)
     assert r == -1
+    r, _ = vj.vjsvd_mixed_dev("d", 64, 24, z, 64, v, 24, e, f, djs, stp)
+    assert r == -2
     # a zero matrix: no sweeps, V = I, sigma = 0
     r, r32 = vj.vjsvd_mixed_dev("d", 64, 32, z, 64, v, 32, e, f, djs, stp)
     torch.cuda.synchronize()

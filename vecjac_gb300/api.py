@@ -156,10 +156,10 @@ def vjsvd_dev(kind, m, n, G, ldG, V, ldV, eS, fS, js, stp, swp=999, preset=False
 
 
 def vjsvd_mixed_dev(kind, m, n, G, ldG, V, ldV, eS, fS, js, stp, swp=999, Gi=None, ldGi=None, Vi=None, ldVi=None,
-                    stream=None):
-    """Mixed-precision device SVD of FP64 data (kind "d" or "z"): FP32 presweeps, FP64
-    re-orthogonalisation of V, FP64 finishing sweeps with V preset. Returns
-    (FP64 sweeps or error code, FP32 sweeps)."""
+                    stream=None, stages=0):
+    """Mixed-precision device SVD of FP64 data (kind "d" or "z"): `stages` (0: 3) rounds of
+    FP32 sweeps with FP64 re-orthogonalisation, then FP64 finishing sweeps with V preset.
+    Returns (FP64 sweeps or error code, FP32 sweeps)."""
     if kind not in "dz":
         raise ValueError("the mixed-precision SVD takes FP64 data (kind d or z)")
     L = lib()
@@ -168,10 +168,10 @@ def vjsvd_mixed_dev(kind, m, n, G, ldG, V, ldV, eS, fS, js, stp, swp=999, Gi=Non
     sw32 = C.c_uint(0)
     if kind == "z":
         r = f(_ull(m), _ull(n), _p(G), _ull(ldG), _p(Gi), _ull(ldGi), _p(V), _ull(ldV), _p(Vi), _ull(ldVi),
-              _p(eS), _p(fS), _p(js), C.c_uint(int(stp)), C.c_uint(int(swp)), C.byref(sw32), s)
+              _p(eS), _p(fS), _p(js), C.c_uint(int(stp)), C.c_uint(int(swp)), C.c_uint(int(stages)), C.byref(sw32), s)
     else:
         r = f(_ull(m), _ull(n), _p(G), _ull(ldG), _p(V), _ull(ldV), _p(eS), _p(fS), _p(js), C.c_uint(int(stp)),
-              C.c_uint(int(swp)), C.byref(sw32), s)
+              C.c_uint(int(swp)), C.c_uint(int(stages)), C.byref(sw32), s)
     return r, sw32.value
 
 

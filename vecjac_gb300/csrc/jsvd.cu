@@ -158,19 +158,29 @@ __global__ void __launch_bounds__(256) k_step(SvdArgs<T> a, int st, int g3, int 
   }
   __syncthreads();
   tphase(1);
-  // ---- 2. scaled dot products: pair j on lanes [j L, (j+1) L) of warp 0 ----
-  if (warp == 0) {
-    const int j = lane / L;
+  // ---- 2. scaled dot products ----
+  // FP32: pair j on lanes [j L, (j+1) L) of warp 0. FP64: pair j on warp j, one
+  // accumulator chain per 8 threads (real data: 2 chains, the other 16 threads idle -- the
+  // FP64 issue slots of a sub-partition, not its lanes, are the scarce resource).
+  constexpr int DT = (sizeof(T) == 8) ? 32 : 32 / P;
+  constexpr int DW = (P * DT + 31) / 32;  // warps taking part in the dot products
+  if (warp < DW) {
+    const int j = tid / DT;
+    const int sub = tid - j * DT;
     const bool act = (j < np);
     const int jj = act ? j : 0;
     const long long p = colp(jj), q = colq(jj);
     const T ep = a.eS[p], fp_ = a.fS[p], eq = a.eS[q], fq = a.fS[q];
     T zr = 0, zi = 0;
-    const bool live = act && (eq >= -svdc<T>::RMAX) && (ep >= -svdc<T>::RMAX);
-    pair_dot<T, CPLX>(a.m, rcol(jj, 1), CPLX ? rcol(jj, 3) : nullptr, rcol(jj, 0), CPLX ? rcol(jj, 2) : nullptr, eq,
-                      ep, fq, fp_, live, zr, zi);
+    const bool live = act && (eq >= -svdc<T>::RMAX) && (ep >= -svdc<T>::RMAX) && (CPLX || sub < 16);
+    if constexpr (sizeof(T) == 8)
+      pair_dot_split<T, CPLX>(a.m, rcol(jj, 1), CPLX ? rcol(jj, 3) : nullptr, rcol(jj, 0), CPLX ? rcol(jj, 2) : nullptr,
+                              eq, ep, fq, fp_, live, sub >> 3, sub & 7, zr, zi);
+    else
+      pair_dot<T, CPLX>(a.m, rcol(jj, 1), CPLX ? rcol(jj, 3) : nullptr, rcol(jj, 0), CPLX ? rcol(jj, 2) : nullptr, eq,
+                        ep, fq, fp_, live, zr, zi);
     tphase(2);
-    if (act && (lane % L) == 0) {
+    if (act && sub == 0) {
       PairState<T> &s = ps[j];
       s.ep = ep; s.fp = fp_; s.eq = eq; s.fq = fq;
       if (!live) {

@@ -322,6 +322,71 @@ __device__ void pair_dot(long long m, const T *xr, const T *xi, const T *yr, con
   zi = CPLX ? fp<T>::div(nui, de) : (T)0;
 }
 
+// The same scaled compensated dot products (FP64 only) with each accumulator chain on its
+// own group of 8 threads: the reference's 8 lanes keep their element order and their
+// 2Sum recurrences, but the independent recurrences of one lane -- the round-down products
+// (pd) and their exact errors (dn), for the real and, for complex data, the imaginary part
+// -- run in different threads: chain 0-1 (real) or 0-3 (complex) says which recurrence,
+// l8 is the lane. On GB300 each SM sub-partition issues about one FP64 warp instruction per
+// 76 cycles whatever the number of active lanes, so a pair's FP64 work spread over 2 or 4
+// chains finishes 2 or 4 times sooner than on one warp's 8 lanes. All threads run the
+// same instruction stream (each forms pd and dn and keeps the one its chain accumulates),
+// and the result combines the chains in the reference's order,
+// nu = S(s_pd) + (S(t_pd) + (S(s_dn) + S(t_dn))), S = the 8-lane halving tree. The result
+// is valid on the pair's first thread; every thread of the warp must call this.
+template <typename T, bool CPLX>
+__device__ void pair_dot_split(long long m, const T *xr, const T *xi, const T *yr, const T *yi, T ex, T ey, T fx, T fy,
+                               bool live, int chain, int l8, T &zr, T &zi)
+{
+  static_assert(sizeof(T) == 8, "the split dot product is the FP64 form");
+  const int nx = -(int)ex, ny = -(int)ey;
+  const bool err = (chain & 1) != 0;              // accumulate dn instead of pd
+  const bool imp = CPLX && (chain >= 2);          // imaginary part: xr yi + (-xi) yr
+  const unsigned long long flip = imp ? 0x8000000000000000ull : 0ull;
+  T s = 0, t = 0;
+  auto acc = [&](T x, T y) {
+    const T pd = fp<T>::mul_rd(x, y);
+    const T dn = fp<T>::fma_(x, y, -pd);
+    two_sum(s, (err ? dn : pd) + t, s, t);
+  };
+  if (live && l8 < m) {
+    T x0 = scale2(xr[l8], nx), y0 = scale2(yr[l8], ny), x1 = 0, y1 = 0;
+    if (CPLX) {
+      x1 = scale2(xi[l8], nx);
+      y1 = scale2(yi[l8], ny);
+    }
+    for (long long i = l8; i < m; i += 8) {
+      const long long inx = (i + 8 < m) ? (i + 8) : i;
+      const T nx0 = scale2(xr[inx], nx), ny0 = scale2(yr[inx], ny);
+      T nx1 = 0, ny1 = 0;
+      if (CPLX) {
+        nx1 = scale2(xi[inx], nx);
+        ny1 = scale2(yi[inx], ny);
+        // real part: xr yr, xi yi; imaginary part: xr yi, xi (-yr) (= (-xi) yr exactly)
+        const T b0 = imp ? y1 : y0;
+        const T b1 = imp ? __longlong_as_double((long long)((unsigned long long)__double_as_longlong(y0) ^ flip)) : y1;
+        acc(x0, b0);
+        acc(x1, b1);
+      }
+      else
+        acc(x0, y0);
+      x0 = nx0;
+      y0 = ny0;
+      x1 = nx1;
+      y1 = ny1;
+    }
+  }
+  const T S = hsum<8>(s), Tt = hsum<8>(t);
+  const T Sdn = __shfl_down_sync(0xffffffffu, S, 8), Tdn = __shfl_down_sync(0xffffffffu, Tt, 8);
+  const T nu = S + (Tt + (Sdn + Tdn));
+  T nui = 0;
+  if (CPLX)
+    nui = __shfl_down_sync(0xffffffffu, nu, 16);
+  const T de = fx * fy;
+  zr = fp<T>::div(nu, de);
+  zi = CPLX ? fp<T>::div(nui, de) : (T)0;
+}
+
 // efcmp (src/defops.h:46)
 template <typename T> __device__ __forceinline__ int efcmp(T e0, T f0, T e1, T f1)
 {
