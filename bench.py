@@ -491,7 +491,8 @@ def bench_mixed(args, vj, dist, rank, world, kind, m, n):
     for _ in range(args.warmup):
         mixed()
     with Clocks(torch.cuda.current_device()) as clk:
-        ms, (sw64, sw32) = timed(mixed, args.steps)
+        ms, (sw64, sw32, swf) = timed(mixed, args.steps)
+    rot64 = vj.last_trace()["rotations"]
     sig_m, rel_m, nrm_m = sigma_err()
     out = {"metric": "Jacobi SVD matrices/s (%svjsvd mixed FP32->FP64)" % kind,
            "value": round(world * 1000.0 / ms, 5), "unit": "matrices/s", "n_gpus": world, "steps": args.steps,
@@ -499,8 +500,9 @@ def bench_mixed(args, vj, dist, rank, world, kind, m, n):
            "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic (Haar factors, log-uniform sigma in [%g, 1])" % (1e-8 if cx else 1e-6),
            "config": {"workload": "%svjsvd_ %dx%d mixed precision (FP32 presweep rounds, each with 2 Newton-Schulz "
                                   "steps, then FP64 finishing sweeps), pivot strategy id %d" % (kind, m, n, args.pivot),
-                      "stages": args.stages or 3,
-                      "sweeps_fp32": int(sw32), "sweeps_fp64": int(sw64),
+                      "stages": args.stages or 2,
+                      "sweeps_fp32": int(sw32), "sweeps_fp64_plain_dot": int(swf), "sweeps_fp64": int(sw64),
+                      "fp64_rotations_per_sweep": rot64,
                       "max_rel_sigma_err_vs_exact": rel_m, "max_sigma_err_over_sigma_max": nrm_m},
            "clocks": clk.summary()}
     if args.plain_steps > 0:

@@ -117,21 +117,23 @@ vj_fint vj_cvjsvd_dev(vj_fnat m, vj_fnat n, float *Gr, vj_fnat ldGr, float *Gi, 
                       vj_fnat ldVr, float *Vi, vj_fnat ldVi, float *eS, float *fS, const unsigned *js,
                       unsigned stp, unsigned swp, int preset, void *stream);
 
-/* Mixed-precision SVD (FP64 data, result to FP64 accuracy): `stages` rounds (0: 3) of FP32
+/* Mixed-precision SVD (FP64 data, result to FP64 accuracy): `stages` rounds (0: 2) of FP32
  * one-sided Jacobi sweeps on the current G rounded to FP32, each followed by FP64
  * re-orthogonalisation of the accumulated rotation W (two Newton-Schulz steps) and the
- * FP64 products G := G W, V := V W; then FP64 finishing sweeps of dvjsvd_/zvjsvd_ with V
+ * FP64 products G := G W, V := V W; FP64 sweeps with plain dot products on G and V to
+ * twice the reference's tolerance; then FP64 finishing sweeps of dvjsvd_/zvjsvd_ with V
  * preset (the reference's iwork[0] != 0 mode, src/dvjsvd.c:88-96, src/zvjsvd.c:100-110).
- * Shape rules and return values are dvjsvd_'s/zvjsvd_'s (the FP64 phase's sweep count or
- * its error); *sweeps32 (optional) receives the number of FP32 sweeps. js/stp is the
- * pivot table of both phases; swp caps each phase (FP32 phases at most 60). All arrays on
- * the device. Links cuBLAS for the FP64 GEMMs. */
+ * Shape rules and return values are dvjsvd_'s/zvjsvd_'s (the finishing phase's sweep
+ * count or its error); presweeps (optional, 2 entries) receives the number of FP32 sweeps
+ * and of plain-dot FP64 sweeps. js/stp is the pivot table of every phase; swp caps each
+ * phase (presweep phases at most 60). All arrays on the device. Links cuBLAS for the FP64
+ * GEMMs. */
 vj_fint vj_dvjsvd_mixed_dev(vj_fnat m, vj_fnat n, double *G, vj_fnat ldG, double *V, vj_fnat ldV, double *eS,
                             double *fS, const unsigned *js, unsigned stp, unsigned swp, unsigned stages,
-                            unsigned *sweeps32, void *stream);
+                            unsigned *presweeps, void *stream);
 vj_fint vj_zvjsvd_mixed_dev(vj_fnat m, vj_fnat n, double *Gr, vj_fnat ldGr, double *Gi, vj_fnat ldGi, double *Vr,
                             vj_fnat ldVr, double *Vi, vj_fnat ldVi, double *eS, double *fS, const unsigned *js,
-                            unsigned stp, unsigned swp, unsigned stages, unsigned *sweeps32, void *stream);
+                            unsigned stp, unsigned swp, unsigned stages, unsigned *presweeps, void *stream);
 
 /* Adjoint of the thin SVD A = U diag(S) V^T (m >= n, V square), batched over `count`
  * matrices of one shape: given the cotangents dS (n), dU (m x k) and dV (n x k) of S and of

@@ -42,7 +42,7 @@ def run_mixed(vj, kind, A, sid=4, swp=999):
     eS = torch.empty(n, dtype=torch.float64, device="cuda")
     fS = torch.empty_like(eS)
     djs = torch.tensor(js.astype(np.int32), device="cuda")
-    r, r32 = vj.vjsvd_mixed_dev(kind, m, n, G, m, V, n, eS, fS, djs, stp, swp, Gi=Gi, ldGi=m, Vi=Vi, ldVi=n)
+    r, r32, _ = vj.vjsvd_mixed_dev(kind, m, n, G, m, V, n, eS, fS, djs, stp, swp, Gi=Gi, ldGi=m, Vi=Vi, ldVi=n)
     torch.cuda.synchronize()
     U = G.cpu().numpy().T
     Vm = V.cpu().numpy().T
@@ -84,8 +84,9 @@ def test_mixed_large(vj, kind, m, n):
     A, s = W.svd_matrix(m, n, seed=11, complex_=(kind == "z"))
     r, r32, U, V, sig = run_mixed(vj, kind, A)
     assert r >= 0 and r32 > 0
-    # the FP64 phase starts from columns orthogonal to FP32 level: a few sweeps finish it
-    assert r <= 5, r
+    # the reference's FP64 phase starts from columns orthogonal to twice its tolerance: it
+    # confirms convergence within a few sweeps
+    assert r <= 3, r
     assert np.max(np.abs(np.sort(sig)[::-1] - s)) <= 32 * n * EPS * s[0]
     check_props(A, U, V, sig)
 
@@ -99,12 +100,12 @@ def test_mixed_errors(vj):
     js, stp = vj.pjs(4, 32)
     djs = torch.tensor(js.astype(np.int32), device="cuda")
     # the reference's shape rules: m % 8 != 0 -> -1, (n/2) % 8 != 0 -> -2
-    r, _ = vj.vjsvd_mixed_dev("d", 36, 32, z, 36, v, 32, e, f, djs, stp)
+    r, _, _ = vj.vjsvd_mixed_dev("d", 36, 32, z, 36, v, 32, e, f, djs, stp)
     assert r == -1
-    r, _ = vj.vjsvd_mixed_dev("d", 64, 24, z, 64, v, 24, e, f, djs, stp)
+    r, _, _ = vj.vjsvd_mixed_dev("d", 64, 24, z, 64, v, 24, e, f, djs, stp)
     assert r == -2
     # a zero matrix: no sweeps, V = I, sigma = 0
-    r, r32 = vj.vjsvd_mixed_dev("d", 64, 32, z, 64, v, 32, e, f, djs, stp)
+    r, r32, _ = vj.vjsvd_mixed_dev("d", 64, 32, z, 64, v, 32, e, f, djs, stp)
     torch.cuda.synchronize()
     assert r == 0 and r32 == 0
     assert np.array_equal(v.cpu().numpy().reshape(32, 32), np.eye(32))

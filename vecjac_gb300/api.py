@@ -157,22 +157,23 @@ def vjsvd_dev(kind, m, n, G, ldG, V, ldV, eS, fS, js, stp, swp=999, preset=False
 
 def vjsvd_mixed_dev(kind, m, n, G, ldG, V, ldV, eS, fS, js, stp, swp=999, Gi=None, ldGi=None, Vi=None, ldVi=None,
                     stream=None, stages=0):
-    """Mixed-precision device SVD of FP64 data (kind "d" or "z"): `stages` (0: 3) rounds of
-    FP32 sweeps with FP64 re-orthogonalisation, then FP64 finishing sweeps with V preset.
-    Returns (FP64 sweeps or error code, FP32 sweeps)."""
+    """Mixed-precision device SVD of FP64 data (kind "d" or "z"): `stages` (0: 2) rounds of
+    FP32 sweeps with FP64 re-orthogonalisation, plain-dot FP64 sweeps, then the reference's
+    FP64 sweeps with V preset. Returns (finishing sweeps or error code, FP32 sweeps,
+    plain-dot FP64 sweeps)."""
     if kind not in "dz":
         raise ValueError("the mixed-precision SVD takes FP64 data (kind d or z)")
     L = lib()
     f = getattr(L, "vj_%svjsvd_mixed_dev" % kind)
     s = C.c_void_p(stream) if stream else None
-    sw32 = C.c_uint(0)
+    pre = (C.c_uint * 2)()
     if kind == "z":
         r = f(_ull(m), _ull(n), _p(G), _ull(ldG), _p(Gi), _ull(ldGi), _p(V), _ull(ldV), _p(Vi), _ull(ldVi),
-              _p(eS), _p(fS), _p(js), C.c_uint(int(stp)), C.c_uint(int(swp)), C.c_uint(int(stages)), C.byref(sw32), s)
+              _p(eS), _p(fS), _p(js), C.c_uint(int(stp)), C.c_uint(int(swp)), C.c_uint(int(stages)), pre, s)
     else:
         r = f(_ull(m), _ull(n), _p(G), _ull(ldG), _p(V), _ull(ldV), _p(eS), _p(fS), _p(js), C.c_uint(int(stp)),
-              C.c_uint(int(swp)), C.c_uint(int(stages)), C.byref(sw32), s)
-    return r, sw32.value
+              C.c_uint(int(swp)), C.c_uint(int(stages)), pre, s)
+    return r, pre[0], pre[1]
 
 
 def pjs(sid, n):

@@ -159,28 +159,76 @@ __global__ void __launch_bounds__(256) k_step(SvdArgs<T> a, int st, int g3, int 
   __syncthreads();
   tphase(1);
   // ---- 2. scaled dot products ----
-  // FP32: pair j on lanes [j L, (j+1) L) of warp 0. FP64: pair j on warp j, one
-  // accumulator chain per 8 threads (real data: 2 chains, the other 16 threads idle -- the
-  // FP64 issue slots of a sub-partition, not its lanes, are the scarce resource).
-  constexpr int DT = (sizeof(T) == 8) ? 32 : 32 / P;
-  constexpr int DW = (P * DT + 31) / 32;  // warps taking part in the dot products
-  if (warp < DW) {
-    const int j = tid / DT;
-    const int sub = tid - j * DT;
+  // FP32: pair j on lanes [j L, (j+1) L) of warp 0. FP64: one warp per accumulator chain
+  // (warp c runs chain c of the CTA's four pairs, pair j on lanes [8j, 8j+8)), so that the
+  // FP64 work of the step is spread over two (real) or four (complex) of the SM's
+  // sub-partitions; the chains meet in shared memory.
+  int cj = -1;  // the pair this thread classifies
+  T zr = 0, zi = 0, ep = 0, fp_ = 0, eq = 0, fq = 0;
+  bool live = false;
+  if constexpr (sizeof(T) == 8) {
+    constexpr int NCH = CPLX ? 4 : 2;
+    constexpr int PPW = 4;  // pairs per chain warp
+    __shared__ T dsum[ppc<T>::P][NCH][2];
+    if (warp < NCH * (ppc<T>::P / PPW)) {
+      const int jw = lane >> 3, l8 = lane & 7;
+      const int j = (warp / NCH) * PPW + jw;
+      const bool act = (jw < PPW) && (j < np);
+      const int jj = act ? j : 0;
+      const long long p = colp(jj), q = colq(jj);
+      const T ep_ = a.eS[p], eq_ = a.eS[q];
+      const bool lv = act && (eq_ >= -svdc<T>::RMAX) && (ep_ >= -svdc<T>::RMAX);
+      const T *xr = rcol(jj, 1), *xi = CPLX ? rcol(jj, 3) : nullptr, *yr = rcol(jj, 0),
+              *yi = CPLX ? rcol(jj, 2) : nullptr;
+      T S = 0, Tt = 0;
+      const int c = warp % NCH;
+      switch (c) {
+        case 0: chain_dot<T, CPLX, 0>(a.m, xr, xi, yr, yi, eq_, ep_, lv, l8, S, Tt); break;
+        case 1: chain_dot<T, CPLX, 1>(a.m, xr, xi, yr, yi, eq_, ep_, lv, l8, S, Tt); break;
+        case 2: chain_dot<T, CPLX, 2>(a.m, xr, xi, yr, yi, eq_, ep_, lv, l8, S, Tt); break;
+        default: chain_dot<T, CPLX, 3>(a.m, xr, xi, yr, yi, eq_, ep_, lv, l8, S, Tt); break;
+      }
+      if (act && l8 == 0) {
+        dsum[j][c][0] = S;
+        dsum[j][c][1] = Tt;
+      }
+    }
+    __syncthreads();
+    if (tid < np) {
+      cj = tid;
+      const long long p = colp(cj), q = colq(cj);
+      ep = a.eS[p]; fp_ = a.fS[p]; eq = a.eS[q]; fq = a.fS[q];
+      live = (eq >= -svdc<T>::RMAX) && (ep >= -svdc<T>::RMAX);
+      // nu = S(s_pd) + (S(t_pd) + (S(s_dn) + S(t_dn))), divided by fx fy (x = G_q)
+      const T de = fq * fp_;
+      zr = F::div(dsum[cj][0][0] + (dsum[cj][0][1] + (dsum[cj][1][0] + dsum[cj][1][1])), de);
+      if (CPLX)
+        zi = F::div(dsum[cj][NCH - 2][0] + (dsum[cj][NCH - 2][1] + (dsum[cj][NCH - 1][0] + dsum[cj][NCH - 1][1])), de);
+    }
+  }
+  else if (warp == 0) {
+    const int j = lane / L;
     const bool act = (j < np);
     const int jj = act ? j : 0;
     const long long p = colp(jj), q = colq(jj);
-    const T ep = a.eS[p], fp_ = a.fS[p], eq = a.eS[q], fq = a.fS[q];
-    T zr = 0, zi = 0;
-    const bool live = act && (eq >= -svdc<T>::RMAX) && (ep >= -svdc<T>::RMAX) && (CPLX || sub < 16);
-    if constexpr (sizeof(T) == 8)
-      pair_dot_split<T, CPLX>(a.m, rcol(jj, 1), CPLX ? rcol(jj, 3) : nullptr, rcol(jj, 0), CPLX ? rcol(jj, 2) : nullptr,
-                              eq, ep, fq, fp_, live, sub >> 3, sub & 7, zr, zi);
-    else
-      pair_dot<T, CPLX>(a.m, rcol(jj, 1), CPLX ? rcol(jj, 3) : nullptr, rcol(jj, 0), CPLX ? rcol(jj, 2) : nullptr, eq,
-                        ep, fq, fp_, live, zr, zi);
-    tphase(2);
-    if (act && sub == 0) {
+    const T ep_ = a.eS[p], fp0 = a.fS[p], eq_ = a.eS[q], fq0 = a.fS[q];
+    const bool lv = act && (eq_ >= -svdc<T>::RMAX) && (ep_ >= -svdc<T>::RMAX);
+    T zr_ = 0, zi_ = 0;
+    pair_dot<T, CPLX>(a.m, rcol(jj, 1), CPLX ? rcol(jj, 3) : nullptr, rcol(jj, 0), CPLX ? rcol(jj, 2) : nullptr, eq_,
+                      ep_, fq0, fp0, lv, zr_, zi_);
+    if (act && (lane % L) == 0) {
+      cj = j;
+      ep = ep_; fp_ = fp0; eq = eq_; fq = fq0;
+      live = lv;
+      zr = zr_;
+      zi = zi_;
+    }
+  }
+  tphase(2);
+  if (cj >= 0) {
+    const int j = cj;
+    const long long p = colp(j), q = colq(j);
+    {
       PairState<T> &s = ps[j];
       s.ep = ep; s.fp = fp_; s.eq = eq; s.fq = fq;
       if (!live) {

@@ -4,23 +4,29 @@
 // done in FP32 and only the last ones in FP64. Starting from G_0 = A (FP64), V_0 = I, each
 // preconditioning stage s = 1..S
 //   1. rounds G_{s-1} (scaled by a power of two to max |g_ij| <= 1) to FP32;
-//   2. runs FP32 one-sided Jacobi sweeps on it (k_presweep, Hestenes rotations from plain
-//      FP32 dot products) from W := I until no pair exceeds the FP32 tolerance;
+//   2. runs FP32 one-sided Jacobi sweeps on it (k_presweep_reg / k_presweep, Hestenes
+//      rotations from plain FP32 dot products) from W := I until no pair exceeds the FP32
+//      tolerance;
 //   3. widens W to FP64 and makes it orthonormal to FP64 accuracy with two Newton-Schulz
 //      polar steps, W <- W (3I - W^H W) / 2 (W is orthonormal to ~1e-5, and each step
 //      squares the error);
 //   4. forms G_s = G_{s-1} W and V_s = V_{s-1} W (FP64 GEMMs).
 // FP32 rounding is relative to each element, so from the second stage on the FP32 sweeps
 // see the columns of G_{s-1} to their own relative accuracy and resolve the directions of
-// small singular values that the first stage (on A itself) could not. Finally
-// dvjsvd_/zvjsvd_'s algorithm runs on G_S with V_S as the preset matrix (the reference's
-// iwork[0] != 0 mode, src/dvjsvd.c:88-96, src/zvjsvd.c:100-110): G_S R = U Sigma and
-// V_S R = V, so A = U Sigma V^H with the FP64 algorithm's accuracy, after a few FP64
-// sweeps instead of a full run. The GEMMs are plain library GEMMs (cuBLAS DGEMM; four
+// small singular values that the first stage (on A itself) could not. FP64 sweeps with
+// plain dot products (the same step kernel in FP64, on G and V themselves) then bring the
+// columns to FP64 orthogonality. Finally dvjsvd_/zvjsvd_'s algorithm runs on G with V as
+// the preset matrix (the reference's iwork[0] != 0 mode, src/dvjsvd.c:88-96,
+// src/zvjsvd.c:100-110): G R = U Sigma and V R = V, so A = U Sigma V^H with the FP64
+// algorithm's accuracy and convergence test, after one or two of its sweeps instead of a
+// full run. The GEMMs are plain library GEMMs (cuBLAS DGEMM; four
 // real products per complex one on the split planes).
 #include <cmath>
 #include <cstdio>
+#include <chrono>
 #include <cstring>
+#include <algorithm>
+#include <vector>
 
 #include <cublas_v2.h>
 #include <cuda_runtime.h>
@@ -72,44 +78,47 @@ __global__ void k_absmax(const double *A, long long ld, long long rows, long lon
     atomicMax(out, mx);
 }
 
-// One pivot step of FP32 one-sided Jacobi on planar G (m x n, ld m) and W (n x n, ld n):
-// CTA k takes pair (p, q) = row st of the pivot table, forms a = |g_p|^2, b = |g_q|^2,
-// c = g_p^H g_q (FP32, per-thread partial sums and a block tree), and when
-// |c| >= tol sqrt(a b) applies the unitary [[cs, sn e^{i phi}], [-sn e^{-i phi}, cs]]
-// (c = |c| e^{i phi}; t = sn/cs the smaller root of t^2 + 2 zeta t - 1 = 0,
-// zeta = (b - a) / (2|c|)) to columns p and q of G and W, which makes them orthogonal.
-template <bool CPLX>
-__global__ void __launch_bounds__(256) k_presweep(int m, int n, float *Gr, float *Gi, float *Wr, float *Wi,
-                                                  const unsigned *js, int st, float tol, unsigned *cnt)
+// Vector of 16 bytes: 4 floats or 2 doubles.
+template <typename T> struct vec16;
+template <> struct vec16<float> { using V = float4; static constexpr int E = 4; };
+template <> struct vec16<double> { using V = double2; static constexpr int E = 2; };
+
+// Hestenes rotation of a Hermitian 2x2 Gram block [[a, c], [conj c, b]]: with c = |c| e^{i phi},
+// t = sn/cs the smaller root of t^2 + 2 zeta t - 1 = 0, zeta = (b - a) / (2|c|), the unitary
+// [[cs, sn e^{i phi}], [-sn e^{-i phi}, cs]] applied to columns (p, q) makes them
+// orthogonal. Sets rot = {cs, sn cos phi, sn sin phi, go}; go = 0 when |c| < tol sqrt(a b).
+template <typename T> __device__ void hestenes(T a, T b, T cr, T ci, T tol, T *rot, unsigned *cnt)
 {
-  __shared__ float red[4][8];
-  __shared__ float rot[4];
-  const int k = blockIdx.x;
-  const unsigned p = js[(size_t)st * n + 2 * k], q = js[(size_t)st * n + 2 * k + 1];
-  float *gpr = Gr + (size_t)p * m, *gqr = Gr + (size_t)q * m;
-  float *gpi = CPLX ? Gi + (size_t)p * m : nullptr, *gqi = CPLX ? Gi + (size_t)q * m : nullptr;
-  float a = 0.f, b = 0.f, cr = 0.f, ci = 0.f;
-  for (int i = threadIdx.x; i < m; i += blockDim.x) {
-    const float xr = gpr[i], yr = gqr[i];
-    a = fmaf(xr, xr, a);
-    b = fmaf(yr, yr, b);
-    cr = fmaf(xr, yr, cr);
-    if (CPLX) {
-      const float xi = gpi[i], yi = gqi[i];
-      a = fmaf(xi, xi, a);
-      b = fmaf(yi, yi, b);
-      cr = fmaf(xi, yi, cr);
-      ci = fmaf(xr, yi, ci);
-      ci = fmaf(-xi, yr, ci);
-    }
+  const T ac = hypot(cr, ci);
+  T cs = 1, snr = 0, sni = 0, go = 0;
+  if (ac > (T)0 && ac >= tol * sqrt(a) * sqrt(b)) {
+    const T zeta = (b - a) / ((T)2 * ac);
+    const T az = fabs(zeta);
+    const T big = (sizeof(T) == 4) ? (T)1e18 : (T)1e150;
+    const T t = (az > big) ? (T)0.5 / zeta : copysign((T)1, zeta) / (az + sqrt(fma(zeta, zeta, (T)1)));
+    cs = (T)1 / sqrt(fma(t, t, (T)1));
+    const T sn = t * cs;
+    snr = sn * (cr / ac);
+    sni = sn * (ci / ac);
+    go = 1;
+    atomicAdd(cnt, 1u);
   }
+  rot[0] = cs;
+  rot[1] = snr;
+  rot[2] = sni;
+  rot[3] = go;
+}
+
+// CTA-wide sums of a, b, cr, ci (256 threads) into thread 0
+template <typename T> __device__ void block_sum4(T &a, T &b, T &cr, T &ci, T (*red)[8])
+{
   for (int o = 16; o >= 1; o >>= 1) {
     a += __shfl_xor_sync(0xffffffffu, a, o);
     b += __shfl_xor_sync(0xffffffffu, b, o);
     cr += __shfl_xor_sync(0xffffffffu, cr, o);
     ci += __shfl_xor_sync(0xffffffffu, ci, o);
   }
-  const int w = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  const int w = threadIdx.x >> 5;
   if ((threadIdx.x & 31) == 0) {
     red[0][w] = a;
     red[1][w] = b;
@@ -118,54 +127,246 @@ __global__ void __launch_bounds__(256) k_presweep(int m, int n, float *Gr, float
   }
   __syncthreads();
   if (threadIdx.x == 0) {
-    a = b = cr = ci = 0.f;
-    for (int j = 0; j < nw; ++j) {
+    a = b = cr = ci = 0;
+    for (int j = 0; j < 8; ++j) {
       a += red[0][j];
       b += red[1][j];
       cr += red[2][j];
       ci += red[3][j];
     }
-    const float ac = hypotf(cr, ci);
-    float cs = 1.f, snr = 0.f, sni = 0.f, go = 0.f;
-    if (ac > 0.f && ac >= tol * sqrtf(a) * sqrtf(b)) {
-      const float zeta = (b - a) / (2.f * ac);
-      const float az = fabsf(zeta);
-      const float t = (az > 1e18f) ? 0.5f / zeta : copysignf(1.f, zeta) / (az + sqrtf(fmaf(zeta, zeta, 1.f)));
-      cs = 1.f / sqrtf(fmaf(t, t, 1.f));
-      const float sn = t * cs;
-      snr = sn * (cr / ac);
-      sni = sn * (ci / ac);
-      go = 1.f;
-      atomicAdd(cnt, 1u);
-    }
-    rot[0] = cs;
-    rot[1] = snr;
-    rot[2] = sni;
-    rot[3] = go;
   }
+}
+
+// (p, q) <- (cs p - sn e^{-i phi} q, sn e^{i phi} p + cs q), element-wise
+template <typename T, bool CPLX>
+__device__ __forceinline__ void rot_elem(T cs, T snr, T sni, T &pr, T &pi, T &qr, T &qi)
+{
+  const T Pr = pr, Qr = qr;
+  if (CPLX) {
+    const T Pi = pi, Qi = qi;
+    pr = cs * Pr - (snr * Qr + sni * Qi);
+    pi = cs * Pi - (snr * Qi - sni * Qr);
+    qr = (snr * Pr - sni * Pi) + cs * Qr;
+    qi = (snr * Pi + sni * Pr) + cs * Qi;
+  }
+  else {
+    pr = cs * Pr - snr * Qr;
+    qr = snr * Pr + cs * Qr;
+  }
+}
+
+template <typename T, bool CPLX>
+__device__ void rot_cols(int rows, T *xr, T *xi, T *yr, T *yi, T cs, T snr, T sni)
+{
+  for (int i = threadIdx.x; i < rows; i += blockDim.x) {
+    T pr = xr[i], qr = yr[i], pi = 0, qi = 0;
+    if (CPLX) {
+      pi = xi[i];
+      qi = yi[i];
+    }
+    rot_elem<T, CPLX>(cs, snr, sni, pr, pi, qr, qi);
+    xr[i] = pr;
+    yr[i] = qr;
+    if (CPLX) {
+      xi[i] = pi;
+      yi[i] = qi;
+    }
+  }
+}
+
+// One pivot step of one-sided Jacobi (Hestenes) with plain dot products, FP32 or FP64, on
+// planar G (m x n) and W (n x n): CTA k takes pair (p, q) = row st of the pivot table,
+// forms a = |g_p|^2, b = |g_q|^2, c = g_p^H g_q (per-thread partial sums and a block
+// tree) and rotates columns p and q of G and W (hestenes above). Any m; G is read twice.
+template <typename T, bool CPLX>
+__global__ void __launch_bounds__(256) k_presweep(int m, int n, T *Gr, long long ldr, T *Gi, long long ldi, T *Wr,
+                                                  long long lwr, T *Wi, long long lwi, const unsigned *js, int st,
+                                                  T tol, unsigned *cnt)
+{
+  __shared__ T red[4][8];
+  __shared__ T rot[4];
+  const int k = blockIdx.x;
+  const unsigned p = js[(size_t)st * n + 2 * k], q = js[(size_t)st * n + 2 * k + 1];
+  T *gpr = Gr + (size_t)p * ldr, *gqr = Gr + (size_t)q * ldr;
+  T *gpi = CPLX ? Gi + (size_t)p * ldi : nullptr, *gqi = CPLX ? Gi + (size_t)q * ldi : nullptr;
+  T a = 0, b = 0, cr = 0, ci = 0;
+  for (int i = threadIdx.x; i < m; i += blockDim.x) {
+    const T xr = gpr[i], yr = gqr[i];
+    a = fma(xr, xr, a);
+    b = fma(yr, yr, b);
+    cr = fma(xr, yr, cr);
+    if (CPLX) {
+      const T xi = gpi[i], yi = gqi[i];
+      a = fma(xi, xi, a);
+      b = fma(yi, yi, b);
+      cr = fma(xi, yi, cr);
+      ci = fma(xr, yi, ci);
+      ci = fma(-xi, yr, ci);
+    }
+  }
+  block_sum4(a, b, cr, ci, red);
+  if (threadIdx.x == 0)
+    hestenes(a, b, cr, ci, tol, rot, cnt);
   __syncthreads();
-  if (rot[3] == 0.f)
+  if (rot[3] == (T)0)
     return;
-  const float cs = rot[0], snr = rot[1], sni = rot[2];
-  auto apply = [&](float *xr_, float *xi_, float *yr_, float *yi_, int rows) {
-    for (int i = threadIdx.x; i < rows; i += blockDim.x) {
-      const float pr = xr_[i], qr = yr_[i];
+  const T cs = rot[0], snr = rot[1], sni = rot[2];
+  rot_cols<T, CPLX>(m, gpr, gpi, gqr, gqi, cs, snr, sni);
+  rot_cols<T, CPLX>(n, Wr + (size_t)p * lwr, CPLX ? Wi + (size_t)p * lwi : nullptr, Wr + (size_t)q * lwr,
+                    CPLX ? Wi + (size_t)q * lwi : nullptr, cs, snr, sni);
+}
+
+// The same step with the two columns of G held in registers between the dot products and
+// the rotation (one read and one write of G): thread t owns the 16-byte vectors t + 256 r,
+// r < R, of each column, so m <= 256 R E (E = 4 floats or 2 doubles per vector); m % E == 0
+// and 16-byte aligned columns.
+template <typename T, bool CPLX, int R>
+__global__ void __launch_bounds__(256) k_presweep_reg(int m, int n, T *Gr, long long ldr, T *Gi, long long ldi,
+                                                      T *Wr, long long lwr, T *Wi, long long lwi, const unsigned *js,
+                                                      int st, T tol, unsigned *cnt)
+{
+  using V = typename vec16<T>::V;
+  constexpr int E = vec16<T>::E;
+  __shared__ T red[4][8];
+  __shared__ T rot[4];
+  const int k = blockIdx.x;
+  const unsigned p = js[(size_t)st * n + 2 * k], q = js[(size_t)st * n + 2 * k + 1];
+  V *gpr = reinterpret_cast<V *>(Gr + (size_t)p * ldr), *gqr = reinterpret_cast<V *>(Gr + (size_t)q * ldr);
+  V *gpi = CPLX ? reinterpret_cast<V *>(Gi + (size_t)p * ldi) : nullptr;
+  V *gqi = CPLX ? reinterpret_cast<V *>(Gi + (size_t)q * ldi) : nullptr;
+  const int mv = m / E;
+  V xr[R], yr[R], xi[R], yi[R];
+  T a = 0, b = 0, cr = 0, ci = 0;
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    const int i = threadIdx.x + r * 256;
+    V z;
+    T *zz = reinterpret_cast<T *>(&z);
+#pragma unroll
+    for (int e = 0; e < E; ++e)
+      zz[e] = 0;
+    xr[r] = (i < mv) ? gpr[i] : z;
+    yr[r] = (i < mv) ? gqr[i] : z;
+    if (CPLX) {
+      xi[r] = (i < mv) ? gpi[i] : z;
+      yi[r] = (i < mv) ? gqi[i] : z;
+    }
+  }
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    const T *X = reinterpret_cast<const T *>(&xr[r]), *Y = reinterpret_cast<const T *>(&yr[r]);
+    const T *Xi = reinterpret_cast<const T *>(&xi[r]), *Yi = reinterpret_cast<const T *>(&yi[r]);
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+      a = fma(X[e], X[e], a);
+      b = fma(Y[e], Y[e], b);
+      cr = fma(X[e], Y[e], cr);
       if (CPLX) {
-        const float pi = xi_[i], qi = yi_[i];
-        xr_[i] = cs * pr - (snr * qr + sni * qi);
-        xi_[i] = cs * pi - (snr * qi - sni * qr);
-        yr_[i] = (snr * pr - sni * pi) + cs * qr;
-        yi_[i] = (snr * pi + sni * pr) + cs * qi;
-      }
-      else {
-        xr_[i] = cs * pr - snr * qr;
-        yr_[i] = snr * pr + cs * qr;
+        a = fma(Xi[e], Xi[e], a);
+        b = fma(Yi[e], Yi[e], b);
+        cr = fma(Xi[e], Yi[e], cr);
+        ci = fma(X[e], Yi[e], ci);
+        ci = fma(-Xi[e], Y[e], ci);
       }
     }
-  };
-  apply(gpr, gpi, gqr, gqi, m);
-  apply(Wr + (size_t)p * n, CPLX ? Wi + (size_t)p * n : nullptr, Wr + (size_t)q * n,
-        CPLX ? Wi + (size_t)q * n : nullptr, n);
+  }
+  block_sum4(a, b, cr, ci, red);
+  if (threadIdx.x == 0)
+    hestenes(a, b, cr, ci, tol, rot, cnt);
+  __syncthreads();
+  if (rot[3] == (T)0)
+    return;
+  const T cs = rot[0], snr = rot[1], sni = rot[2];
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    const int i = threadIdx.x + r * 256;
+    if (i < mv) {
+      T *X = reinterpret_cast<T *>(&xr[r]), *Y = reinterpret_cast<T *>(&yr[r]);
+      T *Xi = reinterpret_cast<T *>(&xi[r]), *Yi = reinterpret_cast<T *>(&yi[r]);
+#pragma unroll
+      for (int e = 0; e < E; ++e) {
+        T d0 = 0, d1 = 0;
+        rot_elem<T, CPLX>(cs, snr, sni, X[e], CPLX ? Xi[e] : d0, Y[e], CPLX ? Yi[e] : d1);
+      }
+      gpr[i] = xr[r];
+      gqr[i] = yr[r];
+      if (CPLX) {
+        gpi[i] = xi[r];
+        gqi[i] = yi[r];
+      }
+    }
+  }
+  rot_cols<T, CPLX>(n, Wr + (size_t)p * lwr, CPLX ? Wi + (size_t)p * lwi : nullptr, Wr + (size_t)q * lwr,
+                    CPLX ? Wi + (size_t)q * lwi : nullptr, cs, snr, sni);
+}
+
+// one sweep of presweep steps (stp launches); returns the number of rotations or < 0
+template <typename T, bool CPLX>
+static long long presweep(int m, int n, T *Gr, long long ldr, T *Gi, long long ldi, T *Wr, long long lwr, T *Wi,
+                          long long lwi, const unsigned *js, unsigned stp, T tol, unsigned *cnt, cudaStream_t s)
+{
+  constexpr int E = vec16<T>::E;
+  const bool al = !(m % E) && !((ldr * (long long)sizeof(T)) % 16) && !((uintptr_t)Gr % 16) &&
+                  (!CPLX || (!((ldi * (long long)sizeof(T)) % 16) && !((uintptr_t)Gi % 16)));
+  if (cudaMemsetAsync(cnt, 0, 4, s) != cudaSuccess)
+    return -1;
+  const unsigned nb = (unsigned)(n / 2);
+  const long long cap = 256LL * E;  // rows per register vector slot
+  for (unsigned st = 0; st < stp; ++st) {
+    if (al && m <= cap)
+      k_presweep_reg<T, CPLX, 1><<<nb, 256, 0, s>>>(m, n, Gr, ldr, Gi, ldi, Wr, lwr, Wi, lwi, js, (int)st, tol, cnt);
+    else if (al && m <= 2 * cap)
+      k_presweep_reg<T, CPLX, 2><<<nb, 256, 0, s>>>(m, n, Gr, ldr, Gi, ldi, Wr, lwr, Wi, lwi, js, (int)st, tol, cnt);
+    else if (al && m <= 4 * cap)
+      k_presweep_reg<T, CPLX, 4><<<nb, 256, 0, s>>>(m, n, Gr, ldr, Gi, ldi, Wr, lwr, Wi, lwi, js, (int)st, tol, cnt);
+    else if (al && sizeof(T) == 8 && m <= 8 * cap)
+      k_presweep_reg<T, CPLX, (sizeof(T) == 8 ? 8 : 4)><<<nb, 256, 0, s>>>(m, n, Gr, ldr, Gi, ldi, Wr, lwr, Wi, lwi,
+                                                                          js, (int)st, tol, cnt);
+    else
+      k_presweep<T, CPLX><<<nb, 256, 0, s>>>(m, n, Gr, ldr, Gi, ldi, Wr, lwr, Wi, lwi, js, (int)st, tol, cnt);
+  }
+  unsigned hc = 0;
+  if (cudaGetLastError() != cudaSuccess || cudaMemcpyAsync(&hc, cnt, 4, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+      cudaStreamSynchronize(s) != cudaSuccess)
+    return -1;
+  return (long long)hc;
+}
+
+// squared 2-norms of the columns of planar G (one CTA per column)
+template <bool CPLX>
+__global__ void __launch_bounds__(256) k_colnorm2(int m, const double *Gr, long long ldr, const double *Gi,
+                                                  long long ldi, double *out)
+{
+  __shared__ double red[8];
+  const int j = blockIdx.x;
+  double a = 0;
+  for (int i = threadIdx.x; i < m; i += 256) {
+    const double x = Gr[(size_t)j * ldr + i];
+    a = fma(x, x, a);
+    if (CPLX) {
+      const double y = Gi[(size_t)j * ldi + i];
+      a = fma(y, y, a);
+    }
+  }
+  for (int o = 16; o >= 1; o >>= 1)
+    a += __shfl_xor_sync(0xffffffffu, a, o);
+  if ((threadIdx.x & 31) == 0)
+    red[threadIdx.x >> 5] = a;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    a = 0;
+    for (int w = 0; w < 8; ++w)
+      a += red[w];
+    out[j] = a;
+  }
+}
+
+// B[:, j] = A[:, perm[j]] (rows x n, B with leading dimension rows)
+__global__ void k_gather_cols(int rows, int n, const double *A, long long lda, const int *perm, double *B)
+{
+  for (int j = blockIdx.y; j < n; j += gridDim.y)
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < rows; i += gridDim.x * blockDim.x)
+      B[(size_t)j * rows + i] = A[(size_t)perm[j] * lda + i];
 }
 
 static dim3 grid2(long long rows, long long cols)
@@ -218,11 +419,11 @@ static bool copy2d(double *dst, long long ldd, const double *src, long long lds,
 template <bool CPLX>
 static vj_fint mixed_dev(vj_fnat m_, vj_fnat n_, double *G, vj_fnat ldG, double *Gi, vj_fnat ldGi, double *V,
                          vj_fnat ldV, double *Vi, vj_fnat ldVi, double *eS, double *fS, const unsigned *js,
-                         unsigned stp, unsigned swp, unsigned stages, cudaStream_t s, unsigned *sweeps32)
+                         unsigned stp, unsigned swp, unsigned stages, cudaStream_t s, unsigned *presweeps)
 {
   const long long m = (long long)m_, n = (long long)n_;
-  if (sweeps32)
-    *sweeps32 = 0;
+  if (presweeps)
+    presweeps[0] = presweeps[1] = 0;
   if (!n)
     return 0;
   // the FP64 phase checks the reference's shape rules (src/dvjsvd.c:43-68) itself; they are
@@ -234,7 +435,7 @@ static vj_fint mixed_dev(vj_fnat m_, vj_fnat n_, double *G, vj_fnat ldG, double 
   if (m > 0x3fffffffLL)
     return VJ_ERR_ARG;
   if (!stages)
-    stages = 3;
+    stages = 2;
   if (!host::gpu_ready())
     return VJ_ERR_NO_GPU;
   cublasHandle_t h = cublas();
@@ -267,6 +468,12 @@ static vj_fint mixed_dev(vj_fnat m_, vj_fnat n_, double *G, vj_fnat ldG, double 
   const float tol = fmaxf(0.5f * sqrtf((float)m), 8.f) * 5.9604645e-8f;
   const unsigned maxsw = swp < 60u ? swp : 60u;
   unsigned total32 = 0;
+  // with VJ_TRACE=1, the wall-clock time of each phase goes to stderr (every phase ends
+  // with a stream synchronisation, so host time is device time here)
+  const bool trace = host::trace_enabled();
+  auto now = [] { return std::chrono::steady_clock::now(); };
+  auto t0 = now();
+  double ms32 = 0, msgemm = 0;
   for (unsigned stage = 0; stage < stages; ++stage) {
     // 1. scale to max |g| in [1/2, 1) and round to FP32
     if (cudaMemsetAsync(cell, 0, 8, s) != cudaSuccess)
@@ -295,19 +502,19 @@ static vj_fint mixed_dev(vj_fnat m_, vj_fnat n_, double *G, vj_fnat ldG, double 
     // 2. FP32 sweeps until a sweep rotates nothing
     unsigned sw = 0;
     for (; sw < maxsw; ++sw) {
-      if (cudaMemsetAsync(cnt, 0, 4, s) != cudaSuccess)
-        return VJ_ERR_CUDA;
-      for (unsigned st = 0; st < stp; ++st)
-        k_presweep<CPLX><<<(unsigned)(n / 2), 256, 0, s>>>(mi, ni, G32, CPLX ? G32 + mn : nullptr, W32,
-                                                          CPLX ? W32 + nn : nullptr, js, (int)st, tol, cnt);
-      unsigned hc = 0;
-      if (cudaGetLastError() != cudaSuccess || cudaMemcpyAsync(&hc, cnt, 4, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
-          cudaStreamSynchronize(s) != cudaSuccess)
+      const long long hc = presweep<float, CPLX>(mi, ni, G32, m, CPLX ? G32 + mn : nullptr, m, W32, n,
+                                                 CPLX ? W32 + nn : nullptr, n, js, stp, tol, cnt, s);
+      if (hc < 0)
         return VJ_ERR_CUDA;
       if (!hc)
         break;
     }
     total32 += sw;
+    if (trace) {
+      const auto t1 = now();
+      ms32 += std::chrono::duration<double, std::milli>(t1 - t0).count();
+      t0 = t1;
+    }
     if (!sw)
       break;  // already orthogonal to the FP32 level: later stages would change nothing
     // 3. W (FP64) with two Newton-Schulz steps: Y = W^H W, T = W Y, W = 1.5 W - 0.5 T
@@ -338,17 +545,89 @@ static vj_fint mixed_dev(vj_fnat m_, vj_fnat n_, double *G, vj_fnat ldG, double 
       if (!zgemm(h, CPLX, false, ni, ni, ni, Tp, Xp, Vpl))
         return VJ_ERR_CUDA;
     }
+    if (trace) {
+      if (cudaStreamSynchronize(s) != cudaSuccess)
+        return VJ_ERR_CUDA;
+      const auto t1 = now();
+      msgemm += std::chrono::duration<double, std::milli>(t1 - t0).count();
+      t0 = t1;
+    }
   }
-  if (sweeps32)
-    *sweeps32 = total32;
+  if (presweeps)
+    presweeps[0] = total32;
   if (!total32) {
     // nothing was rotated (zero matrix or columns already orthogonal): V := I
     k_eye_p<double><<<grid2(n, n), 256, 0, s>>>(V, (long long)ldV, n, 1);
     if (CPLX)
       k_eye_p<double><<<grid2(n, n), 256, 0, s>>>(Vi, (long long)ldVi, n, 0);
   }
-  // 5. FP64 finishing sweeps with V preset
-  return svd_dev_entry<double, CPLX>(m_, n_, G, ldG, Gi, ldGi, V, ldV, Vi, ldVi, eS, fS, js, stp, swp, 1, s);
+  // 5. FP64 sweeps with plain dot products on G and V themselves until no pair reaches half
+  //    the reference's tolerance sqrt(m) eps / 2 (at most 20 sweeps): they take the columns from
+  //    FP32 to FP64 orthogonality at a fraction of a reference sweep's cost (about 12 FP64
+  //    operations per complex element instead of 68), so the reference's sweeps below
+  //    have at most the last rotations to do and the convergence to confirm.
+  if (total32) {
+    // half the reference's tolerance: the plain dot product's rounding (a few eps) stays
+    // well below it, and pairs the reference would still rotate are rotated here
+    const double tol64 = 0.5 * std::sqrt((double)m) * 1.1102230246251565e-16;
+    const unsigned maxsw64 = swp < 20u ? swp : 20u;
+    unsigned sw64 = 0;
+    for (; sw64 < maxsw64; ++sw64) {
+      const long long hc = presweep<double, CPLX>(mi, ni, G, (long long)ldG, Gi, (long long)(CPLX ? ldGi : ldG), V,
+                                                  (long long)ldV, Vi, (long long)(CPLX ? ldVi : ldV), js, stp, tol64,
+                                                  cnt, s);
+      if (hc < 0)
+        return VJ_ERR_CUDA;
+      if (!hc)
+        break;
+    }
+    if (presweeps)
+      presweeps[1] = sw64;
+    // columns in descending order of their norms, the order the reference's sweeps keep
+    // (src/dvjsvd.c:367-370): its sweeps then have no pair to reorder
+    double *nrm = T;  // n entries of scratch
+    int *perm = reinterpret_cast<int *>(T + n);
+    k_colnorm2<CPLX><<<(unsigned)n, 256, 0, s>>>(mi, G, (long long)ldG, Gi, (long long)(CPLX ? ldGi : ldG), nrm);
+    std::vector<double> hn((size_t)n);
+    std::vector<int> hp((size_t)n);
+    if (cudaMemcpyAsync(hn.data(), nrm, (size_t)n * 8, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess)
+      return VJ_ERR_CUDA;
+    for (int j = 0; j < ni; ++j)
+      hp[(size_t)j] = j;
+    std::stable_sort(hp.begin(), hp.end(), [&](int x, int y) { return hn[(size_t)x] > hn[(size_t)y]; });
+    bool moved = false;
+    for (int j = 0; j < ni && !moved; ++j)
+      moved = (hp[(size_t)j] != j);
+    if (moved) {
+      if (cudaMemcpyAsync(perm, hp.data(), (size_t)n * 4, cudaMemcpyHostToDevice, s) != cudaSuccess)
+        return VJ_ERR_CUDA;
+      for (int pl = 0; pl < P; ++pl) {
+        double *Gd = pl ? Gi : G, *Vd = pl ? Vi : V;
+        const long long lg = pl ? (long long)ldGi : (long long)ldG, lv = pl ? (long long)ldVi : (long long)ldV;
+        k_gather_cols<<<grid2(m, n), 256, 0, s>>>(mi, ni, Gd, lg, perm, Gp);
+        k_gather_cols<<<grid2(n, n), 256, 0, s>>>(ni, ni, Vd, lv, perm, Y);
+        if (!copy2d(Gd, lg, Gp, m, m, n, s) || !copy2d(Vd, lv, Y, n, n, n, s))
+          return VJ_ERR_CUDA;
+      }
+      // the host vectors are read by the copy above: wait before they go out of scope
+      if (cudaStreamSynchronize(s) != cudaSuccess)
+        return VJ_ERR_CUDA;
+    }
+  }
+  double ms64 = 0;
+  if (trace) {
+    const auto t1 = now();
+    ms64 = std::chrono::duration<double, std::milli>(t1 - t0).count();
+    t0 = t1;
+  }
+  // 6. FP64 finishing sweeps (the reference's algorithm) with V preset
+  const vj_fint r = svd_dev_entry<double, CPLX>(m_, n_, G, ldG, Gi, ldGi, V, ldV, Vi, ldVi, eS, fS, js, stp, swp, 1, s);
+  if (trace)
+    std::fprintf(stderr, "mixed SVD phases (ms): FP32 sweeps %.1f, Newton-Schulz + GEMMs %.1f, plain FP64 sweeps + sort %.1f, "
+                 "finishing %.1f\n", ms32, msgemm, ms64,
+                 std::chrono::duration<double, std::milli>(now() - t0).count());
+  return r;
 }
 
 }  // namespace vj
@@ -357,18 +636,18 @@ extern "C" {
 
 vj_fint vj_dvjsvd_mixed_dev(vj_fnat m, vj_fnat n, double *G, vj_fnat ldG, double *V, vj_fnat ldV, double *eS,
                             double *fS, const unsigned *js, unsigned stp, unsigned swp, unsigned stages,
-                            unsigned *sweeps32, void *stream)
+                            unsigned *presweeps, void *stream)
 {
   return vj::mixed_dev<false>(m, n, G, ldG, nullptr, ldG, V, ldV, nullptr, ldV, eS, fS, js, stp, swp, stages,
-                              (cudaStream_t)stream, sweeps32);
+                              (cudaStream_t)stream, presweeps);
 }
 
 vj_fint vj_zvjsvd_mixed_dev(vj_fnat m, vj_fnat n, double *Gr, vj_fnat ldGr, double *Gi, vj_fnat ldGi, double *Vr,
                             vj_fnat ldVr, double *Vi, vj_fnat ldVi, double *eS, double *fS, const unsigned *js,
-                            unsigned stp, unsigned swp, unsigned stages, unsigned *sweeps32, void *stream)
+                            unsigned stp, unsigned swp, unsigned stages, unsigned *presweeps, void *stream)
 {
   return vj::mixed_dev<true>(m, n, Gr, ldGr, Gi, ldGi, Vr, ldVr, Vi, ldVi, eS, fS, js, stp, swp, stages,
-                             (cudaStream_t)stream, sweeps32);
+                             (cudaStream_t)stream, presweeps);
 }
 
 }  // extern "C"

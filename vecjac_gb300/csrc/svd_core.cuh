@@ -322,69 +322,79 @@ __device__ void pair_dot(long long m, const T *xr, const T *xi, const T *yr, con
   zi = CPLX ? fp<T>::div(nui, de) : (T)0;
 }
 
-// The same scaled compensated dot products (FP64 only) with each accumulator chain on its
-// own group of 8 threads: the reference's 8 lanes keep their element order and their
-// 2Sum recurrences, but the independent recurrences of one lane -- the round-down products
-// (pd) and their exact errors (dn), for the real and, for complex data, the imaginary part
-// -- run in different threads: chain 0-1 (real) or 0-3 (complex) says which recurrence,
-// l8 is the lane. On GB300 each SM sub-partition issues about one FP64 warp instruction per
-// 76 cycles whatever the number of active lanes, so a pair's FP64 work spread over 2 or 4
-// chains finishes 2 or 4 times sooner than on one warp's 8 lanes. All threads run the
-// same instruction stream (each forms pd and dn and keeps the one its chain accumulates),
-// and the result combines the chains in the reference's order,
-// nu = S(s_pd) + (S(t_pd) + (S(s_dn) + S(t_dn))), S = the 8-lane halving tree. The result
-// is valid on the pair's first thread; every thread of the warp must call this.
-template <typename T, bool CPLX>
-__device__ void pair_dot_split(long long m, const T *xr, const T *xi, const T *yr, const T *yi, T ex, T ey, T fx, T fy,
-                               bool live, int chain, int l8, T &zr, T &zi)
+// The same scaled compensated dot products (FP64 only) with the independent accumulator
+// chains of one lane in different warps. The reference keeps, per lane, two 2Sum
+// recurrences (round-down products pd and their exact errors dn; src/ddpscl.c:46-60) for
+// real data and four for complex data (real and imaginary parts; src/zdpscl.c:58-80).
+// Chain C (bit 0: dn instead of pd, bit 1: imaginary part) of pairs 0..3 runs on one warp,
+// pair j on lanes [8j, 8j+8): every lane keeps the reference's element order and
+// recurrence, the chains of a lane just run side by side on different sub-partitions,
+// each warp with one instruction stream (no per-thread selects: on GB300 an FP64 result
+// that goes through the integer pipes costs hundreds of cycles). Elements are loaded a
+// block of four ahead of their accumulation, so that L2 latency (columns not staged in
+// shared memory) overlaps the recurrence. Returns the 8-lane halving-tree sums of s and t
+// on lane 8j.
+template <typename T, bool CPLX, int C>
+__device__ void chain_dot(long long m, const T *xr, const T *xi, const T *yr, const T *yi, T ex, T ey, bool live,
+                          int l8, T &S, T &Tt)
 {
-  static_assert(sizeof(T) == 8, "the split dot product is the FP64 form");
+  static_assert(sizeof(T) == 8, "the chain-split dot product is the FP64 form");
+  constexpr bool DN = (C & 1) != 0, IM = (C & 2) != 0;
+  constexpr int NV = CPLX ? 4 : 2;  // values loaded per element
+  constexpr int D = 4;              // elements per block: the next block's loads are in flight
+                                    // while this block is accumulated (hides L2 latency)
   const int nx = -(int)ex, ny = -(int)ey;
-  const bool err = (chain & 1) != 0;              // accumulate dn instead of pd
-  const bool imp = CPLX && (chain >= 2);          // imaginary part: xr yi + (-xi) yr
-  const unsigned long long flip = imp ? 0x8000000000000000ull : 0ull;
   T s = 0, t = 0;
-  auto acc = [&](T x, T y) {
-    const T pd = fp<T>::mul_rd(x, y);
-    const T dn = fp<T>::fma_(x, y, -pd);
-    two_sum(s, (err ? dn : pd) + t, s, t);
+  auto load = [&](long long i, T (&v)[NV]) {
+    if (i < m) {
+      v[0] = xr[i];
+      v[1] = yr[i];
+      if (CPLX) {
+        v[2] = xi[i];
+        v[3] = yi[i];
+      }
+    }
+  };
+  // accumulate element i from its raw values: real part xr yr, xi yi; imaginary part
+  // xr yi, xi (-yr) (= (-xi) yr exactly)
+  auto acc = [&](const T (&v)[NV]) {
+    const T xr_ = scale2(v[0], nx), yr_ = scale2(v[1], ny);
+    T a0 = xr_, b0 = yr_;
+    const T p0 = fp<T>::mul_rd(a0, b0);
+    if (CPLX) {
+      const T xi_ = scale2(v[2], nx), yi_ = scale2(v[3], ny);
+      b0 = IM ? yi_ : yr_;
+      const T a1 = xi_, b1 = IM ? -yr_ : yi_;
+      const T q0 = fp<T>::mul_rd(a0, b0);
+      const T q1 = fp<T>::mul_rd(a1, b1);
+      two_sum(s, (DN ? fp<T>::fma_(a0, b0, -q0) : q0) + t, s, t);
+      two_sum(s, (DN ? fp<T>::fma_(a1, b1, -q1) : q1) + t, s, t);
+    }
+    else
+      two_sum(s, (DN ? fp<T>::fma_(a0, b0, -p0) : p0) + t, s, t);
   };
   if (live && l8 < m) {
-    T x0 = scale2(xr[l8], nx), y0 = scale2(yr[l8], ny), x1 = 0, y1 = 0;
-    if (CPLX) {
-      x1 = scale2(xi[l8], nx);
-      y1 = scale2(yi[l8], ny);
-    }
-    for (long long i = l8; i < m; i += 8) {
-      const long long inx = (i + 8 < m) ? (i + 8) : i;
-      const T nx0 = scale2(xr[inx], nx), ny0 = scale2(yr[inx], ny);
-      T nx1 = 0, ny1 = 0;
-      if (CPLX) {
-        nx1 = scale2(xi[inx], nx);
-        ny1 = scale2(yi[inx], ny);
-        // real part: xr yr, xi yi; imaginary part: xr yi, xi (-yr) (= (-xi) yr exactly)
-        const T b0 = imp ? y1 : y0;
-        const T b1 = imp ? __longlong_as_double((long long)((unsigned long long)__double_as_longlong(y0) ^ flip)) : y1;
-        acc(x0, b0);
-        acc(x1, b1);
-      }
-      else
-        acc(x0, y0);
-      x0 = nx0;
-      y0 = ny0;
-      x1 = nx1;
-      y1 = ny1;
+    T cur[D][NV], nxt[D][NV];
+#pragma unroll
+    for (int d = 0; d < D; ++d)
+      load(l8 + 8LL * d, cur[d]);
+    for (long long i0 = l8; i0 < m; i0 += 8LL * D) {
+#pragma unroll
+      for (int d = 0; d < D; ++d)
+        load(i0 + 8LL * (D + d), nxt[d]);
+#pragma unroll
+      for (int d = 0; d < D; ++d)
+        if (i0 + 8LL * d < m)
+          acc(cur[d]);
+#pragma unroll
+      for (int d = 0; d < D; ++d)
+#pragma unroll
+        for (int k = 0; k < NV; ++k)
+          cur[d][k] = nxt[d][k];
     }
   }
-  const T S = hsum<8>(s), Tt = hsum<8>(t);
-  const T Sdn = __shfl_down_sync(0xffffffffu, S, 8), Tdn = __shfl_down_sync(0xffffffffu, Tt, 8);
-  const T nu = S + (Tt + (Sdn + Tdn));
-  T nui = 0;
-  if (CPLX)
-    nui = __shfl_down_sync(0xffffffffu, nu, 16);
-  const T de = fx * fy;
-  zr = fp<T>::div(nu, de);
-  zi = CPLX ? fp<T>::div(nui, de) : (T)0;
+  S = hsum<8>(s);
+  Tt = hsum<8>(t);
 }
 
 // efcmp (src/defops.h:46)
