@@ -318,9 +318,11 @@ def e2e_bjac2(args, vj, dist, world):
             "path": "C ABI dbjac2_/zbjac2_/sbjac2_/cbjac2_ on pageable host buffers"}
 
 
-def cpu_baseline_bjac2(elems_lg, threads=None):
+def cpu_baseline_bjac2(elems_lg, threads=None, warmup=1, steps=None, target_s=10.0):
     """The oracle port (oracle/vjo.c, the reference's algorithm in portable C) on the host
-    cores, a bounded sample of 2^elems_lg elements per precision, all threads."""
+    cores, all threads, on a bounded sample of 2^elems_lg elements per precision: `warmup`
+    untimed passes, then `steps` timed passes (None: as many as fill about target_s
+    seconds, at most 64). One pass = d, z, s and c batches of the sample, n < 0."""
     from concurrent.futures import ThreadPoolExecutor
 
     from oracle import oracle as O
@@ -330,14 +332,13 @@ def cpu_baseline_bjac2(elems_lg, threads=None):
     threads = threads or os.cpu_count()
     n = 1 << elems_lg
     data = {k: W.pairs2x2(k, n, 7) for k in "dzsc"}
+    outs = {k: [np.empty(n, data[k][0].dtype) for _ in range(5)] for k in "dzsc"}
+    perm = {k: np.empty(n // 8, np.uint32) for k in "dzsc"}
     chunk = n // threads
     chunk -= chunk % 16
 
-    def run_kind(k):
-        ins = data[k]
-        dt = ins[0].dtype
-        outs = [np.empty(n, dt) for _ in range(5)]
-        p = np.empty(n // 8, np.uint32)
+    def run_kind(k, ex):
+        ins, out, p = data[k], outs[k], perm[k]
         f = R.fn(k + "bjac2_")
         f.restype = C.c_longlong
         lanes = 8 if k in "dz" else 16
@@ -345,43 +346,49 @@ def cpu_baseline_bjac2(elems_lg, threads=None):
         def part(off):
             cnt = min(chunk, n - off)
             nn = C.c_longlong(-cnt)
-            ptr = lambda a, elt=1: C.c_void_p(a.ctypes.data + off * a.itemsize // elt)
+            ptr = lambda a: C.c_void_p(a.ctypes.data + off * a.itemsize)
             if k in "zc":
-                f(C.byref(nn), ptr(ins[0]), ptr(ins[1]), ptr(ins[2]), ptr(ins[3]), ptr(outs[0]), ptr(outs[1]),
-                  ptr(outs[2]), ptr(outs[3]), ptr(outs[4]), C.c_void_p(p.ctypes.data + (off // lanes) * 4))
+                f(C.byref(nn), ptr(ins[0]), ptr(ins[1]), ptr(ins[2]), ptr(ins[3]), ptr(out[0]), ptr(out[1]),
+                  ptr(out[2]), ptr(out[3]), ptr(out[4]), C.c_void_p(p.ctypes.data + (off // lanes) * 4))
             else:
-                f(C.byref(nn), ptr(ins[0]), ptr(ins[1]), ptr(ins[2]), ptr(outs[0]), ptr(outs[1]), ptr(outs[2]),
-                  ptr(outs[3]), C.c_void_p(p.ctypes.data + (off // lanes) * 4))
+                f(C.byref(nn), ptr(ins[0]), ptr(ins[1]), ptr(ins[2]), ptr(out[0]), ptr(out[1]), ptr(out[2]),
+                  ptr(out[3]), C.c_void_p(p.ctypes.data + (off // lanes) * 4))
 
-        with ThreadPoolExecutor(threads) as ex:
-            list(ex.map(part, range(0, n, chunk)))
+        list(ex.map(part, range(0, n, chunk)))
 
-    t = time.perf_counter()
-    for k in "dzsc":
-        run_kind(k)
-    el = time.perf_counter() - t
+    with ThreadPoolExecutor(threads) as ex:
+        def one_pass():
+            t0 = time.perf_counter()
+            for k in "dzsc":
+                run_kind(k, ex)
+            return time.perf_counter() - t0
+
+        t1 = 0.0
+        for _ in range(max(1, warmup)):
+            t1 = one_pass()
+        if steps is None:
+            steps = int(min(64, max(1, round(target_s / max(t1, 1e-3)))))
+        el = sum(one_pass() for _ in range(steps))
     total = sum(BPE[k] * n for k in "dzsc")
-    return {"value": round(total / el / 1e9, 3), "unit": "GB/s", "cores": threads, "kind": "port",
-            "sample": "2^%d elements each of d/z/s/c (n<0), oracle/vjo.c on %d host threads" % (elems_lg, threads),
-            "seconds": round(el, 2)}
+    return {"value": round(total * steps / el / 1e9, 3), "unit": "GB/s", "cores": threads, "kind": "port",
+            "sample": "2^%d elements each of d/z/s/c (n<0) per pass, %d timed passes, oracle/vjo.c on %d host "
+                      "threads" % (elems_lg, steps, threads),
+            "seconds": round(el, 2), "steps": steps, "ms_per_step": round(el / steps * 1e3, 3)}
 
 
 def reference_arm(args, dist, rank):
     """The reference's CPU implementation of the path on this host's cores. VecJac's own
     AVX-512 code cannot be compiled on this (Arm) host, so its portable restatement in C
-    (oracle/vjo.c) is timed; each step is a bounded sample of the same workload."""
+    (oracle/vjo.c) is timed: W untimed and K timed steps, each step one pass over a
+    bounded sample of the same workload (2^cpu_elems elements per precision)."""
     if rank != 0:
         return None
-    base = cpu_baseline_bjac2(args.cpu_elems)
-    for _ in range(max(0, args.warmup - 1)):
-        pass
-    vals = [base["value"]]
-    for _ in range(max(1, args.steps) - 1):
-        vals.append(cpu_baseline_bjac2(args.cpu_elems)["value"])
-    v = float(np.median(vals))
+    base = cpu_baseline_bjac2(args.cpu_elems, warmup=args.warmup, steps=max(1, args.steps))
+    v = base["value"]
     return {"metric": "batched 2x2 Hermitian EVD throughput (GB/s of HBM traffic)", "value": v, "unit": "GB/s",
-            "n_gpus": 1, "steps": len(vals), "warmup": 0, "ms_per_step": None, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64+f32", "data": "synthetic (seeded)",
+            "n_gpus": 1, "steps": base["steps"], "warmup": args.warmup, "ms_per_step": base["ms_per_step"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64+f32",
+            "data": "synthetic (seeded)",
             "config": {"workload": "bjac2: d/z/s/c 2x2 EVD, bounded CPU sample 2^%d each" % args.cpu_elems},
             "impl": "reference",
             "cpu_baseline": {"value": v, "unit": "GB/s", "cores": base["cores"], "kind": "port",
@@ -733,7 +740,7 @@ def main():
     ap.add_argument("--e2e-shift", type=int, default=0, help="further shrink of the e2e batches")
     ap.add_argument("--no-e2e", dest="e2e", action="store_false")
     ap.add_argument("--no-cpu", dest="cpu_baseline", action="store_false")
-    ap.add_argument("--cpu-elems", type=int, default=22)
+    ap.add_argument("--cpu-elems", type=int, default=24)
     ap.add_argument("--pivot", type=int, default=4, help="pivot strategy id for the SVD workloads")
     args = ap.parse_args()
     if args.impl == "reference":
