@@ -57,6 +57,7 @@ __global__ void __launch_bounds__(256) k_step(SvdArgs<T> a, int st, int g3, int 
   __shared__ unsigned long long red[8][2];
   __shared__ int s_err;
   __shared__ unsigned long long bar;
+  pdl_enter();
   SvdGlobal *const g = a.g;
   if (*(volatile long long *)&g->err)
     return;
@@ -579,18 +580,16 @@ static vj_fint svd_dev(vj_fnat m_, vj_fnat n_, T *G, vj_fnat ldG, T *Gi, vj_fnat
     for (unsigned st = 0; st < stp; ++st, ++gstep) {
       const int last = ((sw + 1u == swp) && (st + 1u == stp)) ? 1 : 0;
       const int g3 = (int)(gstep % 3);
-      if (stage) {
-        if (preset)
-          k_step<T, CPLX, true, true><<<grid, blk, smem, s>>>(a, (int)st, g3, last);
-        else
-          k_step<T, CPLX, false, true><<<grid, blk, smem, s>>>(a, (int)st, g3, last);
-      }
-      else {
-        if (preset)
-          k_step<T, CPLX, true, false><<<grid, blk, 0, s>>>(a, (int)st, g3, last);
-        else
-          k_step<T, CPLX, false, false><<<grid, blk, 0, s>>>(a, (int)st, g3, last);
-      }
+      const int ist = (int)st;
+      cudaError_t e;
+      if (stage)
+        e = preset ? host::launch_pdl(k_step<T, CPLX, true, true>, dim3(grid), blk, smem, s, a, ist, g3, last)
+                   : host::launch_pdl(k_step<T, CPLX, false, true>, dim3(grid), blk, smem, s, a, ist, g3, last);
+      else
+        e = preset ? host::launch_pdl(k_step<T, CPLX, true, false>, dim3(grid), blk, 0, s, a, ist, g3, last)
+                   : host::launch_pdl(k_step<T, CPLX, false, false>, dim3(grid), blk, 0, s, a, ist, g3, last);
+      if (e != cudaSuccess)
+        return VJ_ERR_CUDA;
     }
     if (cudaGetLastError() != cudaSuccess)
       return VJ_ERR_CUDA;

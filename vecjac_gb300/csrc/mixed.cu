@@ -31,6 +31,7 @@
 #include <cublas_v2.h>
 #include <cuda_runtime.h>
 
+#include "svd_core.cuh"
 #include "vj_fp.cuh"
 #include "vj_host.h"
 
@@ -194,6 +195,7 @@ __global__ void __launch_bounds__(256) k_presweep(int m, int n, T *Gr, long long
 {
   __shared__ T red[4][8];
   __shared__ T rot[5];
+  pdl_enter();
   const int k = blockIdx.x;
   const unsigned p = js[(size_t)st * n + 2 * k], q = js[(size_t)st * n + 2 * k + 1];
   T *gpr = Gr + (size_t)p * ldr, *gqr = Gr + (size_t)q * ldr;
@@ -239,6 +241,7 @@ __global__ void __launch_bounds__(256) k_presweep_reg(int m, int n, T *Gr, long 
   constexpr int E = vec16<T>::E;
   __shared__ T red[4][8];
   __shared__ T rot[5];
+  pdl_enter();
   const int k = blockIdx.x;
   const unsigned p = js[(size_t)st * n + 2 * k], q = js[(size_t)st * n + 2 * k + 1];
   V *gpr = reinterpret_cast<V *>(Gr + (size_t)p * ldr), *gqr = reinterpret_cast<V *>(Gr + (size_t)q * ldr);
@@ -324,19 +327,20 @@ static long long presweep(int m, int n, T *Gr, long long ldr, T *Gi, long long l
     return -1;
   const unsigned nb = (unsigned)(n / 2);
   const long long cap = 256LL * E;  // rows per register vector slot
-  for (unsigned st = 0; st < stp; ++st) {
-    if (al && m <= cap)
-      k_presweep_reg<T, CPLX, 1><<<nb, 256, 0, s>>>(m, n, Gr, ldr, Gi, ldi, Wr, lwr, Wi, lwi, js, (int)st, tol, cnt);
-    else if (al && m <= 2 * cap)
-      k_presweep_reg<T, CPLX, 2><<<nb, 256, 0, s>>>(m, n, Gr, ldr, Gi, ldi, Wr, lwr, Wi, lwi, js, (int)st, tol, cnt);
-    else if (al && m <= 4 * cap)
-      k_presweep_reg<T, CPLX, 4><<<nb, 256, 0, s>>>(m, n, Gr, ldr, Gi, ldi, Wr, lwr, Wi, lwi, js, (int)st, tol, cnt);
-    else if (al && sizeof(T) == 8 && m <= 8 * cap)
-      k_presweep_reg<T, CPLX, (sizeof(T) == 8 ? 8 : 4)><<<nb, 256, 0, s>>>(m, n, Gr, ldr, Gi, ldi, Wr, lwr, Wi, lwi,
-                                                                          js, (int)st, tol, cnt);
-    else
-      k_presweep<T, CPLX><<<nb, 256, 0, s>>>(m, n, Gr, ldr, Gi, ldi, Wr, lwr, Wi, lwi, js, (int)st, tol, cnt);
-  }
+  void (*k)(int, int, T *, long long, T *, long long, T *, long long, T *, long long, const unsigned *, int, T,
+            unsigned *) = k_presweep<T, CPLX>;
+  if (al && m <= cap)
+    k = k_presweep_reg<T, CPLX, 1>;
+  else if (al && m <= 2 * cap)
+    k = k_presweep_reg<T, CPLX, 2>;
+  else if (al && m <= 4 * cap)
+    k = k_presweep_reg<T, CPLX, 4>;
+  else if (al && sizeof(T) == 8 && m <= 8 * cap)
+    k = k_presweep_reg<T, CPLX, (sizeof(T) == 8 ? 8 : 4)>;
+  for (unsigned st = 0; st < stp; ++st)
+    if (host::launch_pdl(k, dim3(nb), dim3(256), 0, s, m, n, Gr, ldr, Gi, ldi, Wr, lwr, Wi, lwi, js, (int)st, tol,
+                         cnt) != cudaSuccess)
+      return -1;
   unsigned hc = 0;
   if (cudaGetLastError() != cudaSuccess || cudaMemcpyAsync(&hc, cnt, 4, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
       cudaStreamSynchronize(s) != cudaSuccess)

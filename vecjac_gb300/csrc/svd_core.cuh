@@ -223,6 +223,16 @@ template <typename T, bool CPLX> __device__ T col_norm(const SvdArgs<T> &a, long
   return d;
 }
 
+// Programmatic dependent launch: wait until the previous grid of the stream has completed
+// and its writes are visible (a no-op for a launch without the attribute), then allow the
+// next grid to be scheduled while this one runs, which hides the launch gap between the
+// many short step kernels of a sweep.
+__device__ __forceinline__ void pdl_enter()
+{
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 // 2Sum (src/d2sum.h)
 template <typename T> __device__ __forceinline__ void two_sum(T a, T b, T &s, T &t)
 {

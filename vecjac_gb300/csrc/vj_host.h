@@ -32,6 +32,23 @@ unsigned *batch_queue();
 // two non-blocking streams owned by the library
 bool streams2(cudaStream_t s[2]);
 
+// launch with programmatic stream serialisation (the kernel calls pdl_enter first)
+template <typename... KArgs, typename... Args>
+cudaError_t launch_pdl(void (*k)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s, Args... args)
+{
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, k, args...);
+}
+
 // per-sweep statistics of the last SVD (transformed pairs per sweep)
 void trace_reset();
 void trace_sweep(unsigned sweep, unsigned long long rotations);
