@@ -107,6 +107,9 @@ template <typename T> __device__ void hestenes(T a, T b, T cr, T ci, T tol, T *r
     go = 1;
     sw = (b + t * ac > a - t * ac) ? (T)1 : (T)0;
     atomicAdd(cnt, 1u);
+    // the largest |cos| of the rotated pairs of this sweep (non-negative floats order as
+    // their bit patterns)
+    atomicMax(cnt + 1, __float_as_uint((float)(ac / (sqrt(a) * sqrt(b)))));
   }
   rot[0] = cs;
   rot[1] = snr;
@@ -315,15 +318,17 @@ __global__ void __launch_bounds__(256) k_presweep_reg(int m, int n, T *Gr, long 
                     CPLX ? Wi + (size_t)q * lwi : nullptr, cs, snr, sni, swap);
 }
 
-// one sweep of presweep steps (stp launches); returns the number of rotations or < 0
+// one sweep of presweep steps (stp launches); returns the number of rotations or < 0, and
+// in *mu the largest |cos| of a rotated pair
 template <typename T, bool CPLX>
 static long long presweep(int m, int n, T *Gr, long long ldr, T *Gi, long long ldi, T *Wr, long long lwr, T *Wi,
-                          long long lwi, const unsigned *js, unsigned stp, T tol, unsigned *cnt, cudaStream_t s)
+                          long long lwi, const unsigned *js, unsigned stp, T tol, unsigned *cnt, cudaStream_t s,
+                          float *mu)
 {
   constexpr int E = vec16<T>::E;
   const bool al = !(m % E) && !((ldr * (long long)sizeof(T)) % 16) && !((uintptr_t)Gr % 16) &&
                   (!CPLX || (!((ldi * (long long)sizeof(T)) % 16) && !((uintptr_t)Gi % 16)));
-  if (cudaMemsetAsync(cnt, 0, 4, s) != cudaSuccess)
+  if (cudaMemsetAsync(cnt, 0, 8, s) != cudaSuccess)
     return -1;
   const unsigned nb = (unsigned)(n / 2);
   const long long cap = 256LL * E;  // rows per register vector slot
@@ -341,11 +346,12 @@ static long long presweep(int m, int n, T *Gr, long long ldr, T *Gi, long long l
     if (host::launch_pdl(k, dim3(nb), dim3(256), 0, s, m, n, Gr, ldr, Gi, ldi, Wr, lwr, Wi, lwi, js, (int)st, tol,
                          cnt) != cudaSuccess)
       return -1;
-  unsigned hc = 0;
-  if (cudaGetLastError() != cudaSuccess || cudaMemcpyAsync(&hc, cnt, 4, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+  unsigned hc[2] = {0u, 0u};
+  if (cudaGetLastError() != cudaSuccess || cudaMemcpyAsync(hc, cnt, 8, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
       cudaStreamSynchronize(s) != cudaSuccess)
     return -1;
-  return (long long)hc;
+  memcpy(mu, &hc[1], 4);
+  return (long long)hc[0];
 }
 
 // squared 2-norms of the columns of planar G (one CTA per column)
@@ -516,14 +522,21 @@ static vj_fint mixed_dev(vj_fnat m_, vj_fnat n_, double *G, vj_fnat ldG, double 
     if (CPLX)
       k_eye_p<float><<<grid2(n, n), 256, 0, s>>>(W32 + nn, n, n, 0);
     // 2. FP32 sweeps until a sweep rotates nothing
+    // (a sweep whose rotated pairs were all within 4x the tolerance ends the stage without
+    // a confirming sweep: the stage is a preconditioner, the next one finishes the work)
     unsigned sw = 0;
     for (; sw < maxsw; ++sw) {
+      float mu = 0.f;
       const long long hc = presweep<float, CPLX>(mi, ni, G32, m, CPLX ? G32 + mn : nullptr, m, W32, n,
-                                                 CPLX ? W32 + nn : nullptr, n, js, stp, tol, cnt, s);
+                                                 CPLX ? W32 + nn : nullptr, n, js, stp, tol, cnt, s, &mu);
       if (hc < 0)
         return VJ_ERR_CUDA;
       if (!hc)
         break;
+      if (mu < 4.f * tol) {
+        ++sw;
+        break;
+      }
     }
     total32 += sw;
     if (trace) {
@@ -588,14 +601,22 @@ static vj_fint mixed_dev(vj_fnat m_, vj_fnat n_, double *G, vj_fnat ldG, double 
     const double tol64 = 0.5 * std::sqrt((double)m) * 1.1102230246251565e-16;
     const unsigned maxsw64 = swp < 20u ? swp : 20u;
     unsigned sw64 = 0;
+    // A sweep whose rotated pairs all had |cos| <= 1e-11 leaves off-diagonal terms of the
+    // order of their squares (times n / relative gap), far below the tolerance: its
+    // confirming sweep is skipped, the reference's sweep below confirms.
     for (; sw64 < maxsw64; ++sw64) {
+      float mu = 0.f;
       const long long hc = presweep<double, CPLX>(mi, ni, G, (long long)ldG, Gi, (long long)(CPLX ? ldGi : ldG), V,
                                                   (long long)ldV, Vi, (long long)(CPLX ? ldVi : ldV), js, stp, tol64,
-                                                  cnt, s);
+                                                  cnt, s, &mu);
       if (hc < 0)
         return VJ_ERR_CUDA;
       if (!hc)
         break;
+      if (mu <= 1e-11f) {
+        ++sw64;
+        break;
+      }
     }
     if (presweeps)
       presweeps[1] = sw64;
