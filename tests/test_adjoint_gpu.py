@@ -105,6 +105,26 @@ def test_fp32_vs_torch_svd(ad):
         assert np.max(np.abs(g[b] - ref[b])) <= 5e-3 * np.max(np.abs(ref[b])), b
 
 
+@pytest.mark.parametrize("dtype_name", ["float64", "float32"])
+def test_gap_broadening(ad, dtype_name):
+    # a repeated singular value: the broadened kernel stays finite and matches the formula
+    import torch
+    dtype = getattr(torch, dtype_name)
+    rng = np.random.default_rng(8)
+    m, n, k = 64, 32, 8
+    U = np.linalg.qr(rng.standard_normal((m, n)))[0][None].astype(dtype_name).astype(np.float64)
+    V = np.linalg.qr(rng.standard_normal((n, n)))[0][None].astype(dtype_name).astype(np.float64)
+    S = np.linspace(5.0, 0.5, n)[None]
+    S[0, 3] = S[0, 2]
+    dS, dU, dV = rng.standard_normal((1, n)), rng.standard_normal((1, m, k)), rng.standard_normal((1, n, k))
+    t = lambda x: torch.tensor(x, dtype=dtype, device="cuda")
+    dA = ad.adjoint(t(U), t(S), t(V), t(dS), t(dU), t(dV), gap=1e-3).double().cpu().numpy()[0]
+    ref = adjoint_np(U[0], S[0], V[0], dS[0], dU[0], dV[0], gap=1e-3)
+    assert np.all(np.isfinite(dA))
+    tol = 1e-12 if dtype_name == "float64" else 2e-4
+    assert np.max(np.abs(dA - ref)) <= tol * np.max(np.abs(ref))
+
+
 def test_adjoint_errors(ad):
     import torch
     from vecjac_gb300 import api

@@ -91,6 +91,37 @@ def test_mixed_large(vj, kind, m, n):
     check_props(A, U, V, sig)
 
 
+@pytest.mark.parametrize("kind,m,n", [("d", 4608, 32), ("z", 4608, 32)])
+def test_mixed_tall(vj, kind, m, n):
+    # more rows than the register-resident presweep kernels hold: the two-pass kernel
+    from vecjac_gb300 import workloads as W
+    A, s = W.svd_matrix(m, n, seed=13, complex_=(kind == "z"))
+    r, r32, U, V, sig = run_mixed(vj, kind, A)
+    assert r >= 0 and r32 > 0
+    assert np.max(np.abs(np.sort(sig)[::-1] - s)) <= 32 * n * EPS * s[0]
+    check_props(A, U, V, sig)
+
+
+@pytest.mark.parametrize("stages", [1, 3])
+def test_mixed_stages(vj, stages):
+    import torch
+    from vecjac_gb300 import workloads as W
+    m, n = 256, 128
+    A, s = W.svd_matrix(m, n, seed=17, lo=-8.0)
+    js, stp = vj.pjs(4, n)
+    G = torch.tensor(np.ascontiguousarray(A.T), dtype=torch.float64, device="cuda")
+    V = torch.empty((n, n), dtype=torch.float64, device="cuda")
+    eS = torch.empty(n, dtype=torch.float64, device="cuda")
+    fS = torch.empty_like(eS)
+    djs = torch.tensor(js.astype(np.int32), device="cuda")
+    r, r32, r64 = vj.vjsvd_mixed_dev("d", m, n, G, m, V, n, eS, fS, djs, stp, stages=stages)
+    torch.cuda.synchronize()
+    assert r >= 0 and r32 > 0 and r64 >= 0
+    sig = fS.cpu().numpy() * np.exp2(eS.cpu().numpy())
+    assert np.max(np.abs(np.sort(sig)[::-1] - s)) <= 32 * n * EPS * s[0]
+    check_props(A, G.cpu().numpy().T, V.cpu().numpy().T, sig)
+
+
 def test_mixed_errors(vj):
     import torch
     z = torch.zeros(64 * 32, dtype=torch.float64, device="cuda")
