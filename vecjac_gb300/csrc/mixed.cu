@@ -334,14 +334,15 @@ static long long presweep(int m, int n, T *Gr, long long ldr, T *Gi, long long l
   const long long cap = 256LL * E;  // rows per register vector slot
   void (*k)(int, int, T *, long long, T *, long long, T *, long long, T *, long long, const unsigned *, int, T,
             unsigned *) = k_presweep<T, CPLX>;
+  // register-resident columns up to 4 vectors per thread and plane in FP32 and 2 in FP64
+  // (measured at 4096x2048: beyond that the FP64 kernel's register use leaves too few
+  // CTAs per SM to keep the FP64 pipe busy, and the two-pass kernel is 20% faster)
   if (al && m <= cap)
     k = k_presweep_reg<T, CPLX, 1>;
   else if (al && m <= 2 * cap)
     k = k_presweep_reg<T, CPLX, 2>;
-  else if (al && m <= 4 * cap)
+  else if (al && sizeof(T) == 4 && m <= 4 * cap)
     k = k_presweep_reg<T, CPLX, 4>;
-  else if (al && sizeof(T) == 8 && m <= 8 * cap)
-    k = k_presweep_reg<T, CPLX, (sizeof(T) == 8 ? 8 : 4)>;
   for (unsigned st = 0; st < stp; ++st)
     if (host::launch_pdl(k, dim3(nb), dim3(256), 0, s, m, n, Gr, ldr, Gi, ldi, Wr, lwr, Wi, lwi, js, (int)st, tol,
                          cnt) != cudaSuccess)
