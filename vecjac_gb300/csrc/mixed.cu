@@ -432,6 +432,83 @@ static bool zgemm(cublasHandle_t h, bool cplx, bool conjA, int m, int n, int k, 
   return ok;
 }
 
+// T(r, c) = T(c, r) for r < c (fill the upper triangle of an n x n matrix from the lower)
+__global__ void k_sym_lower(double *Tm, int n)
+{
+  for (int c = blockIdx.y; c < n; c += gridDim.y)
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < c; r += gridDim.x * blockDim.x)
+      Tm[(size_t)c * n + r] = Tm[(size_t)r * n + c];
+}
+
+// D(r, c) = M(r, c) - M(c, r) (n x n)
+__global__ void k_antisym(const double *M, int n, double *D)
+{
+  for (int c = blockIdx.y; c < n; c += gridDim.y)
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x)
+      D[(size_t)c * n + r] = M[(size_t)c * n + r] - M[(size_t)r * n + c];
+}
+
+// 3M combination: Cr holds P1 = Ar Br, Ci holds P3 = (Ar + Ai)(Br + Bi), P2 = Ai Bi:
+// Cr = P1 - P2, Ci = P3 - P1 - P2 (rows x cols, leading dimensions ldr / ldi / rows)
+__global__ void k_combine3m(int rows, int cols, double *Cr, long long ldr, double *Ci, long long ldi, const double *P2)
+{
+  for (int c = blockIdx.y; c < cols; c += gridDim.y)
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += gridDim.x * blockDim.x) {
+      const double p1 = Cr[(size_t)c * ldr + r], p2 = P2[(size_t)c * rows + r], p3 = Ci[(size_t)c * ldi + r];
+      Cr[(size_t)c * ldr + r] = p1 - p2;
+      Ci[(size_t)c * ldi + r] = (p3 - p1) - p2;
+    }
+}
+
+// T = X^H X for an n x n split-plane X (leading dimension n): the real part by two
+// symmetric rank-k updates (half a product each), the imaginary part from one product
+// M = Xr^T Xi as M - M^T. tmp: n x n doubles.
+static bool gram(cublasHandle_t h, bool cplx, int n, Planes X, Planes Tm, double *tmp, cudaStream_t s)
+{
+  const double one = 1.0, zero = 0.0;
+  if (cublasDsyrk(h, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_T, n, n, &one, X.re, X.ldr, &zero, Tm.re, n) !=
+      CUBLAS_STATUS_SUCCESS)
+    return false;
+  if (cplx) {
+    if (cublasDsyrk(h, CUBLAS_FILL_MODE_LOWER, CUBLAS_OP_T, n, n, &one, X.im, X.ldi, &one, Tm.re, n) !=
+            CUBLAS_STATUS_SUCCESS ||
+        cublasDgemm(h, CUBLAS_OP_T, CUBLAS_OP_N, n, n, n, &one, X.re, X.ldr, X.im, X.ldi, &zero, tmp, n) !=
+            CUBLAS_STATUS_SUCCESS)
+      return false;
+    k_antisym<<<grid2(n, n), 256, 0, s>>>(tmp, n, Tm.im);
+  }
+  k_sym_lower<<<grid2(n, n), 256, 0, s>>>(Tm.re, n);
+  return cudaGetLastError() == cudaSuccess;
+}
+
+// C = A B for complex split planes with three real products (Gauss / 3M): P1 = Ar Br,
+// P2 = Ai Bi, P3 = (Ar + Ai)(Br + Bi). Used for products of near-unitary n x n matrices
+// (rotation accumulators), where its slightly larger error bound is harmless. tmp: room
+// for m k + k n + m n doubles. Real data: one product.
+static bool zgemm3m(cublasHandle_t h, bool cplx, int m, int n, int k, Planes A, Planes B, Planes Cm, double *tmp,
+                    cudaStream_t s)
+{
+  const double one = 1.0, zero = 0.0;
+  if (!cplx)
+    return cublasDgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, m, n, k, &one, A.re, A.ldr, B.re, B.ldr, &zero, Cm.re, Cm.ldr) ==
+           CUBLAS_STATUS_SUCCESS;
+  double *As = tmp, *Bs = As + (size_t)m * k, *P2 = Bs + (size_t)k * n;
+  bool ok = cublasDgeam(h, CUBLAS_OP_N, CUBLAS_OP_N, m, k, &one, A.re, A.ldr, &one, A.im, A.ldi, As, m) ==
+                CUBLAS_STATUS_SUCCESS &&
+            cublasDgeam(h, CUBLAS_OP_N, CUBLAS_OP_N, k, n, &one, B.re, B.ldr, &one, B.im, B.ldi, Bs, k) ==
+                CUBLAS_STATUS_SUCCESS &&
+            cublasDgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, m, n, k, &one, A.re, A.ldr, B.re, B.ldr, &zero, Cm.re, Cm.ldr) ==
+                CUBLAS_STATUS_SUCCESS &&
+            cublasDgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, m, n, k, &one, A.im, A.ldi, B.im, B.ldi, &zero, P2, m) ==
+                CUBLAS_STATUS_SUCCESS &&
+            cublasDgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, m, n, k, &one, As, m, Bs, k, &zero, Cm.im, Cm.ldi) ==
+                CUBLAS_STATUS_SUCCESS;
+  if (!ok)
+    return false;
+  k_combine3m<<<grid2(m, n), 256, 0, s>>>(m, n, Cm.re, Cm.ldr, Cm.im, Cm.ldi, P2);
+  return cudaGetLastError() == cudaSuccess;
+}
+
 static bool copy2d(double *dst, long long ldd, const double *src, long long lds, long long rows, long long cols,
                    cudaStream_t s)
 {
@@ -468,16 +545,19 @@ static vj_fint mixed_dev(vj_fnat m_, vj_fnat n_, double *G, vj_fnat ldG, double 
     return VJ_ERR_CUDA;
   const int P = CPLX ? 2 : 1;
   const size_t mn = (size_t)m * n, nn = (size_t)n * n;
-  // scratch: G32 (P m n), W32 (P n n) floats; Gp (P m n), X, T, Y (P n n each) doubles; counters
+  // scratch: G32 (P m n), W32 (P n n) floats; Gp, X, T, Y (P n n each) doubles; counters
   const size_t f32b = ((P * (mn + nn) * 4) + 255) & ~(size_t)255;
-  const size_t f64b = P * (mn + 3 * nn) * 8;
+  // Gp: the copy of G for G W (P m n doubles), earlier the temporaries of the 3M products
+  // (3 n n doubles)
+  const size_t gpn = ((size_t)P * mn > 3 * nn) ? (size_t)P * mn : 3 * nn;
+  const size_t f64b = (gpn + P * 3 * nn) * 8;
   host::Staging &stg = host::staging3();
   if (!stg.reserve(f32b + f64b + 256))
     return VJ_ERR_NOMEM;
   float *G32 = reinterpret_cast<float *>(stg.ptr);
   float *W32 = G32 + P * mn;
   double *Gp = reinterpret_cast<double *>(stg.ptr + f32b);
-  double *X = Gp + P * mn;
+  double *X = Gp + gpn;
   double *T = X + P * nn;
   double *Y = T + P * nn;
   unsigned long long *cell = reinterpret_cast<unsigned long long *>(Y + P * nn);
@@ -551,8 +631,10 @@ static vj_fint mixed_dev(vj_fnat m_, vj_fnat n_, double *G, vj_fnat ldG, double 
     for (int pl = 0; pl < P; ++pl)
       k_to_f64<<<(unsigned)((nn + 255) / 256 < 4096 ? (nn + 255) / 256 : 4096), 256, 0, s>>>(
           W32 + pl * nn, (long long)nn, X + pl * nn);
+    // (the Gram product by symmetric rank-k updates, the products of near-unitary
+    // matrices by 3M; the Gp scratch, free until step 4, holds their temporaries)
     for (int it = 0; it < 2; ++it) {
-      if (!zgemm(h, CPLX, true, ni, ni, ni, Xp, Xp, Yp) || !zgemm(h, CPLX, false, ni, ni, ni, Xp, Yp, Tp))
+      if (!gram(h, CPLX, ni, Xp, Yp, Gp, s) || !zgemm3m(h, CPLX, ni, ni, ni, Xp, Yp, Tp, Gp, s))
         return VJ_ERR_CUDA;
       const double a15 = 1.5, am05 = -0.5;
       for (int pl = 0; pl < P; ++pl)
@@ -560,11 +642,7 @@ static vj_fint mixed_dev(vj_fnat m_, vj_fnat n_, double *G, vj_fnat ldG, double 
                         X + pl * nn, ni) != CUBLAS_STATUS_SUCCESS)
           return VJ_ERR_CUDA;
     }
-    // 4. G <- G W, V <- V W (V_0 = I, so the first stage that rotates sets V = W)
-    if (!copy2d(Gp, m, G, ldG, m, n, s) || (CPLX && !copy2d(Gp + mn, m, Gi, ldGi, m, n, s)))
-      return VJ_ERR_CUDA;
-    if (!zgemm(h, CPLX, false, mi, ni, ni, Gpp, Xp, Gpl))
-      return VJ_ERR_CUDA;
+    // 4. V <- V W (V_0 = I, so the first stage that rotates sets V = W), G <- G W
     if (total32 == sw) {
       if (!copy2d(V, ldV, X, n, n, n, s) || (CPLX && !copy2d(Vi, ldVi, X + nn, n, n, n, s)))
         return VJ_ERR_CUDA;
@@ -572,9 +650,13 @@ static vj_fint mixed_dev(vj_fnat m_, vj_fnat n_, double *G, vj_fnat ldG, double 
     else {
       if (!copy2d(T, n, V, ldV, n, n, s) || (CPLX && !copy2d(T + nn, n, Vi, ldVi, n, n, s)))
         return VJ_ERR_CUDA;
-      if (!zgemm(h, CPLX, false, ni, ni, ni, Tp, Xp, Vpl))
+      if (!zgemm3m(h, CPLX, ni, ni, ni, Tp, Xp, Vpl, Gp, s))
         return VJ_ERR_CUDA;
     }
+    if (!copy2d(Gp, m, G, ldG, m, n, s) || (CPLX && !copy2d(Gp + mn, m, Gi, ldGi, m, n, s)))
+      return VJ_ERR_CUDA;
+    if (!zgemm(h, CPLX, false, mi, ni, ni, Gpp, Xp, Gpl))
+      return VJ_ERR_CUDA;
     if (trace) {
       if (cudaStreamSynchronize(s) != cudaSuccess)
         return VJ_ERR_CUDA;
