@@ -118,8 +118,8 @@ template <typename T> __device__ void hestenes(T a, T b, T cr, T ci, T tol, T *r
   rot[4] = sw;
 }
 
-// CTA-wide sums of a, b, cr, ci (256 threads) into thread 0
-template <typename T> __device__ void block_sum4(T &a, T &b, T &cr, T &ci, T (*red)[8])
+// CTA-wide sums of a, b, cr, ci (up to 512 threads) into thread 0
+template <typename T> __device__ void block_sum4(T &a, T &b, T &cr, T &ci, T (*red)[16])
 {
   for (int o = 16; o >= 1; o >>= 1) {
     a += __shfl_xor_sync(0xffffffffu, a, o);
@@ -137,7 +137,7 @@ template <typename T> __device__ void block_sum4(T &a, T &b, T &cr, T &ci, T (*r
   __syncthreads();
   if (threadIdx.x == 0) {
     a = b = cr = ci = 0;
-    for (int j = 0; j < 8; ++j) {
+    for (int j = 0; j < (int)(blockDim.x >> 5); ++j) {
       a += red[0][j];
       b += red[1][j];
       cr += red[2][j];
@@ -196,7 +196,7 @@ __global__ void __launch_bounds__(256) k_presweep(int m, int n, T *Gr, long long
                                                   long long lwr, T *Wi, long long lwi, const unsigned *js, int st,
                                                   T tol, unsigned *cnt)
 {
-  __shared__ T red[4][8];
+  __shared__ T red[4][16];
   __shared__ T rot[5];
   pdl_enter();
   const int k = blockIdx.x;
@@ -232,17 +232,17 @@ __global__ void __launch_bounds__(256) k_presweep(int m, int n, T *Gr, long long
 }
 
 // The same step with the two columns of G held in registers between the dot products and
-// the rotation (one read and one write of G): thread t owns the 16-byte vectors t + 256 r,
-// r < R, of each column, so m <= 256 R E (E = 4 floats or 2 doubles per vector); m % E == 0
-// and 16-byte aligned columns.
-template <typename T, bool CPLX, int R>
-__global__ void __launch_bounds__(256) k_presweep_reg(int m, int n, T *Gr, long long ldr, T *Gi, long long ldi,
+// the rotation (one read and one write of G): thread t of NT owns the 16-byte vectors
+// t + NT r, r < R, of each column, so m <= NT R E (E = 4 floats or 2 doubles per vector);
+// m % E == 0 and 16-byte aligned columns.
+template <typename T, bool CPLX, int R, int NT>
+__global__ void __launch_bounds__(NT) k_presweep_reg(int m, int n, T *Gr, long long ldr, T *Gi, long long ldi,
                                                       T *Wr, long long lwr, T *Wi, long long lwi, const unsigned *js,
                                                       int st, T tol, unsigned *cnt)
 {
   using V = typename vec16<T>::V;
   constexpr int E = vec16<T>::E;
-  __shared__ T red[4][8];
+  __shared__ T red[4][16];
   __shared__ T rot[5];
   pdl_enter();
   const int k = blockIdx.x;
@@ -255,7 +255,7 @@ __global__ void __launch_bounds__(256) k_presweep_reg(int m, int n, T *Gr, long 
   T a = 0, b = 0, cr = 0, ci = 0;
 #pragma unroll
   for (int r = 0; r < R; ++r) {
-    const int i = threadIdx.x + r * 256;
+    const int i = threadIdx.x + r * NT;
     V z;
     T *zz = reinterpret_cast<T *>(&z);
 #pragma unroll
@@ -297,7 +297,7 @@ __global__ void __launch_bounds__(256) k_presweep_reg(int m, int n, T *Gr, long 
   V *dpr = swap ? gqr : gpr, *dqr = swap ? gpr : gqr, *dpi = swap ? gqi : gpi, *dqi = swap ? gpi : gqi;
 #pragma unroll
   for (int r = 0; r < R; ++r) {
-    const int i = threadIdx.x + r * 256;
+    const int i = threadIdx.x + r * NT;
     if (i < mv) {
       T *X = reinterpret_cast<T *>(&xr[r]), *Y = reinterpret_cast<T *>(&yr[r]);
       T *Xi = reinterpret_cast<T *>(&xi[r]), *Yi = reinterpret_cast<T *>(&yi[r]);
@@ -334,17 +334,21 @@ static long long presweep(int m, int n, T *Gr, long long ldr, T *Gi, long long l
   const long long cap = 256LL * E;  // rows per register vector slot
   void (*k)(int, int, T *, long long, T *, long long, T *, long long, T *, long long, const unsigned *, int, T,
             unsigned *) = k_presweep<T, CPLX>;
-  // register-resident columns up to 4 vectors per thread and plane in FP32 and 2 in FP64
-  // (measured at 4096x2048: beyond that the FP64 kernel's register use leaves too few
-  // CTAs per SM to keep the FP64 pipe busy, and the two-pass kernel is 20% faster)
+  int nt = 256;
+  // register-resident columns: up to 2 vectors per thread and plane with 256 threads, then
+  // (FP32) 2 vectors with 512 threads; beyond that the FP64 kernel's register use would
+  // leave too few CTAs per SM to keep the FP64 pipe busy, and the two-pass kernel is
+  // faster (measured at 4096x2048)
   if (al && m <= cap)
-    k = k_presweep_reg<T, CPLX, 1>;
+    k = k_presweep_reg<T, CPLX, 1, 256>;
   else if (al && m <= 2 * cap)
-    k = k_presweep_reg<T, CPLX, 2>;
-  else if (al && sizeof(T) == 4 && m <= 4 * cap)
-    k = k_presweep_reg<T, CPLX, 4>;
+    k = k_presweep_reg<T, CPLX, 2, 256>;
+  else if (al && sizeof(T) == 4 && m <= 4 * cap) {
+    k = k_presweep_reg<T, CPLX, 2, 512>;
+    nt = 512;
+  }
   for (unsigned st = 0; st < stp; ++st)
-    if (host::launch_pdl(k, dim3(nb), dim3(256), 0, s, m, n, Gr, ldr, Gi, ldi, Wr, lwr, Wi, lwi, js, (int)st, tol,
+    if (host::launch_pdl(k, dim3(nb), dim3(nt), 0, s, m, n, Gr, ldr, Gi, ldi, Wr, lwr, Wi, lwi, js, (int)st, tol,
                          cnt) != cudaSuccess)
       return -1;
   unsigned hc[2] = {0u, 0u};
