@@ -610,6 +610,7 @@ static vj_fint mixed_dev(vj_fnat m_, vj_fnat n_, double *G, vj_fnat ldG, double 
     // (a sweep whose rotated pairs were all within 4x the tolerance ends the stage without
     // a confirming sweep: the stage is a preconditioner, the next one finishes the work)
     unsigned sw = 0;
+    const float stop = 4.f * tol;
     for (; sw < maxsw; ++sw) {
       float mu = 0.f;
       const long long hc = presweep<float, CPLX>(mi, ni, G32, m, CPLX ? G32 + mn : nullptr, m, W32, n,
@@ -618,11 +619,13 @@ static vj_fint mixed_dev(vj_fnat m_, vj_fnat n_, double *G, vj_fnat ldG, double 
         return VJ_ERR_CUDA;
       if (!hc)
         break;
-      if (mu < 4.f * tol) {
+      if (mu < stop) {
         ++sw;
         break;
       }
     }
+    if (trace)
+      std::fprintf(stderr, "mixed SVD stage %u: %u FP32 sweeps\n", stage, sw);
     total32 += sw;
     if (trace) {
       const auto t1 = now();
