@@ -122,6 +122,29 @@ def test_mixed_stages(vj, stages):
     check_props(A, G.cpu().numpy().T, V.cpu().numpy().T, sig)
 
 
+def test_mixed_graded_and_rank_deficient(vj, rst):
+    # column-graded (one-sided Jacobi's high relative accuracy must survive the FP32
+    # stages) and rank-deficient (zero columns) matrices: singular values relative to the
+    # oracle's FP64 SVD of the same matrix
+    rng = np.random.default_rng(21)
+    m, n = 256, 128
+    B = rng.standard_normal((m, n))
+    A = B * 10.0 ** (-np.linspace(0, 20, n))
+    Z = rng.standard_normal((m, n))
+    Z[:, [3, 40, 77]] = 0.0
+    js, stp = rst.pjs(4, n)
+    for M in (A, Z):
+        r, r32, U, V, sig = run_mixed(vj, "d", M)
+        assert r >= 0 and r32 > 0
+        ro = rst.vjsvd("d", M, js, stp)
+        so = np.sort(ro[4] * np.exp2(ro[3]))[::-1]
+        sm = np.sort(sig)[::-1]
+        nz = so > 0
+        assert np.array_equal(sm > 0, nz)
+        assert np.max(np.abs(sm[nz] - so[nz]) / so[nz]) <= 1e-12
+        assert np.max(np.abs(V.T @ V - np.eye(n))) <= 32 * n * EPS
+
+
 def test_mixed_errors(vj):
     import torch
     z = torch.zeros(64 * 32, dtype=torch.float64, device="cuda")
