@@ -411,6 +411,53 @@ def reference_arm(args, dist, rank):
 
 
 # ---------------------------------------------------------------- SVD workloads
+# FP64 and FP32 FMA rates measured on this GB300 (operations per clock per SM)
+FP64_FMA_PER_CLK_SM = 1.68
+FP32_FMA_PER_CLK_SM = 116.0
+
+
+def svd_roofline(flops_per_s, fp64, sm_mhz, kernel, sms=152):
+    """Roofline object for the Jacobi SVD workloads: algorithmic FLOP rate (12m + 6n real,
+    36m + 20n complex per pair and sweep) against the FMA pipe's peak at the sampled clock."""
+    per = FP64_FMA_PER_CLK_SM if fp64 else FP32_FMA_PER_CLK_SM
+    peak = 2.0 * per * sms * sm_mhz * 1e6 / 1e12
+    ach = flops_per_s / 1e12
+    return {"bound": "fp64_pipe" if fp64 else "fp32_pipe", "kernel": kernel, "achieved": round(ach, 5),
+            "peak": round(peak, 3), "unit": "TFLOP/s", "frac": round(ach / peak, 4), "traffic": None,
+            "peak_source": "measured FMA rate per SM x %d SMs x sampled clock" % sms,
+            "note": "algorithmic FLOPs; the reference's scaled compensated dot product executes ~9 operations "
+                    "per element and accumulator chain, so the pipe is busier than this fraction"}
+
+
+def cpu_baseline_svd(kind, A, js, stp, sweeps, budget_s=10.0):
+    """The oracle's restatement of the reference's ?vjsvd_ (oracle/vjo.c, one host thread)
+    on the same matrix: a sweep restricted to the first s pivot steps is timed (s chosen to
+    fill about budget_s), and scaled to the full run (stp steps per sweep, sweeps + 1
+    sweeps including the converged one)."""
+    from oracle import oracle as O
+    O.build()
+    R = O.Restatement()
+    cx = kind in "zc"
+
+    def run(s_):
+        t0 = time.perf_counter()
+        if cx:
+            R.vjsvd(kind, A.real, js[:s_], s_, swp=1, Gi=A.imag)
+        else:
+            R.vjsvd(kind, A, js[:s_], s_, swp=1)
+        return time.perf_counter() - t0
+
+    t1 = run(1)
+    s_ = int(max(1, min(stp, budget_s / max(t1, 1e-6))))
+    t = run(s_)
+    per_sweep = t * stp / s_
+    total = per_sweep * (sweeps + 1)
+    return {"value": round(1.0 / total, 6), "unit": "matrices/s", "cores": 1, "kind": "port",
+            "sample": "%svjsvd_ restatement (oracle/vjo.c), one sweep of %d of %d pivot steps on the same matrix "
+                      "(%.1f s), scaled to %d sweeps" % (kind, s_, stp, t, sweeps + 1),
+            "seconds_per_matrix": round(total, 1)}
+
+
 def bench_svd(args, vj, dist, rank, world, kind, m, n):
     import torch
     from vecjac_gb300 import workloads as W
@@ -453,7 +500,7 @@ def bench_svd(args, vj, dist, rank, world, kind, m, n):
     err = float(np.max(np.abs(np.sort(sig)[::-1] - s) / s))
     per_pair = (36 * m + 20 * n) if cx else (12 * m + 6 * n)
     flops = sweeps * (n * (n - 1) / 2) * per_pair
-    return {"metric": "Jacobi SVD matrices/s (%svjsvd_)" % kind, "value": round(world * 1000.0 / ms, 4),
+    out = {"metric": "Jacobi SVD matrices/s (%svjsvd_)" % kind, "value": round(world * 1000.0 / ms, 4),
             "unit": "matrices/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": round(ms, 3), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f64" if kind in "dz" else "f32", "data": "synthetic (Haar factors, log-uniform sigma)",
@@ -462,6 +509,13 @@ def bench_svd(args, vj, dist, rank, world, kind, m, n):
                        "sweeps": int(sweeps), "max_rel_sigma_err_vs_exact": err},
             "flops_per_s": flops / (ms * 1e-3), "clocks": clk.summary(),
             "gpu_launches": int(sweeps + 1) * stp}
+    csum = out["clocks"]
+    out["roofline"] = svd_roofline(out["flops_per_s"], kind in "dz", csum.get("sm_mhz") or 2070.0,
+                                   "k_step<%s,%s>" % ("double" if kind in "dz" else "float",
+                                                      "cplx" if cx else "real"))
+    if rank == 0 and args.cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline_svd(kind, A, js, stp, int(sweeps))
+    return out
 
 
 def bench_mixed(args, vj, dist, rank, world, kind, m, n):
@@ -521,6 +575,7 @@ def bench_mixed(args, vj, dist, rank, world, kind, m, n):
     with Clocks(torch.cuda.current_device()) as clk:
         ms, (sw64, sw32, swf) = timed(mixed, args.steps)
     rot64 = vj.last_trace()["rotations"]
+    phases = vj.last_mixed_phases()
     sig_m, rel_m, nrm_m = sigma_err()
     out = {"metric": "Jacobi SVD matrices/s (%svjsvd mixed FP32->FP64)" % kind,
            "value": round(world * 1000.0 / ms, 5), "unit": "matrices/s", "n_gpus": world, "steps": args.steps,
@@ -532,7 +587,20 @@ def bench_mixed(args, vj, dist, rank, world, kind, m, n):
                       "sweeps_fp32": int(sw32), "sweeps_fp64_plain_dot": int(swf), "sweeps_fp64": int(sw64),
                       "fp64_rotations_per_sweep": rot64,
                       "max_rel_sigma_err_vs_exact": rel_m, "max_sigma_err_over_sigma_max": nrm_m},
+           "phases_ms": {k: round(v, 1) for k, v in phases.items() if k.endswith("_ms")},
            "clocks": clk.summary()}
+    # roofline of the FP32 stage's step kernel: every step reads and writes the columns of
+    # G and of the rotation accumulator W once (FP32, split planes)
+    pk, src = peaks()
+    P = 2 if cx else 1
+    step_bytes = 2.0 * P * 4 * (m * n + n * n)
+    if phases["fp32_ms"] > 0 and phases["fp32_steps"] > 0:
+        ach = step_bytes * phases["fp32_steps"] / (phases["fp32_ms"] * 1e-3) / 1e9
+        out["roofline"] = {"bound": "hbm", "kernel": "k_presweep_reg<float> (FP32 stages)", "achieved": round(ach, 1),
+                           "peak": pk["hbm_gbs"], "unit": "GB/s", "frac": round(ach / pk["hbm_gbs"], 4),
+                           "traffic": None, "peak_source": src,
+                           "note": "algorithmic bytes: G and W columns read and written once per step; the "
+                                   "FP64 phases are FP64-pipe bound (profiles)"}
     if args.plain_steps > 0:
         pms, psw = timed(plain, args.plain_steps)
         sig_p, rel_p, nrm_p = sigma_err()
@@ -540,6 +608,8 @@ def bench_mixed(args, vj, dist, rank, world, kind, m, n):
                         "max_rel_sigma_err_vs_exact": rel_p, "max_sigma_err_over_sigma_max": nrm_p,
                         "max_rel_sigma_diff_mixed_vs_plain": float(np.max(np.abs(sig_m - sig_p) / sig_p))}
         out["speedup_vs_plain"] = round(pms / ms, 3)
+        if rank == 0 and args.cpu_baseline:
+            out["cpu_baseline"] = cpu_baseline_svd(kind, A, js, stp, int(psw))
     return out
 
 
@@ -721,7 +791,7 @@ def bench_batch(args, vj, dist, rank, world, kind):
         torch.cuda.synchronize()
         t += time.perf_counter() - t0
     per_launch = len(mats) * (t / sample)
-    return {"metric": "batched Jacobi SVD matrices/s (%svjsvd_, uneven sizes)" % kind,
+    out = {"metric": "batched Jacobi SVD matrices/s (%svjsvd_, uneven sizes)" % kind,
             "value": round(world * len(mats) / (ms * 1e-3), 2), "unit": "matrices/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 2), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64" if kind == "d" else "f32",
@@ -733,6 +803,45 @@ def bench_batch(args, vj, dist, rank, world, kind):
             "one_launch_per_matrix_s_estimate": round(per_launch, 2),
             "speedup_vs_per_matrix_launches": round(per_launch / (ms * 1e-3), 2),
             "clocks": clk.summary(), "gpu_launches": 2 * args.steps}
+    out["roofline"] = svd_roofline(out["flops_per_s"], kind == "d", out["clocks"].get("sm_mhz") or 2070.0,
+                                   "k_batch<%s>" % ("double" if kind == "d" else "float"))
+    if rank == 0 and args.cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline_batch(mats, kind, args.pivot)
+    return out
+
+
+def cpu_baseline_batch(mats, kind, pivot, budget_s=10.0):
+    """The oracle's restatement of ?vjsvd_ (oracle/vjo.c) on every host thread, one matrix per
+    task, over a random sample of the batch (zero-padded like the GPU batch) sized to fill
+    about budget_s; reported as whole-batch matrices/s."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    from oracle import oracle as O
+    from vecjac_gb300 import batch as B
+    O.build()
+    R = O.Restatement()
+    threads = os.cpu_count()
+    rng = np.random.default_rng(6)
+    order = rng.permutation(len(mats))
+
+    def one(i):
+        A = mats[i]
+        m2, n2 = B.padded_shape(A.shape[0], A.shape[1], kind)
+        P = np.zeros((m2, n2), A.dtype)
+        P[:A.shape[0], :A.shape[1]] = A
+        js, stp = R.pjs(pivot, n2)
+        R.vjsvd(kind, P, js, stp)
+
+    done, t0 = 0, time.perf_counter()
+    with ThreadPoolExecutor(threads) as ex:
+        while time.perf_counter() - t0 < budget_s and done < len(mats):
+            chunk = order[done:done + threads]
+            list(ex.map(one, chunk))
+            done += len(chunk)
+    el = time.perf_counter() - t0
+    return {"value": round(done / el, 2), "unit": "matrices/s", "cores": threads, "kind": "port",
+            "sample": "%d random matrices of the batch through the %svjsvd_ restatement (oracle/vjo.c), one per host "
+                      "thread, %.1f s" % (done, kind, el)}
 
 
 def main():

@@ -135,6 +135,12 @@ vj_fint vj_zvjsvd_mixed_dev(vj_fnat m, vj_fnat n, double *Gr, vj_fnat ldGr, doub
                             vj_fnat ldVr, double *Vi, vj_fnat ldVi, double *eS, double *fS, const unsigned *js,
                             unsigned stp, unsigned swp, unsigned stages, unsigned *presweeps, void *stream);
 
+/* Phase times of the last vj_?vjsvd_mixed_dev call on this process, in milliseconds:
+ * out[0] FP32 sweeps, out[1] Newton-Schulz steps and GEMMs, out[2] plain-dot FP64 sweeps
+ * and the column sort, out[3] the reference's finishing sweeps; out[4] the number of FP32
+ * step launches. */
+vj_fint vj_last_mixed_phases(double out[5]);
+
 /* Adjoint of the thin SVD A = U diag(S) V^T (m >= n, V square), batched over `count`
  * matrices of one shape: given the cotangents dS (n), dU (m x k) and dV (n x k) of S and of
  * the first k columns of U and V, writes dA (m x n) = the cotangent of A. All arrays on the

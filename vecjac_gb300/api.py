@@ -41,7 +41,7 @@ def lib():
                      "svjsvd_", "cvjsvd_", "vj_dvjsvd_dev", "vj_zvjsvd_dev", "vj_svjsvd_dev", "vj_cvjsvd_dev",
                      "vj_pjs_dev", "vj_dvjsvd_mixed_dev", "vj_zvjsvd_mixed_dev",
                      "vj_ssvd_adjoint_batch_dev", "vj_dsvd_adjoint_batch_dev", "vj_dvjsvd_batch_dev",
-                     "vj_svjsvd_batch_dev"):
+                     "vj_svjsvd_batch_dev", "vj_last_mixed_phases"):
             if hasattr(_LIB, name):
                 getattr(_LIB, name).restype = _ll
         if hasattr(_LIB, "pjs"):
@@ -199,6 +199,15 @@ class _Trace(C.Structure):
 
 
 PHASES = ("control", "staging", "dots", "2x2", "rotations", "norms")
+
+
+def last_mixed_phases():
+    """Phase times (ms) of the last mixed-precision SVD: FP32 sweeps, Newton-Schulz + GEMMs,
+    plain FP64 sweeps + sort, the reference's finishing sweeps; and the FP32 step launches."""
+    out = (C.c_double * 5)()
+    lib().vj_last_mixed_phases(out)
+    return {"fp32_ms": out[0], "gemm_ms": out[1], "fp64_plain_ms": out[2], "finish_ms": out[3],
+            "fp32_steps": int(out[4])}
 
 
 def last_trace():

@@ -575,8 +575,9 @@ static vj_fint mixed_dev(vj_fnat m_, vj_fnat n_, double *G, vj_fnat ldG, double 
   const float tol = fmaxf(0.5f * sqrtf((float)m), 8.f) * 5.9604645e-8f;
   const unsigned maxsw = swp < 60u ? swp : 60u;
   unsigned total32 = 0;
-  // with VJ_TRACE=1, the wall-clock time of each phase goes to stderr (every phase ends
-  // with a stream synchronisation, so host time is device time here)
+  // the wall-clock time of each phase is kept for vj_last_mixed_phases (every phase ends
+  // with a stream synchronisation, so host time is device time here); with VJ_TRACE=1 it
+  // also goes to stderr
   const bool trace = host::trace_enabled();
   auto now = [] { return std::chrono::steady_clock::now(); };
   auto t0 = now();
@@ -627,7 +628,7 @@ static vj_fint mixed_dev(vj_fnat m_, vj_fnat n_, double *G, vj_fnat ldG, double 
     if (trace)
       std::fprintf(stderr, "mixed SVD stage %u: %u FP32 sweeps\n", stage, sw);
     total32 += sw;
-    if (trace) {
+    {
       const auto t1 = now();
       ms32 += std::chrono::duration<double, std::milli>(t1 - t0).count();
       t0 = t1;
@@ -664,7 +665,7 @@ static vj_fint mixed_dev(vj_fnat m_, vj_fnat n_, double *G, vj_fnat ldG, double 
       return VJ_ERR_CUDA;
     if (!zgemm(h, CPLX, false, mi, ni, ni, Gpp, Xp, Gpl))
       return VJ_ERR_CUDA;
-    if (trace) {
+    {
       if (cudaStreamSynchronize(s) != cudaSuccess)
         return VJ_ERR_CUDA;
       const auto t1 = now();
@@ -743,17 +744,18 @@ static vj_fint mixed_dev(vj_fnat m_, vj_fnat n_, double *G, vj_fnat ldG, double 
     }
   }
   double ms64 = 0;
-  if (trace) {
+  {
     const auto t1 = now();
     ms64 = std::chrono::duration<double, std::milli>(t1 - t0).count();
     t0 = t1;
   }
   // 6. FP64 finishing sweeps (the reference's algorithm) with V preset
   const vj_fint r = svd_dev_entry<double, CPLX>(m_, n_, G, ldG, Gi, ldGi, V, ldV, Vi, ldVi, eS, fS, js, stp, swp, 1, s);
+  const double msfin = std::chrono::duration<double, std::milli>(now() - t0).count();
+  host::mixed_phases_set(ms32, msgemm, ms64, msfin, (double)total32 * stp);
   if (trace)
     std::fprintf(stderr, "mixed SVD phases (ms): FP32 sweeps %.1f, Newton-Schulz + GEMMs %.1f, plain FP64 sweeps + sort %.1f, "
-                 "finishing %.1f\n", ms32, msgemm, ms64,
-                 std::chrono::duration<double, std::milli>(now() - t0).count());
+                 "finishing %.1f\n", ms32, msgemm, ms64, msfin);
   return r;
 }
 

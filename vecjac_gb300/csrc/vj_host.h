@@ -56,6 +56,9 @@ void trace_sweep(unsigned sweep, unsigned long long rotations);
 bool trace_enabled();
 void trace_phases(const unsigned long long *cycles, int count);
 
+// phase times (ms) of the last mixed-precision SVD and its number of FP32 step launches
+void mixed_phases_set(double fp32, double gemm, double fp64, double fin, double fp32_steps);
+
 // elements per chunk of a host-pointer 2x2 call (a multiple of `lanes`)
 long long bjac2_chunk(long long n, size_t elem, bool cplx, int lanes);
 
