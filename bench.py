@@ -411,6 +411,11 @@ def reference_arm(args, dist, rank):
 
 
 # ---------------------------------------------------------------- SVD workloads
+# DRAM bytes (read + write) of one FP32 presweep step of the complex 4096x2048 mixed SVD
+# (ncu dram__bytes_read.sum + dram__bytes_write.sum; the profile summary
+# mixed_zsvd4096x2048_kernels_full)
+MIXED_F32_STEP_DRAM = 100.695296e6 + 39.812864e6
+
 # FP64 and FP32 FMA rates measured on this GB300 (operations per clock per SM)
 FP64_FMA_PER_CLK_SM = 1.68
 FP32_FMA_PER_CLK_SM = 116.0
@@ -596,11 +601,15 @@ def bench_mixed(args, vj, dist, rank, world, kind, m, n):
     step_bytes = 2.0 * P * 4 * (m * n + n * n)
     if phases["fp32_ms"] > 0 and phases["fp32_steps"] > 0:
         ach = step_bytes * phases["fp32_steps"] / (phases["fp32_ms"] * 1e-3) / 1e9
+        # DRAM bytes of one complex 4096x2048 step (ncu), scaled by the size of G and W
+        traffic = MIXED_F32_STEP_DRAM * (m * n + n * n) / (4096 * 2048 + 2048 * 2048) * (P / 2.0)
         out["roofline"] = {"bound": "hbm", "kernel": "k_presweep_reg<float> (FP32 stages)", "achieved": round(ach, 1),
                            "peak": pk["hbm_gbs"], "unit": "GB/s", "frac": round(ach / pk["hbm_gbs"], 4),
-                           "traffic": None, "peak_source": src,
-                           "note": "algorithmic bytes: G and W columns read and written once per step; the "
-                                   "FP64 phases are FP64-pipe bound (profiles)"}
+                           "traffic": round(traffic), "peak_source": src,
+                           "note": "algorithmic bytes: G and W columns read and written once per step (%d per "
+                                   "step); where the 2 x FP32 copy of G and W fits partly in L2 the DRAM traffic is "
+                                   "lower (traffic, from ncu) and the fraction can exceed 1. The FP64 phases are "
+                                   "FP64-pipe bound." % step_bytes}
     if args.plain_steps > 0:
         pms, psw = timed(plain, args.plain_steps)
         sig_p, rel_p, nrm_p = sigma_err()
