@@ -22,10 +22,40 @@ def _p(t):
     return C.c_void_p(t.data_ptr())
 
 
-def svd_batch_dev(A, strategy=4, swp=999):
-    """SVD of every matrix of A (B, m, n) CUDA tensor (float32 or float64) in one launch.
-    Returns (S (B, n), U (B, m, n), V (B, n, n), sweeps (B,)) unsorted, as the kernel leaves them."""
+_BLOCK = {}
+
+
+def _tuned_block(A, strategy, swp):
+    """CTA size of the batched kernel for this matrix shape and precision: each of 64, 128
+    and 256 threads is timed on up to 512 of the matrices (after one warm-up), the fastest
+    is kept for the process."""
     import torch
+    key = (tuple(A.shape[1:]), A.dtype, strategy)
+    if key not in _BLOCK:
+        sub = A[: min(A.shape[0], 512)]
+        best, best_t = 128, None
+        for blk in (64, 128, 256):
+            svd_batch_dev(sub, strategy, swp, block=blk)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record()
+            svd_batch_dev(sub, strategy, swp, block=blk)
+            e1.record()
+            torch.cuda.synchronize()
+            t = e0.elapsed_time(e1)
+            if best_t is None or t < best_t:
+                best, best_t = blk, t
+        _BLOCK[key] = best
+    return _BLOCK[key]
+
+
+def svd_batch_dev(A, strategy=4, swp=999, block=None):
+    """SVD of every matrix of A (B, m, n) CUDA tensor (float32 or float64) in one launch
+    (block: threads per CTA; None = autotuned per shape). Returns (S (B, n), U (B, m, n),
+    V (B, n, n), sweeps (B,)) unsorted, as the kernel leaves them."""
+    import torch
+    if block is None:
+        block = _tuned_block(A, strategy, swp)
     Bn, m, n = A.shape
     kind = "s" if A.dtype == torch.float32 else "d"
     L = 16 if kind == "s" else 8
@@ -44,7 +74,7 @@ def svd_batch_dev(A, strategy=4, swp=999):
     f = getattr(api.lib(), "vj_%svjsvd_batch_dev" % kind)
     stream = torch.cuda.current_stream().cuda_stream
     r = f(C.c_longlong(Bn), _p(mm), _p(nn), _p(G), _p(offG), _p(V), _p(offV), _p(eS), _p(fS), _p(offS), None,
-          C.c_long(strategy), C.c_uint(swp), _p(info), C.c_int(128), C.c_void_p(stream))
+          C.c_long(strategy), C.c_uint(swp), _p(info), C.c_int(block), C.c_void_p(stream))
     if r != 0:
         raise RuntimeError("batched SVD launch failed: %d" % r)
     S = fS * torch.exp2(eS)
