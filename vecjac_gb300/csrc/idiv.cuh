@@ -5,7 +5,7 @@
 // FP32 pipes are 40-70 times wider. For operands and quotients in the normal range the
 // quotient is formed here by schoolbook long division of the 53-bit significands in three
 // digits of at most 21 bits: each digit is estimated from an FP32 reciprocal, and the
-// exact 64-bit remainder corrects the estimate by at most two steps either way. The
+// exact 64-bit remainder corrects the estimate by one step either way. The
 // result is correct by construction (0 <= remainder < divisor is checked before
 // rounding), not by the accuracy of the estimate; anything else -- zero, subnormal,
 // infinite or NaN operands, a quotient outside the normal range, or an estimate that the
@@ -39,20 +39,16 @@ __device__ __forceinline__ unsigned ldiv_digit(unsigned long long &R, unsigned l
   const float qf = rf * inv * __uint_as_float((unsigned)(127 + S - 42) << 23);
   unsigned q = __float2uint_rz(qf);
   long long r = (long long)((R << S) - (unsigned long long)q * d);
-  // at most two corrections either way
-#pragma unroll
-  for (int k = 0; k < 2; ++k) {
-    if (r < 0) {
-      --q;
-      r += (long long)d;
-    }
+  // one correction either way: the estimate's relative error (FP32 reciprocal, products
+  // and conversions, < 2^-21) is below one unit of a 20-bit digit; anything else is caught
+  // by the range check below and left to the FP64 unit
+  if (r < 0) {
+    --q;
+    r += (long long)d;
   }
-#pragma unroll
-  for (int k = 0; k < 2; ++k) {
-    if (r >= (long long)d) {
-      ++q;
-      r -= (long long)d;
-    }
+  if (r >= (long long)d) {
+    ++q;
+    r -= (long long)d;
   }
   ok = ok && (r >= 0) && (r < (long long)d);
   R = (unsigned long long)r;
