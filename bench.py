@@ -169,9 +169,9 @@ class Batch:
 
 # thread instructions per element of k_bjac2 (ncu smsp__inst_executed.sum x 32 / elements,
 # 2^24 real and 2^23 complex launches; the profile summary k_bjac2_2e24_full)
-BJAC2_INST_PER_ELEM = {"d": 1507.0, "z": 2341.0}
+BJAC2_INST_PER_ELEM = {"d": 1243.0, "z": 1946.0}
 # DRAM bytes (read + write) of one 2^24-element real FP64 launch, from the same capture
-BJAC2_D_DRAM_2E24 = 402.763264e6 + 487.287296e6
+BJAC2_D_DRAM_2E24 = 402.791680e6 + 487.371776e6
 
 
 def issue_bound(kind, sm_mhz, sms=152):
@@ -241,7 +241,7 @@ def bench_bjac2(args, vj, dist, rank, world):
                      "peak_source": pk_src,
                      "traffic": round(BJAC2_D_DRAM_2E24 * dom.n / 2 ** 24),
                      "traffic_source": "ncu dram__bytes_read+write of a 2^24-element launch, scaled to this launch",
-                     "binding": "instruction issue (FP64 pipe 65% and ALU 61% active, ncu)",
+                     "binding": "FP64 pipe (75% active) and instruction issue (49%), ncu",
                      "issue": {"elements_per_s": round(dom.n / (per_ms["d"] * 1e-3), 1),
                                "bound_elements_per_s": round(fb, 1),
                                "frac": round(dom.n / (per_ms["d"] * 1e-3) / fb, 4),
