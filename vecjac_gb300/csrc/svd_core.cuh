@@ -341,17 +341,20 @@ __device__ void pair_dot(long long m, const T *xr, const T *xi, const T *yr, con
 // recurrence, the chains of a lane just run side by side on different sub-partitions,
 // each warp with one instruction stream (no per-thread selects: on GB300 an FP64 result
 // that goes through the integer pipes costs hundreds of cycles). Elements are loaded a
-// block of four ahead of their accumulation, so that L2 latency (columns not staged in
-// shared memory) overlaps the recurrence. Returns the 8-lane halving-tree sums of s and t
-// on lane 8j.
+// block (8 real, 4 complex) ahead of their accumulation, so that L2 latency (columns not
+// staged in shared memory) overlaps the recurrence, and a block of normal values is
+// accumulated by straight-line code whose products the scheduler can interleave with the
+// recurrence. Returns the 8-lane halving-tree sums of s and t on lane 8j.
 template <typename T, bool CPLX, int C>
 __device__ void chain_dot(long long m, const T *xr, const T *xi, const T *yr, const T *yi, T ex, T ey, bool live,
                           int l8, T &S, T &Tt)
 {
   static_assert(sizeof(T) == 8, "the chain-split dot product is the FP64 form");
+  using F = fp<T>;
   constexpr bool DN = (C & 1) != 0, IM = (C & 2) != 0;
   constexpr int NV = CPLX ? 4 : 2;  // values loaded per element
-  constexpr int D = 4;              // elements per block: the next block's loads are in flight
+  constexpr int NT = CPLX ? 2 : 1;  // terms accumulated per element
+  constexpr int D = CPLX ? 4 : 8;   // elements per block: the next block's loads are in flight
                                     // while this block is accumulated (hides L2 latency)
   const int nx = -(int)ex, ny = -(int)ey;
   T s = 0, t = 0;
@@ -365,24 +368,33 @@ __device__ void chain_dot(long long m, const T *xr, const T *xi, const T *yr, co
       }
     }
   };
-  // accumulate element i from its raw values: real part xr yr, xi yi; imaginary part
+  // the term(s) of element i from its scaled values: real part xr yr, xi yi; imaginary part
   // xr yi, xi (-yr) (= (-xi) yr exactly)
-  auto acc = [&](const T (&v)[NV]) {
-    const T xr_ = scale2(v[0], nx), yr_ = scale2(v[1], ny);
-    T a0 = xr_, b0 = yr_;
-    const T p0 = fp<T>::mul_rd(a0, b0);
+  auto terms = [&](T xr_, T yr_, T xi_, T yi_, T (&v)[NT]) {
+    const T a0 = xr_, b0 = (CPLX && IM) ? yi_ : yr_;
+    const T q0 = F::mul_rd(a0, b0);
+    v[0] = DN ? F::fma_(a0, b0, -q0) : q0;
     if (CPLX) {
-      const T xi_ = scale2(v[2], nx), yi_ = scale2(v[3], ny);
-      b0 = IM ? yi_ : yr_;
       const T a1 = xi_, b1 = IM ? -yr_ : yi_;
-      const T q0 = fp<T>::mul_rd(a0, b0);
-      const T q1 = fp<T>::mul_rd(a1, b1);
-      two_sum(s, (DN ? fp<T>::fma_(a0, b0, -q0) : q0) + t, s, t);
-      two_sum(s, (DN ? fp<T>::fma_(a1, b1, -q1) : q1) + t, s, t);
+      const T q1 = F::mul_rd(a1, b1);
+      v[NT - 1] = DN ? F::fma_(a1, b1, -q1) : q1;
     }
-    else
-      two_sum(s, (DN ? fp<T>::fma_(a0, b0, -p0) : p0) + t, s, t);
   };
+  // the general path: scale2 with its special cases, one element at a time
+  auto acc = [&](const T (&w)[NV]) {
+    T v[NT];
+    terms(scale2(w[0], nx), scale2(w[1], ny), CPLX ? scale2(w[2], nx) : (T)0, CPLX ? scale2(w[3], ny) : (T)0, v);
+#pragma unroll
+    for (int k = 0; k < NT; ++k)
+      two_sum(s, v[k] + t, s, t);
+  };
+  // the power-of-two scaling of a normal value to a normal result is an integer add on the
+  // exponent field (scale2's fast path)
+  auto normal_after = [&](T w, int n) {
+    const int be = (int)((F::bits(w) & ~F::SIGN) >> F::MB);
+    return (be > 0) && (be <= F::EMAXB) && (be + n > 0) && (be + n <= F::EMAXB);
+  };
+  auto fscale = [&](T w, int n) { return F::val(F::bits(w) + ((typename F::U)(long long)n << F::MB)); };
   if (live && l8 < m) {
     T cur[D][NV], nxt[D][NV];
 #pragma unroll
@@ -392,10 +404,33 @@ __device__ void chain_dot(long long m, const T *xr, const T *xi, const T *yr, co
 #pragma unroll
       for (int d = 0; d < D; ++d)
         load(i0 + 8LL * (D + d), nxt[d]);
+      // a full block of normal values: straight-line code, so that the products of later
+      // elements fill the latency of the earlier elements' 2Sum recurrence
+      bool fast = (i0 + 8LL * (D - 1) < m);
 #pragma unroll
-      for (int d = 0; d < D; ++d)
-        if (i0 + 8LL * d < m)
-          acc(cur[d]);
+      for (int d = 0; d < D; ++d) {
+        fast = fast && normal_after(cur[d][0], nx) && normal_after(cur[d][1], ny);
+        if (CPLX)
+          fast = fast && normal_after(cur[d][2], nx) && normal_after(cur[d][3], ny);
+      }
+      if (fast) {
+        T v[D][NT];
+#pragma unroll
+        for (int d = 0; d < D; ++d)
+          terms(fscale(cur[d][0], nx), fscale(cur[d][1], ny), CPLX ? fscale(cur[d][2], nx) : (T)0,
+                CPLX ? fscale(cur[d][3], ny) : (T)0, v[d]);
+#pragma unroll
+        for (int d = 0; d < D; ++d)
+#pragma unroll
+          for (int k = 0; k < NT; ++k)
+            two_sum(s, v[d][k] + t, s, t);
+      }
+      else {
+#pragma unroll
+        for (int d = 0; d < D; ++d)
+          if (i0 + 8LL * d < m)
+            acc(cur[d]);
+      }
 #pragma unroll
       for (int d = 0; d < D; ++d)
 #pragma unroll
