@@ -254,37 +254,15 @@ template <int LANES, typename T> __device__ __forceinline__ T hsum(T v)
   return v;
 }
 
-// scaled compensated dot products (src/ddpscl.c / src/zdpscl.c) by warp 0; x = G_q, y = G_p.
-// Only the two (four for complex data) 2Sum accumulations carry a dependency from one
-// element to the next; the loads, the power-of-two scaling and the exact product split
-// (round-down product and its error by an FMA) of element i + LANES are issued before the
-// accumulation of element i, so that their FP64 latency overlaps the accumulator chain.
+// scaled compensated dot products (src/ddpscl.c / src/zdpscl.c) by LANES lanes; x = G_q,
+// y = G_p. Only the two (four for complex data) 2Sum accumulations carry a dependency from
+// one element to the next; the loads, the power-of-two scaling and the exact product split
+// (round-down product and its error by an FMA) of the elements of a block are independent
+// of it, and blocks of normal values run as straight-line code so that their latency
+// overlaps the accumulator chains.
 template <typename T, bool CPLX> struct DotTerms {
   T pd[CPLX ? 4 : 1], dn[CPLX ? 4 : 1];
 };
-
-template <typename T, bool CPLX>
-__device__ __forceinline__ void dot_terms(const T *xr, const T *xi, const T *yr, const T *yi, long long i, int nx,
-                                          int ny, DotTerms<T, CPLX> &d)
-{
-  const T xri = scale2(xr[i], nx);
-  const T yri = scale2(yr[i], ny);
-  if (CPLX) {
-    const T yii = scale2(yi[i], ny);
-    const T xii = scale2(xi[i], nx);
-    // (negations are written as FP negations: the FMA folds them, with the same bits)
-    const T xs[4] = {xri, xii, xri, -xii}, ys[4] = {yri, yii, yii, yri};
-#pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      d.pd[k] = fp<T>::mul_rd(xs[k], ys[k]);
-      d.dn[k] = fp<T>::fma_(xs[k], ys[k], -d.pd[k]);
-    }
-  }
-  else {
-    d.pd[0] = fp<T>::mul_rd(xri, yri);
-    d.dn[0] = fp<T>::fma_(xri, yri, -d.pd[0]);
-  }
-}
 
 // The accumulation uses branch-free 2Sum: on GB300 a value moving from the FP64 unit to
 // the integer pipes (as Fast2Sum's magnitude test would need) costs several hundred
@@ -300,27 +278,98 @@ template <typename T, bool CPLX>
 __device__ void pair_dot(long long m, const T *xr, const T *xi, const T *yr, const T *yi, T ex, T ey, T fx, T fy,
                          bool live, T &zr, T &zi)
 {
+  using F = fp<T>;
   constexpr int L = svdc<T>::LANES;
+  constexpr int NV = CPLX ? 4 : 2;  // values loaded per element
+  constexpr int D = 4;              // elements per block (the next block's loads in flight)
   const int lane = (threadIdx.x & 31) % L;
   const int nx = -(int)ex, ny = -(int)ey;
   T sr = 0, tr = 0, sr_ = 0, tr_ = 0, si = 0, ti = 0, si_ = 0, ti_ = 0;
-  if (live && lane < m) {
-    DotTerms<T, CPLX> cur, nxt;
-    dot_terms<T, CPLX>(xr, xi, yr, yi, lane, nx, ny, cur);
-    for (long long i = lane; i < m; i += L) {
-      // the terms of the next element (of this one again on the last pass, unused), with
-      // no branch so that they interleave with the accumulation below
-      const long long inx = (i + L < m) ? (i + L) : i;
-      dot_terms<T, CPLX>(xr, xi, yr, yi, inx, nx, ny, nxt);
+  auto load = [&](long long i, T (&v)[NV]) {
+    if (i < m) {
+      v[0] = xr[i];
+      v[1] = yr[i];
       if (CPLX) {
-        dot_acc(cur.pd[0], cur.dn[0], sr, tr, sr_, tr_);
-        dot_acc(cur.pd[1], cur.dn[1], sr, tr, sr_, tr_);
-        dot_acc(cur.pd[2], cur.dn[2], si, ti, si_, ti_);
-        dot_acc(cur.pd[3], cur.dn[3], si, ti, si_, ti_);
+        v[2] = xi[i];
+        v[3] = yi[i];
       }
-      else
-        dot_acc(cur.pd[0], cur.dn[0], sr, tr, sr_, tr_);
-      cur = nxt;
+    }
+  };
+  // products of one element from its scaled values; (negations are written as FP
+  // negations: the FMA folds them, with the same bits)
+  auto products = [&](T xri, T yri, T xii, T yii, DotTerms<T, CPLX> &d) {
+    if (CPLX) {
+      const T xs[4] = {xri, xii, xri, -xii}, ys[4] = {yri, yii, yii, yri};
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        d.pd[k] = F::mul_rd(xs[k], ys[k]);
+        d.dn[k] = F::fma_(xs[k], ys[k], -d.pd[k]);
+      }
+    }
+    else {
+      d.pd[0] = F::mul_rd(xri, yri);
+      d.dn[0] = F::fma_(xri, yri, -d.pd[0]);
+    }
+  };
+  auto accumulate = [&](const DotTerms<T, CPLX> &c) {
+    if (CPLX) {
+      dot_acc(c.pd[0], c.dn[0], sr, tr, sr_, tr_);
+      dot_acc(c.pd[1], c.dn[1], sr, tr, sr_, tr_);
+      dot_acc(c.pd[2], c.dn[2], si, ti, si_, ti_);
+      dot_acc(c.pd[3], c.dn[3], si, ti, si_, ti_);
+    }
+    else
+      dot_acc(c.pd[0], c.dn[0], sr, tr, sr_, tr_);
+  };
+  auto normal_after = [&](T w, int n) {
+    const int be = (int)((F::bits(w) & ~F::SIGN) >> F::MB);
+    return (be > 0) && (be <= F::EMAXB) && (be + n > 0) && (be + n <= F::EMAXB);
+  };
+  auto fscale = [&](T w, int n) { return F::val(F::bits(w) + ((typename F::U)(long long)n << F::MB)); };
+  if (live && lane < m) {
+    T cur[D][NV], nxt[D][NV];
+#pragma unroll
+    for (int d = 0; d < D; ++d)
+      load(lane + (long long)L * d, cur[d]);
+    for (long long i0 = lane; i0 < m; i0 += (long long)L * D) {
+#pragma unroll
+      for (int d = 0; d < D; ++d)
+        load(i0 + (long long)L * (D + d), nxt[d]);
+      // a full block of values that scale to normal values: straight-line code (the
+      // exponent add of scale2's fast path), so that the products of later elements can
+      // fill the latency of the earlier elements' 2Sum recurrences
+      bool fast = (i0 + (long long)L * (D - 1) < m);
+#pragma unroll
+      for (int d = 0; d < D; ++d) {
+        fast = fast && normal_after(cur[d][0], nx) && normal_after(cur[d][1], ny);
+        if (CPLX)
+          fast = fast && normal_after(cur[d][2], nx) && normal_after(cur[d][3], ny);
+      }
+      if (fast) {
+        DotTerms<T, CPLX> tm[D];
+#pragma unroll
+        for (int d = 0; d < D; ++d)
+          products(fscale(cur[d][0], nx), fscale(cur[d][1], ny), CPLX ? fscale(cur[d][2], nx) : (T)0,
+                   CPLX ? fscale(cur[d][3], ny) : (T)0, tm[d]);
+#pragma unroll
+        for (int d = 0; d < D; ++d)
+          accumulate(tm[d]);
+      }
+      else {
+#pragma unroll
+        for (int d = 0; d < D; ++d)
+          if (i0 + (long long)L * d < m) {
+            DotTerms<T, CPLX> tm;
+            products(scale2(cur[d][0], nx), scale2(cur[d][1], ny), CPLX ? scale2(cur[d][2], nx) : (T)0,
+                     CPLX ? scale2(cur[d][3], ny) : (T)0, tm);
+            accumulate(tm);
+          }
+      }
+#pragma unroll
+      for (int d = 0; d < D; ++d)
+#pragma unroll
+        for (int k = 0; k < NV; ++k)
+          cur[d][k] = nxt[d][k];
     }
   }
   const T nur = hsum<L>(sr) + (hsum<L>(tr) + (hsum<L>(sr_) + hsum<L>(tr_)));
@@ -328,8 +377,8 @@ __device__ void pair_dot(long long m, const T *xr, const T *xi, const T *yr, con
   if (CPLX)
     nui = hsum<L>(si) + (hsum<L>(ti) + (hsum<L>(si_) + hsum<L>(ti_)));
   const T de = fx * fy;
-  zr = fp<T>::div(nur, de);
-  zi = CPLX ? fp<T>::div(nui, de) : (T)0;
+  zr = F::div(nur, de);
+  zi = CPLX ? F::div(nui, de) : (T)0;
 }
 
 // The same scaled compensated dot products (FP64 only) with the independent accumulator
