@@ -58,5 +58,60 @@ def build(verbose=False, extra=()):
     return LIB
 
 
+CLI_KINDS = "dzsc"
+
+
+def cli_path(kind):
+    """The command-line SVD driver t<kind>vjsvd.exe (kind in 'dzsc')."""
+    return os.path.join(OUT, "t%svjsvd.exe" % kind)
+
+
+def _cuda_libdir():
+    import shutil
+    nv = nvcc()
+    nv = nv if os.path.isabs(nv) else (shutil.which(nv) or "/usr/local/cuda/bin/nvcc")
+    return os.path.join(os.path.dirname(os.path.dirname(os.path.realpath(nv))), "lib64")
+
+
+def build_cli(verbose=False, lib=None, out_dir=None, extra_sources=(), link_lib=True):
+    """Compile csrc/tvjsvd.cpp once per precision into t?vjsvd.exe next to the library
+    (host C++ only, linked against libvecjac_gb300.so with an rpath to it and to the CUDA
+    runtime). Tests build the same source against a stub through extra_sources/link_lib."""
+    import shutil
+    src = os.path.join(CSRC, "tvjsvd.cpp")
+    hdr = os.path.join(os.path.dirname(HERE), "include", "vecjac_gb300.h")
+    out_dir = out_dir or OUT
+    os.makedirs(out_dir, exist_ok=True)
+    cxx = shutil.which("g++") or shutil.which("c++")
+    base = [cxx] if cxx else [nvcc(), "-x", "c++"]
+    # linker options: -Wl for a C++ driver, -Xlinker for nvcc
+    lk = (lambda o: ["-Wl," + o]) if cxx else (lambda o: ["-Xlinker", o])
+    deps = [src, hdr, __file__] + list(extra_sources) + ([lib or LIB] if link_lib else [])
+
+    def one(kind):
+        exe = os.path.join(out_dir, "t%svjsvd.exe" % kind)
+        if os.path.exists(exe) and os.path.getmtime(exe) >= max(os.path.getmtime(d) for d in deps):
+            return exe
+        cmd = base + ["-O2", "-std=c++17", "-DVJ_CLI_KIND='%s'" % kind, "-I" + os.path.dirname(hdr), src]
+        cmd += list(extra_sources)
+        if link_lib:
+            ld = os.path.dirname(lib or LIB)
+            here = "$ORIGIN" if os.path.realpath(ld) == os.path.realpath(out_dir) else ld
+            cmd += ["-L" + ld, "-lvecjac_gb300"] + lk("--disable-new-dtags") + lk("-rpath=" + here) + \
+                lk("-rpath=" + _cuda_libdir())
+        cmd += ["-o", exe]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError("compiling the command-line driver failed:\n%s\n%s" % (" ".join(cmd), r.stderr))
+        return exe
+
+    with cf.ThreadPoolExecutor(max_workers=len(CLI_KINDS)) as ex:
+        exes = list(ex.map(one, CLI_KINDS))
+    if verbose:
+        print("built", " ".join(os.path.basename(e) for e in exes))
+    return exes
+
+
 if __name__ == "__main__":
     build(verbose=True, extra=sys.argv[1:])
+    build_cli(verbose=True)

@@ -1,0 +1,52 @@
+"""The raw matrix files of the command-line drivers (t?vjsvd.exe), as the reference's
+src/mtxio.c reads and writes them: no header, column-major, complex entries interleaved
+(re, im), and singular values in the reference's `wide` type -- IEEE binary128 ("q",
+its default build) or x87 80-bit extended in 16-byte slots ("l", WP=l).
+"""
+import numpy as np
+
+
+def write_matrix(path, A):
+    """Write the (m, n) array A column-major to path (its dtype as it is)."""
+    np.asarray(A).T.tofile(path)  # tofile writes C order: the rows of A^T, i.e. A's columns
+
+
+def read_matrix(path, m, n, dtype):
+    """The (m, n) column-major matrix in path; the file must hold exactly m n entries."""
+    a = np.fromfile(path, dtype=dtype)
+    if a.size != m * n:
+        raise ValueError("%s holds %d entries, not %d x %d" % (path, a.size, m, n))
+    return a.reshape((n, m)).T
+
+
+def wide_to_float(b, fmt="q"):
+    """Value of one 16-byte `wide` (little-endian) as a Python float; exact when the value
+    fits a double (always so for singular values written from (eS, fS) pairs)."""
+    import math
+    x = int.from_bytes(bytes(b[:16]), "little")
+    if fmt == "q":
+        s, e, f = x >> 127, (x >> 112) & 0x7FFF, x & ((1 << 112) - 1)
+        if e == 0x7FFF:
+            v = math.nan if f else math.inf
+        elif e == 0:
+            v = math.ldexp(float(f), -16382 - 112)
+        else:
+            v = math.ldexp(float((1 << 112) | f), e - 16383 - 112)
+    elif fmt == "l":
+        sig, se = x & ((1 << 64) - 1), (x >> 64) & 0xFFFF
+        s, e = se >> 15, se & 0x7FFF
+        if e == 0x7FFF:
+            v = math.nan if (sig << 1) & ((1 << 64) - 1) else math.inf
+        else:
+            v = math.ldexp(float(sig), max(e, 1) - 16383 - 63)
+    else:
+        raise ValueError("fmt is 'q' or 'l'")
+    return -v if s else v
+
+
+def read_wide(path, n, fmt="q"):
+    """The n singular values of a BaseName.S? file as float64."""
+    raw = np.fromfile(path, dtype=np.uint8)
+    if raw.size != 16 * n:
+        raise ValueError("%s holds %d bytes, not 16 x %d" % (path, raw.size, n))
+    return np.array([wide_to_float(raw[16 * i:16 * i + 16], fmt) for i in range(n)])
