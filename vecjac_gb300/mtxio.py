@@ -50,3 +50,53 @@ def read_wide(path, n, fmt="q"):
     if raw.size != 16 * n:
         raise ValueError("%s holds %d bytes, not 16 x %d" % (path, raw.size, n))
     return np.array([wide_to_float(raw[16 * i:16 * i + 16], fmt) for i in range(n)])
+
+
+def encode_wide(x, fmt="q"):
+    """16 little-endian bytes of the finite value x (a float, int or Fraction) in the wide
+    type, rounded to nearest even: binary128 ("q") or x87 extended ("l", 6 zero padding
+    bytes). Exact for the product of two doubles in binary128."""
+    from fractions import Fraction
+    x = Fraction(x)
+    sign = 1 if x < 0 else 0
+    x = abs(x)
+    P, EMIN = (113, -16382) if fmt == "q" else (64, -16382)
+    if x == 0:
+        sig, e = 0, None
+    else:
+        e = x.numerator.bit_length() - x.denominator.bit_length()
+        if Fraction(2) ** e > x:
+            e -= 1                                  # 2^e <= x < 2^(e+1)
+        e = max(e, EMIN)
+        q = x / Fraction(2) ** (e - P + 1)          # the significand scaled to P bits
+        sig = q.numerator // q.denominator
+        rem = q - sig
+        if rem > Fraction(1, 2) or (rem == Fraction(1, 2) and sig & 1):
+            sig += 1
+        if sig >> P:
+            sig >>= 1
+            e += 1
+        if e > 16383:
+            raise OverflowError("outside the wide type's range")
+    if fmt == "q":
+        if sig == 0:
+            bits = 0
+        elif sig >> (P - 1):
+            bits = ((e + 16383) << 112) | (sig & ((1 << 112) - 1))
+        else:
+            bits = sig                              # subnormal
+        return ((sign << 127) | bits).to_bytes(16, "little")
+    if fmt != "l":
+        raise ValueError("fmt is 'q' or 'l'")
+    if sig == 0:
+        se = 0
+    else:
+        se = (e + 16383) if sig >> (P - 1) else 0
+    return (sig | (((sign << 15) | se) << 64)).to_bytes(16, "little")
+
+
+def write_wide(path, values, fmt="q"):
+    """Write the values (floats or Fractions) as a BaseName.S? file."""
+    with open(path, "wb") as f:
+        for v in values:
+            f.write(encode_wide(v, fmt))
