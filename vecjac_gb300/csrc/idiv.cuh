@@ -5,12 +5,15 @@
 // FP32 pipes are 40-70 times wider. For operands and quotients in the normal range the
 // quotient is formed here by schoolbook long division of the 53-bit significands in three
 // digits of at most 21 bits: each digit is estimated from an FP32 reciprocal, and the
-// exact 64-bit remainder corrects the estimate by one step either way. The
-// result is correct by construction (0 <= remainder < divisor is checked before
-// rounding), not by the accuracy of the estimate; anything else -- zero, subnormal,
-// infinite or NaN operands, a quotient outside the normal range, or an estimate that the
-// bounded correction cannot repair -- is left to the FP64 division. Rounding is to nearest
-// even: up when 2R > d, or 2R == d with an odd quotient.
+// exact 64-bit remainder corrects the estimate by one step either way. The result does
+// not rest on the estimate being within one step: 0 <= remainder < divisor is checked for
+// every digit before rounding, and that check is sound while a digit estimate is off by
+// less than 2^10 (the 64-bit remainder arithmetic then cannot wrap), i.e. for an FP32
+// reciprocal with relative error below 2^-10 -- the estimate here is within about 2^-21,
+// and one step suffices up to 4 ulps of it. Anything else -- zero, subnormal, infinite or
+// NaN operands, a quotient outside the normal range, or an estimate that the bounded
+// correction cannot repair -- is left to the FP64 division. Rounding is to nearest even:
+// up when 2R > d, or 2R == d with an odd quotient.
 #pragma once
 #include "vj_fp.cuh"
 
@@ -22,6 +25,8 @@ __device__ __forceinline__ float rcp_approx(float x)
   float r;
   asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
   return r;
+#elif defined(VJ_IDIV_HOST_RCP)
+  return VJ_IDIV_HOST_RCP(x);  // a host test's model of the approximate reciprocal
 #else
   return 1.0f / x;
 #endif
