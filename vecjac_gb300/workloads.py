@@ -5,7 +5,8 @@ these generators produce the same kinds of inputs from a seed:
 
 * ``pairs2x2``: SoA 2x2 Hermitian batches (a11, a22, a21[, a21i]) with entries
   ``±2^e * u``, ``e`` uniform in [-300, 300] (FP64) or [-40, 40] (FP32), ``u`` uniform in
-  [1, 2) -- the distribution of the 2^28 / 2^27 element batched-EVD workload.
+  [1, 2) -- the distribution of the 2^28 / 2^27 element batched-EVD workload
+  (``pairs2x2_torch``: the same, drawn with torch on a device).
 * ``svd_matrix``: ``A = U diag(sigma) V^H`` with Haar-random orthogonal/unitary factors
   (QR of a Gaussian matrix, columns fixed by the phase of diag(R)) and log-uniform sigma
   sorted descending -- the 1024x1024 real and 4096x2048 complex SVD workloads.
@@ -28,6 +29,25 @@ def pairs2x2(kind, n, seed):
         u = rng.uniform(1.0, 2.0, n)
         s = rng.integers(0, 2, n) * 2.0 - 1.0
         out.append(np.ldexp(s * u, e).astype(dt))
+    return out
+
+
+def pairs2x2_torch(kind, n, seed, device="cuda"):
+    """The pairs2x2 distribution drawn with torch on ``device`` (a seeded torch.Generator
+    there), for batches too large to build on the host: e.g. the 2^28-element FP64 batch
+    of the batched-EVD workload in 6 GB of device memory."""
+    import torch
+    g = torch.Generator(device=device)
+    g.manual_seed(seed)
+    dt = torch.float64 if kind in "dz" else torch.float32
+    lo, hi = (-300, 300) if kind in "dz" else (-40, 40)
+    out = []
+    for _ in range(4 if kind in "zc" else 3):
+        e = torch.randint(lo, hi + 1, (n,), generator=g, device=device, dtype=torch.int32)
+        u = torch.rand(n, generator=g, device=device, dtype=dt) + 1.0
+        sg = torch.randint(0, 2, (n,), generator=g, device=device, dtype=torch.int32).to(dt) * 2 - 1
+        out.append(torch.ldexp(sg * u, e.to(dt)).to(dt))
+        del e, u, sg
     return out
 
 
