@@ -91,6 +91,16 @@ def test_mixed_large(vj, kind, m, n):
     check_props(A, U, V, sig)
 
 
+def test_mixed_full_size(vj):
+    # the benchmark's complex 4096 x 2048 matrix (sigma = 10^U(-8, 0)), same seed
+    from vecjac_gb300 import workloads as W
+    A, s = W.svd_matrix(4096, 2048, seed=2024, lo=-8.0, complex_=True)
+    r, r32, U, V, sig = run_mixed(vj, "z", A)
+    assert r >= 0 and r32 > 0, (r, r32)
+    assert np.max(np.abs(np.sort(sig)[::-1] - s)) <= 32 * 2048 * EPS * s[0]
+    check_props(A, U, V, sig)
+
+
 @pytest.mark.parametrize("kind,m,n", [("d", 4608, 32), ("z", 4608, 32)])
 def test_mixed_tall(vj, kind, m, n):
     # more rows than the register-resident presweep kernels hold: the two-pass kernel
