@@ -105,6 +105,32 @@ def test_fp32_vs_torch_svd(ad):
         assert np.max(np.abs(g[b] - ref[b])) <= 5e-3 * np.max(np.abs(ref[b])), b
 
 
+def test_full_batch(ad):
+    # the differentiable-batch workload itself: 4096 FP32 matrices 128 x 64, k = 16.
+    # Forward: every sigma within 640 n eps_32 of the construction (sigma in [0.1, 10]);
+    # backward: the adjoint kernel on the forward's own U, S, V against the restatement
+    # of the formula, every matrix, 2e-4 relative to max |dA| as above.
+    import torch
+    count, m, n, k = 4096, 128, 64, 16
+    A, Ss = ad.spaced_sigma_matrices(count, m, n, seed=91)
+    rng = np.random.default_rng(92)
+    w, GU, GV = rng.standard_normal((count, n)), rng.standard_normal((count, m, k)), rng.standard_normal((count, n, k))
+    At = torch.tensor(A, dtype=torch.float32, device="cuda")
+    S, U, V, info = ad.svd_batch_dev(At)
+    assert int((info < 0).sum()) == 0
+    S, U, V = ad._sort_and_fix(S, U, V)
+    eps = np.finfo(np.float32).eps
+    assert np.max(np.abs(S.double().cpu().numpy() - Ss)) <= 640 * n * eps
+    t = lambda x: torch.tensor(x, dtype=torch.float32, device="cuda")
+    dA = ad.adjoint(U, S, V, t(w), t(GU), t(GV)).double().cpu().numpy()
+    Un, Sn, Vn = U.double().cpu().numpy(), S.double().cpu().numpy(), V.double().cpu().numpy()
+    worst = 0.0
+    for b in range(count):
+        ref = adjoint_np(Un[b], Sn[b], Vn[b], w[b], GU[b], GV[b])
+        worst = max(worst, np.max(np.abs(dA[b] - ref)) / np.max(np.abs(ref)))
+    assert worst <= 2e-4, worst
+
+
 @pytest.mark.parametrize("dtype_name", ["float64", "float32"])
 def test_gap_broadening(ad, dtype_name):
     # a repeated singular value: the broadened kernel stays finite and matches the formula
