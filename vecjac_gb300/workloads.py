@@ -13,7 +13,8 @@ these generators produce the same kinds of inputs from a seed:
 * ``graded16``: a 16x16 matrix whose entries span the whole exponent range, built by the
   rule of the reference's etc/dgsex.c (columns j < 8: 2^(1023-j-|i-j|); j >= 8:
   2^(-51-j-|i-j|)); it drives the rescaling and shear paths of the SVD.
-* ``uneven_batch``: shapes and matrices of the 20,000-matrix uneven batch.
+* ``uneven_shapes`` / ``uneven_batch``: shapes, matrices and singular values of the
+  20,000-matrix uneven batch.
 """
 import numpy as np
 
@@ -91,3 +92,25 @@ def uneven_shapes(count, seed, mmin=16, mmax=512, nmin=8):
     m = rng.integers(mmin, mmax + 1, count)
     n = np.array([rng.integers(nmin, mm + 1) for mm in m])
     return m, n
+
+
+def uneven_batch(count, seed, kind="d", threads=None):
+    """The uneven-batch workload with its singular values: m ~ U{16..512}, n ~ U{8..m},
+    A = Q1 diag(sigma) Q2^T (Q1, Q2 from QR of Gaussian matrices), sigma = 10^U(-4, 0).
+    Returns (matrices, sigmas sorted descending); the matrices are built on host threads."""
+    import os
+    from concurrent.futures import ThreadPoolExecutor
+    m, n = uneven_shapes(count, seed)
+    seeds = np.random.default_rng(seed + 1).integers(0, 2 ** 63 - 1, count)
+    dt = np.float64 if kind == "d" else np.float32
+
+    def one(i):
+        r = np.random.default_rng(int(seeds[i]))
+        q1, _ = np.linalg.qr(r.standard_normal((int(m[i]), int(n[i]))))
+        q2, _ = np.linalg.qr(r.standard_normal((int(n[i]), int(n[i]))))
+        s = np.sort(10.0 ** r.uniform(-4.0, 0.0, int(n[i])))[::-1]
+        return ((q1 * s) @ q2.T).astype(dt), s
+
+    with ThreadPoolExecutor(threads or os.cpu_count()) as ex:
+        out = list(ex.map(one, range(count)))
+    return [a for a, _ in out], [s for _, s in out]
