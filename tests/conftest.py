@@ -8,3 +8,11 @@ if ROOT not in sys.path:
 
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (sm_103a) and the built library")
+    config.addinivalue_line("markers", "late: full-size and host-environment checks, run after the bit-exact "
+                                       "parity tests of the session")
+
+
+def pytest_collection_modifyitems(session, config, items):
+    # the fast bit-exact parity tests first, the full-size workloads and the checks that
+    # depend on the host (a second GPU process, a bundled LAPACK) after them
+    items.sort(key=lambda it: 1 if it.get_closest_marker("late") else 0)

@@ -105,6 +105,7 @@ def test_fp32_vs_torch_svd(ad):
         assert np.max(np.abs(g[b] - ref[b])) <= 5e-3 * np.max(np.abs(ref[b])), b
 
 
+@pytest.mark.late
 def test_full_batch(ad):
     # the differentiable-batch workload itself: 4096 FP32 matrices 128 x 64, k = 16.
     # Forward: every sigma within 640 n eps_32 of the construction (sigma in [0.1, 10]);

@@ -92,6 +92,7 @@ def test_batch_autotune_and_graph(env):
             assert same(u, v)
 
 
+@pytest.mark.late
 def test_full_size_fp32_batch(env):
     """20,000 FP32 matrices with the uneven workload's shapes (m ~ U{16..512},
     n ~ U{8..m}; Gaussian entries, which build in seconds) in one persistent launch:

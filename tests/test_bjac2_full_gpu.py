@@ -10,7 +10,7 @@ import pytest
 
 from props2x2 import props2x2
 
-pytestmark = pytest.mark.gpu
+pytestmark = [pytest.mark.gpu, pytest.mark.late]
 
 
 @pytest.fixture(scope="module")

@@ -15,7 +15,7 @@ import subprocess
 import numpy as np
 import pytest
 
-pytestmark = pytest.mark.gpu
+pytestmark = [pytest.mark.gpu, pytest.mark.late]
 
 CASES = [("d", 64, 32, 2), ("z", 64, 32, 4), ("s", 64, 32, 2), ("c", 64, 32, 4)]
 

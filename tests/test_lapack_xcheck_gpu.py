@@ -8,7 +8,7 @@ import pytest
 from oracle import lapack as LA
 from test_lapack_xcheck_cpu import check, graded, sigma_of
 
-pytestmark = [pytest.mark.gpu,
+pytestmark = [pytest.mark.gpu, pytest.mark.late,
               pytest.mark.skipif(not LA.available(), reason="no LAPACK with xGESVJ in this numpy/scipy")]
 
 

@@ -91,6 +91,7 @@ def test_mixed_large(vj, kind, m, n):
     check_props(A, U, V, sig)
 
 
+@pytest.mark.late
 def test_mixed_full_size(vj):
     # the benchmark's complex 4096 x 2048 matrix (sigma = 10^U(-8, 0)), same seed
     from vecjac_gb300 import workloads as W

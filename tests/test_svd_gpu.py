@@ -150,6 +150,7 @@ def test_properties_large(vj, kind, m, n):
     assert res <= 16 * n * eps
 
 
+@pytest.mark.late
 def test_full_size_dvjsvd_1024(vj):
     """the benchmark's 1024 x 1024 FP64 matrix (sigma = 10^U(-6, 0), same seed) through the
     host entry: |sigma - sigma_exact| <= 4 n eps sigma_max, ||U^T U - I||_F <= 16 n eps,
