@@ -41,3 +41,73 @@ def test_no_gpu_errors_cleanly(libpath):
     import vecjac_gb300 as vj
     a = np.ones(8)
     assert vj.bjac2("d", -8, a, a, a)[0] == vj.VJ_ERR_NO_GPU
+
+
+def _svd_call(lib, kind, m, n, ldG, ldV, ptr, G=None, V=None, work=None, Gi=None, Vi=None, ldGi=None, ldVi=None):
+    import ctypes as C
+    u = lambda x: C.byref(C.c_ulonglong(x))
+    ctr = C.byref(C.c_uint(1))
+    f = getattr(lib, kind + "vjsvd_")
+    f.restype = C.c_longlong
+    G, V, work = (ptr if x is None else x for x in (G, V, work))
+    if kind in "zc":
+        Gi, Vi = (ptr if x is None else x for x in (Gi, Vi))
+        return f(u(m), u(n), G, u(ldG), Gi, u(ldGi if ldGi is not None else ldG), V, u(ldV), Vi,
+                 u(ldVi if ldVi is not None else ldV), ptr, ptr, ptr, ctr, ctr, work, ptr)
+    return f(u(m), u(n), G, u(ldG), V, u(ldV), ptr, ptr, ptr, ctr, ctr, work, ptr)
+
+
+@pytest.mark.parametrize("kind", "dzsc")
+def test_svd_argument_codes(libpath, kind):
+    """The reference's argument checks and codes, in its order (src/dvjsvd.c:43-67,
+    src/zvjsvd.c:43-80 and the FP32 twins): they all return before the GPU is touched."""
+    import ctypes as C
+    import numpy as np
+    import torch
+    lib = C.CDLL(libpath)
+    buf = np.zeros(1 << 12, np.float64)
+    al = (buf.ctypes.data + 63) & ~63
+    A, B = C.c_void_p(al), C.c_void_p(al + 8)           # 64-byte aligned, misaligned
+    L = 8 if kind in "dz" else 16
+    m, n = 4 * L, 2 * L
+    call = lambda **kw: _svd_call(lib, kind, kw.pop("m", m), kw.pop("n", n), kw.pop("ldG", m), kw.pop("ldV", n), A,
+                                  **kw)
+    assert call(n=0) == 0
+    assert call(m=n - 2, ldG=n) == -1                    # m < n
+    assert call(m=m + 1, ldG=m + L) == -1                # m % L
+    assert call(n=n + 1) == -2                           # odd n
+    assert call(n=2 * L + 2, m=8 * L, ldG=8 * L, ldV=4 * L) == -2    # (n/2) % L
+    assert call(G=B) == -3
+    assert call(ldG=m - L) == -4
+    assert call(ldG=m + 1) == -4
+    if kind in "zc":
+        assert call(Gi=B) == -5
+        assert call(ldGi=m + 1) == -6
+        assert call(V=B) == -7
+        assert call(ldV=n + 1) == -8
+        assert call(Vi=B) == -9
+        assert call(ldVi=n - L) == -10
+        assert call(work=B) == -16
+    else:
+        assert call(V=B) == -5
+        assert call(ldV=n - L) == -6
+        assert call(ldV=n + 1) == -6
+        assert call(work=B) == -12
+    if not torch.cuda.is_available():
+        assert call() == -100001                          # VJ_ERR_NO_GPU: no CPU fallback
+
+
+@pytest.mark.parametrize("kind", "dzsc")
+def test_bjac2_length_code(libpath, kind):
+    """|n| must be a multiple of the vector length (8 FP64, 16 FP32): -1 otherwise."""
+    import ctypes as C
+    import numpy as np
+    lib = C.CDLL(libpath)
+    f = getattr(lib, kind + "bjac2_")
+    f.restype = C.c_longlong
+    L = 8 if kind in "dz" else 16
+    buf = np.zeros(64, np.float64)
+    p = C.c_void_p(buf.ctypes.data)
+    args = [p] * (10 if kind in "zc" else 8)
+    for bad in (L + 2, -(L + 2), L // 2):
+        assert f(C.byref(C.c_longlong(bad)), *args) == -1, bad
