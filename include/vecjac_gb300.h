@@ -17,8 +17,13 @@
 extern "C" {
 #endif
 
-typedef long long vj_fint;           /* fint under MKL_ILP64 (src/common.h:180-183) */
+#ifdef VJ_LP64
+typedef int vj_fint;                 /* fint under the reference's ABI=lp64 (src/common.h:184-186) */
+typedef unsigned vj_fnat;            /* fnat under ABI=lp64 */
+#else
+typedef long long vj_fint;           /* fint under MKL_ILP64, the default (src/common.h:180-183) */
 typedef unsigned long long vj_fnat;  /* fnat under MKL_ILP64 */
+#endif
 
 /* library-specific failures; never produced by the reference */
 #define VJ_ERR_NO_GPU   (-100001LL)
@@ -210,6 +215,9 @@ typedef struct vj_trace {
 } vj_trace;
 vj_fint vj_last_trace(vj_trace *out);
 const char *vj_version(void);
+/* Width in bits of vj_fint / vj_fnat in this build: 64 (ILP64, the default, as the
+ * reference's ABI=ilp64) or 32 (built with -DVJ_LP64, as the reference's ABI=lp64). */
+int vj_abi_int_bits(void);
 
 #ifdef __cplusplus
 }

@@ -43,12 +43,13 @@ def test_no_gpu_errors_cleanly(libpath):
     assert vj.bjac2("d", -8, a, a, a)[0] == vj.VJ_ERR_NO_GPU
 
 
-def _svd_call(lib, kind, m, n, ldG, ldV, ptr, G=None, V=None, work=None, Gi=None, Vi=None, ldGi=None, ldVi=None):
+def _svd_call(lib, kind, m, n, ldG, ldV, ptr, G=None, V=None, work=None, Gi=None, Vi=None, ldGi=None, ldVi=None,
+              lp64=False):
     import ctypes as C
-    u = lambda x: C.byref(C.c_ulonglong(x))
+    u = lambda x: C.byref((C.c_uint if lp64 else C.c_ulonglong)(x))
     ctr = C.byref(C.c_uint(1))
     f = getattr(lib, kind + "vjsvd_")
-    f.restype = C.c_longlong
+    f.restype = C.c_int if lp64 else C.c_longlong
     G, V, work = (ptr if x is None else x for x in (G, V, work))
     if kind in "zc":
         Gi, Vi = (ptr if x is None else x for x in (Gi, Vi))
@@ -57,21 +58,17 @@ def _svd_call(lib, kind, m, n, ldG, ldV, ptr, G=None, V=None, work=None, Gi=None
     return f(u(m), u(n), G, u(ldG), V, u(ldV), ptr, ptr, ptr, ctr, ctr, work, ptr)
 
 
-@pytest.mark.parametrize("kind", "dzsc")
-def test_svd_argument_codes(libpath, kind):
-    """The reference's argument checks and codes, in its order (src/dvjsvd.c:43-67,
-    src/zvjsvd.c:43-80 and the FP32 twins): they all return before the GPU is touched."""
+def _check_svd_codes(lib, kind, lp64=False):
     import ctypes as C
     import numpy as np
     import torch
-    lib = C.CDLL(libpath)
     buf = np.zeros(1 << 12, np.float64)
     al = (buf.ctypes.data + 63) & ~63
     A, B = C.c_void_p(al), C.c_void_p(al + 8)           # 64-byte aligned, misaligned
     L = 8 if kind in "dz" else 16
     m, n = 4 * L, 2 * L
     call = lambda **kw: _svd_call(lib, kind, kw.pop("m", m), kw.pop("n", n), kw.pop("ldG", m), kw.pop("ldV", n), A,
-                                  **kw)
+                                  lp64=lp64, **kw)
     assert call(n=0) == 0
     assert call(m=n - 2, ldG=n) == -1                    # m < n
     assert call(m=m + 1, ldG=m + L) == -1                # m % L
@@ -95,6 +92,38 @@ def test_svd_argument_codes(libpath, kind):
         assert call(work=B) == -12
     if not torch.cuda.is_available():
         assert call() == -100001                          # VJ_ERR_NO_GPU: no CPU fallback
+
+
+@pytest.mark.parametrize("kind", "dzsc")
+def test_svd_argument_codes(libpath, kind):
+    """The reference's argument checks and codes, in its order (src/dvjsvd.c:43-67,
+    src/zvjsvd.c:43-80 and the FP32 twins): they all return before the GPU is touched."""
+    import ctypes as C
+    lib = C.CDLL(libpath)
+    assert lib.vj_abi_int_bits() == 64
+    _check_svd_codes(lib, kind)
+
+
+@pytest.fixture(scope="module")
+def lp64_path(tmp_path_factory):
+    # device code is not run here: ptxas at -O0 keeps this build short
+    from vecjac_gb300 import build
+    return build.build(lp64=True, out_dir=str(tmp_path_factory.mktemp("lp64")), extra=["-Xptxas", "-O0"])
+
+
+def test_lp64_build(lp64_path):
+    """The flavour for callers built with the reference's ABI=lp64 (32-bit fint/fnat): it
+    says so, exports the same symbols, and reads 32-bit arguments."""
+    import ctypes as C
+    lib = C.CDLL(lp64_path)
+    assert lib.vj_abi_int_bits() == 32
+    missing = [n for n in declared() if not hasattr(lib, n)]
+    assert not missing, missing
+    for kind in "dzsc":
+        _check_svd_codes(lib, kind, lp64=True)
+    f = lib.dbjac2_
+    f.restype = C.c_int
+    assert f(C.byref(C.c_int(12)), *([C.c_void_p(8)] * 8)) == -1
 
 
 @pytest.mark.parametrize("kind", "dzsc")

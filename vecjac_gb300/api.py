@@ -35,7 +35,10 @@ def lib():
         path = lib_path()
         if not os.path.exists(path):
             raise RuntimeError("libvecjac_gb300.so is not built: run python -m vecjac_gb300.build")
-        _LIB = C.CDLL(path)
+        lib_ = C.CDLL(path)
+        if lib_.vj_abi_int_bits() != 64:
+            raise RuntimeError("%s is an LP64 build; this module binds the ILP64 (default) build" % path)
+        _LIB = lib_
         for name in ("dbjac2_", "zbjac2_", "sbjac2_", "cbjac2_", "dbjac2i", "zbjac2i", "sbjac2i", "cbjac2i",
                      "vj_dbjac2_dev", "vj_zbjac2_dev", "vj_sbjac2_dev", "vj_cbjac2_dev", "dvjsvd_", "zvjsvd_",
                      "svjsvd_", "cvjsvd_", "vj_dvjsvd_dev", "vj_zvjsvd_dev", "vj_svjsvd_dev", "vj_cvjsvd_dev",

@@ -28,8 +28,8 @@ def nvcc():
     return "nvcc"
 
 
-def _compile(src, extra):
-    obj = os.path.join(OUT, os.path.basename(src) + ".o")
+def _compile(src, extra, out=OUT):
+    obj = os.path.join(out, os.path.basename(src) + ".o")
     if os.path.exists(obj) and os.path.getmtime(obj) >= max(
             os.path.getmtime(p) for p in [src] + glob.glob(os.path.join(CSRC, "*.cuh")) +
             glob.glob(os.path.join(CSRC, "*.h")) + [os.path.join(os.path.dirname(HERE), "include",
@@ -42,20 +42,29 @@ def _compile(src, extra):
     return obj
 
 
-def build(verbose=False, extra=()):
-    os.makedirs(OUT, exist_ok=True)
+LP64_OUT = os.path.join(HERE, "_build_lp64")
+
+
+def build(verbose=False, extra=(), lp64=False, out_dir=None):
+    """Compile and link the library; returns its path. lp64=True builds the flavour with
+    32-bit Fortran integers (-DVJ_LP64, the reference's ABI=lp64) into _build_lp64/ (or
+    out_dir); the default is ILP64 in _build/, the build the Python API binds."""
+    out = out_dir or (LP64_OUT if lp64 else OUT)
+    lib = os.path.join(out, "libvecjac_gb300.so")
+    extra = list(extra) + (["-DVJ_LP64"] if lp64 else [])
+    os.makedirs(out, exist_ok=True)
     srcs = sorted(glob.glob(os.path.join(CSRC, "*.cu")))
     with cf.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
-        objs = list(ex.map(lambda s: _compile(s, list(extra)), srcs))
-    if os.path.exists(LIB) and os.path.getmtime(LIB) >= max(os.path.getmtime(o) for o in objs):
-        return LIB
-    cmd = [nvcc()] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart", "-lcublas"]
+        objs = list(ex.map(lambda s: _compile(s, extra, out), srcs))
+    if os.path.exists(lib) and os.path.getmtime(lib) >= max(os.path.getmtime(o) for o in objs):
+        return lib
+    cmd = [nvcc()] + ARCH + ["-shared", "-o", lib] + objs + ["-lcudart", "-lcublas"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s\n%s" % (" ".join(cmd), r.stderr))
     if verbose:
-        print("built", LIB)
-    return LIB
+        print("built", lib)
+    return lib
 
 
 CLI_KINDS = "dzsc"
@@ -113,5 +122,9 @@ def build_cli(verbose=False, lib=None, out_dir=None, extra_sources=(), link_lib=
 
 
 if __name__ == "__main__":
-    build(verbose=True, extra=sys.argv[1:])
-    build_cli(verbose=True)
+    args = sys.argv[1:]
+    if "--lp64" in args:
+        build(verbose=True, extra=[a for a in args if a != "--lp64"], lp64=True)
+    else:
+        build(verbose=True, extra=args)
+        build_cli(verbose=True)

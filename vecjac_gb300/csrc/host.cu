@@ -172,6 +172,8 @@ extern "C" vj_fint vj_last_trace(vj_trace *out)
   return 0;
 }
 
+extern "C" int vj_abi_int_bits(void) { return (int)(8 * sizeof(vj_fint)); }
+
 extern "C" const char *vj_version(void)
 {
   return "vecjac_gb300 0.1 (sm_103a)";

@@ -652,172 +652,171 @@ __device__ void pair_apply(const PairState<T> &s, long long m, long long nv, T *
 {
   using F = fp<T>;
   const int code = s.code;
-  unsigned long long mq = 0ull, mqi = 0ull;
-  (void)mqi;
-    if (code == 1) {
+  if (code == 1) {
+    // the pair is in order and orthogonal: nothing to apply
+  }
+  else if (code == -1) {
+    #pragma unroll 4
+    for (long long i = ltid; i < m; i += TPP) {
+      const T x = rp[i], y = rq[i];
+      Gp[i] = y; Gq[i] = x;
+      if (CPLX) { const T xi = rpi[i], yi = rqi[i]; Gip[i] = yi; Giq[i] = xi; }
     }
-    else if (code == -1) {
+    #pragma unroll 4
+    for (long long i = ltid; i < nv; i += TPP) {
+      T t = Vp[i]; Vp[i] = Vq[i]; Vq[i] = t;
+      if (CPLX) { t = Vip[i]; Vip[i] = Viq[i]; Viq[i] = t; }
+    }
+  }
+  else if (code == 3 || code == -3) {
+    // Gram-Schmidt-like shear (src/dgsscl.c:5-85, src/zgsscl.c)
+    const T ex = s.ep, ey = s.eq, fx = s.fp, fy = s.fq;
+    const int nx = -(int)ex, ny = -(int)ey;
+    const int px = (int)ex, py = (int)ey;
+    if (code == 3) {
+      const T ff = F::div(fy, fx);
+      const T tfr = -s.a21r * ff;
+      const T tfi = CPLX ? (s.a21i * ff) : (T)0;
       #pragma unroll 4
       for (long long i = ltid; i < m; i += TPP) {
-        const T x = rp[i], y = rq[i];
-        Gp[i] = y; Gq[i] = x;
-        if (CPLX) { const T xi = rpi[i], yi = rqi[i]; Gip[i] = yi; Giq[i] = xi; }
+        if (CPLX) {
+          const T xri_ = scale2(rp[i], nx), xii_ = scale2(rpi[i], nx);
+          const T yri_ = scale2(rq[i], ny), yii_ = scale2(rqi[i], ny);
+          const T xr = F::fma_(tfr, xri_, F::fma_(-tfi, xii_, yri_));
+          const T xi = F::fma_(tfr, xii_, F::fma_(tfi, xri_, yii_));
+          const T ur = scale2(xr, py), ui = scale2(xi, py);
+          Gq[i] = ur; Giq[i] = ui;
+          rq[i] = ur; rqi[i] = ui;
+          amax(mG, ur); amax(mG, ui);
+        }
+        else {
+          const T xi = scale2(rp[i], nx);
+          const T yi = scale2(rq[i], ny);
+          const T u = scale2(F::fma_(tfr, xi, yi), py);
+          Gq[i] = u;
+          rq[i] = u;
+          amax(mG, u);
+        }
+      }
+    }
+    else {
+      const T ff = F::div(fx, fy);
+      const T tfr = -s.a21r * ff;
+      const T tfi = CPLX ? (-s.a21i * ff) : (T)0;
+      #pragma unroll 4
+      for (long long i = ltid; i < m; i += TPP) {
+        if (CPLX) {
+          const T yri = rq[i], yii = rqi[i], xri = rp[i], xii = rpi[i];
+          Gp[i] = yri; Gip[i] = yii;
+          rp[i] = yri; rpi[i] = yii;
+          const T yri_ = scale2(yri, ny), yii_ = scale2(yii, ny);
+          const T xri_ = scale2(xri, nx), xii_ = scale2(xii, nx);
+          const T vr = F::fma_(tfr, yri_, F::fma_(-tfi, yii_, xri_));
+          const T vi = F::fma_(tfr, yii_, F::fma_(tfi, yri_, xii_));
+          const T ur = scale2(vr, px), ui = scale2(vi, px);
+          Gq[i] = ur; Giq[i] = ui;
+          rq[i] = ur; rqi[i] = ui;
+          amax(mG, ur); amax(mG, ui);
+        }
+        else {
+          const T xi = rp[i], yi = rq[i];
+          Gp[i] = yi;
+          rp[i] = yi;
+          const T u = scale2(F::fma_(tfr, scale2(yi, ny), scale2(xi, nx)), px);
+          Gq[i] = u;
+          rq[i] = u;
+          amax(mG, u);
+        }
       }
       #pragma unroll 4
       for (long long i = ltid; i < nv; i += TPP) {
         T t = Vp[i]; Vp[i] = Vq[i]; Vq[i] = t;
         if (CPLX) { t = Vip[i]; Vip[i] = Viq[i]; Viq[i] = t; }
       }
-    }
-    else if (code == 3 || code == -3) {
-      // Gram-Schmidt-like shear (src/dgsscl.c:5-85, src/zgsscl.c)
-      const T ex = s.ep, ey = s.eq, fx = s.fp, fy = s.fq;
-      const int nx = -(int)ex, ny = -(int)ey;
-      const int px = (int)ex, py = (int)ey;
-      if (code == 3) {
-        const T ff = F::div(fy, fx);
-        const T tfr = -s.a21r * ff;
-        const T tfi = CPLX ? (s.a21i * ff) : (T)0;
-        #pragma unroll 4
-        for (long long i = ltid; i < m; i += TPP) {
-          if (CPLX) {
-            const T xri_ = scale2(rp[i], nx), xii_ = scale2(rpi[i], nx);
-            const T yri_ = scale2(rq[i], ny), yii_ = scale2(rqi[i], ny);
-            const T xr = F::fma_(tfr, xri_, F::fma_(-tfi, xii_, yri_));
-            const T xi = F::fma_(tfr, xii_, F::fma_(tfi, xri_, yii_));
-            const T ur = scale2(xr, py), ui = scale2(xi, py);
-            Gq[i] = ur; Giq[i] = ui;
-            rq[i] = ur; rqi[i] = ui;
-            amax(mG, ur); amax(mG, ui);
-          }
-          else {
-            const T xi = scale2(rp[i], nx);
-            const T yi = scale2(rq[i], ny);
-            const T u = scale2(F::fma_(tfr, xi, yi), py);
-            Gq[i] = u;
-            rq[i] = u;
-            amax(mG, u);
-          }
-        }
+      if (ltid == 0) {
+        *eSp = s.eq; *eSq = s.ep;
+        *fSp = s.fq; *fSq = s.fp;
       }
-      else {
-        const T ff = F::div(fx, fy);
-        const T tfr = -s.a21r * ff;
-        const T tfi = CPLX ? (-s.a21i * ff) : (T)0;
+    }
+  }
+  else {
+    // rotation (src/djrot.c, src/djrotf.c, src/zjrot.c, src/zjrotf.c); code -2 permutes
+    const bool perm = (code == -2);
+    const T c = s.c, at = s.cat, sat = s.sat;
+    // the reference marks both columns as changed after any rotation (src/dvjsvd.c:573)
+    const bool real_rot = (!CPLX) || (sat == (T)0);
+    const bool cone = (c == (T)1);
+    if (real_rot && at == (T)0) {
+      // c == 1: identity (or a swap when permuting); c != 1 "never happens" (-4 / -10)
+      if (cone && perm) {
         #pragma unroll 4
         for (long long i = ltid; i < m; i += TPP) {
-          if (CPLX) {
-            const T yri = rq[i], yii = rqi[i], xri = rp[i], xii = rpi[i];
-            Gp[i] = yri; Gip[i] = yii;
-            rp[i] = yri; rpi[i] = yii;
-            const T yri_ = scale2(yri, ny), yii_ = scale2(yii, ny);
-            const T xri_ = scale2(xri, nx), xii_ = scale2(xii, nx);
-            const T vr = F::fma_(tfr, yri_, F::fma_(-tfi, yii_, xri_));
-            const T vi = F::fma_(tfr, yii_, F::fma_(tfi, yri_, xii_));
-            const T ur = scale2(vr, px), ui = scale2(vi, px);
-            Gq[i] = ur; Giq[i] = ui;
-            rq[i] = ur; rqi[i] = ui;
-            amax(mG, ur); amax(mG, ui);
-          }
-          else {
-            const T xi = rp[i], yi = rq[i];
-            Gp[i] = yi;
-            rp[i] = yi;
-            const T u = scale2(F::fma_(tfr, scale2(yi, ny), scale2(xi, nx)), px);
-            Gq[i] = u;
-            rq[i] = u;
-            amax(mG, u);
-          }
+          const T x = rp[i], y = rq[i];
+          Gp[i] = y; Gq[i] = x; rp[i] = y; rq[i] = x;
+          if (CPLX) { const T xi = rpi[i], yi = rqi[i]; Gip[i] = yi; Giq[i] = xi; rpi[i] = yi; rqi[i] = xi; }
         }
         #pragma unroll 4
         for (long long i = ltid; i < nv; i += TPP) {
           T t = Vp[i]; Vp[i] = Vq[i]; Vq[i] = t;
           if (CPLX) { t = Vip[i]; Vip[i] = Viq[i]; Viq[i] = t; }
         }
-        if (ltid == 0) {
-          *eSp = s.eq; *eSq = s.ep;
-          *fSp = s.fq; *fSq = s.fp;
+      }
+    }
+    else if (real_rot) {
+      // the permuted form writes (y - t x) c to x and (x + t y) c to y: the same two
+      // products with the destinations exchanged
+      for (int pl = 0; pl < (CPLX ? 2 : 1); ++pl) {
+        T *X = pl ? Gip : Gp, *Y = pl ? Giq : Gq, *RX = pl ? rpi : rp, *RY = pl ? rqi : rq;
+        T *DX = perm ? Y : X, *DY = perm ? X : Y, *RDX = perm ? RY : RX, *RDY = perm ? RX : RY;
+        #pragma unroll 4
+        for (long long i = ltid; i < m; i += TPP) {
+          const T x = RX[i], y = RY[i];
+          T u = F::fma_(y, at, x);
+          T w = F::fma_(-x, at, y);
+          if (!cone) { u = u * c; w = w * c; }
+          DX[i] = u; DY[i] = w;
+          RDX[i] = u; RDY[i] = w;
+          amax(mG, u); amax(mG, w);
+        }
+        T *XV = pl ? Vip : Vp, *YV = pl ? Viq : Vq;
+        T *DXV = perm ? YV : XV, *DYV = perm ? XV : YV;
+        #pragma unroll 4
+        for (long long i = ltid; i < nv; i += TPP) {
+          const T x = XV[i], y = YV[i];
+          T u = F::fma_(y, at, x);
+          T w = F::fma_(-x, at, y);
+          if (!cone) { u = u * c; w = w * c; }
+          DXV[i] = u; DYV[i] = w;
+          if (TRACKV) { amax(mV, u); amax(mV, w); }
         }
       }
     }
     else {
-      // rotation (src/djrot.c, src/djrotf.c, src/zjrot.c, src/zjrotf.c); code -2 permutes
-      const bool perm = (code == -2);
-      const T c = s.c, at = s.cat, sat = s.sat;
-      // the reference marks both columns as changed after any rotation (src/dvjsvd.c:573)
-      const bool real_rot = (!CPLX) || (sat == (T)0);
-      const bool cone = (c == (T)1);
-      if (real_rot && at == (T)0) {
-        // c == 1: identity (or a swap when permuting); c != 1 "never happens" (-4 / -10)
-        if (cone && perm) {
-          #pragma unroll 4
-          for (long long i = ltid; i < m; i += TPP) {
-            const T x = rp[i], y = rq[i];
-            Gp[i] = y; Gq[i] = x; rp[i] = y; rq[i] = x;
-            if (CPLX) { const T xi = rpi[i], yi = rqi[i]; Gip[i] = yi; Giq[i] = xi; rpi[i] = yi; rqi[i] = xi; }
+      const T cta = at, sta = sat, cna = -at;
+      for (int mat = 0; mat < 2; ++mat) {
+        T *Xr = mat ? Vp : Gp, *Xi = mat ? Vip : Gip, *Yr = mat ? Vq : Gq, *Yi = mat ? Viq : Giq;
+        const T *Rxr = mat ? Vp : rp, *Rxi = mat ? Vip : rpi, *Ryr = mat ? Vq : rq, *Ryi = mat ? Viq : rqi;
+        const long long rows = mat ? nv : m;
+        unsigned long long &mm = mat ? mV : mG;
+        #pragma unroll 4
+        for (long long i = ltid; i < rows; i += TPP) {
+          const T x_r = Rxr[i], x_i = Rxi[i], y_r = Ryr[i], y_i = Ryi[i];
+          T ar = F::fma_(y_r, cta, F::fma_(-y_i, sta, x_r));
+          T ai = F::fma_(y_r, sta, F::fma_(y_i, cta, x_i));
+          T br = F::fma_(x_r, cna, F::fma_(-x_i, sta, y_r));
+          T bi = F::fma_(x_r, sta, F::fma_(x_i, cna, y_i));
+          if (!cone) { ar = ar * c; ai = ai * c; br = br * c; bi = bi * c; }
+          if (perm) { Yr[i] = ar; Yi[i] = ai; Xr[i] = br; Xi[i] = bi; }
+          else { Xr[i] = ar; Xi[i] = ai; Yr[i] = br; Yi[i] = bi; }
+          if (!mat) {
+            if (perm) { rq[i] = ar; rqi[i] = ai; rp[i] = br; rpi[i] = bi; }
+            else { rp[i] = ar; rpi[i] = ai; rq[i] = br; rqi[i] = bi; }
           }
-          #pragma unroll 4
-          for (long long i = ltid; i < nv; i += TPP) {
-            T t = Vp[i]; Vp[i] = Vq[i]; Vq[i] = t;
-            if (CPLX) { t = Vip[i]; Vip[i] = Viq[i]; Viq[i] = t; }
-          }
-        }
-      }
-      else if (real_rot) {
-        // the permuted form writes (y - t x) c to x and (x + t y) c to y: the same two
-        // products with the destinations exchanged
-        for (int pl = 0; pl < (CPLX ? 2 : 1); ++pl) {
-          T *X = pl ? Gip : Gp, *Y = pl ? Giq : Gq, *RX = pl ? rpi : rp, *RY = pl ? rqi : rq;
-          T *DX = perm ? Y : X, *DY = perm ? X : Y, *RDX = perm ? RY : RX, *RDY = perm ? RX : RY;
-          #pragma unroll 4
-          for (long long i = ltid; i < m; i += TPP) {
-            const T x = RX[i], y = RY[i];
-            T u = F::fma_(y, at, x);
-            T w = F::fma_(-x, at, y);
-            if (!cone) { u = u * c; w = w * c; }
-            DX[i] = u; DY[i] = w;
-            RDX[i] = u; RDY[i] = w;
-            amax(mG, u); amax(mG, w);
-          }
-          T *XV = pl ? Vip : Vp, *YV = pl ? Viq : Vq;
-          T *DXV = perm ? YV : XV, *DYV = perm ? XV : YV;
-          #pragma unroll 4
-          for (long long i = ltid; i < nv; i += TPP) {
-            const T x = XV[i], y = YV[i];
-            T u = F::fma_(y, at, x);
-            T w = F::fma_(-x, at, y);
-            if (!cone) { u = u * c; w = w * c; }
-            DXV[i] = u; DYV[i] = w;
-            if (TRACKV) { amax(mV, u); amax(mV, w); }
-          }
-        }
-      }
-      else {
-        const T cta = at, sta = sat, cna = -at;
-        for (int mat = 0; mat < 2; ++mat) {
-          T *Xr = mat ? Vp : Gp, *Xi = mat ? Vip : Gip, *Yr = mat ? Vq : Gq, *Yi = mat ? Viq : Giq;
-          const T *Rxr = mat ? Vp : rp, *Rxi = mat ? Vip : rpi, *Ryr = mat ? Vq : rq, *Ryi = mat ? Viq : rqi;
-          const long long rows = mat ? nv : m;
-          unsigned long long &mm = mat ? mV : mG;
-          #pragma unroll 4
-          for (long long i = ltid; i < rows; i += TPP) {
-            const T x_r = Rxr[i], x_i = Rxi[i], y_r = Ryr[i], y_i = Ryi[i];
-            T ar = F::fma_(y_r, cta, F::fma_(-y_i, sta, x_r));
-            T ai = F::fma_(y_r, sta, F::fma_(y_i, cta, x_i));
-            T br = F::fma_(x_r, cna, F::fma_(-x_i, sta, y_r));
-            T bi = F::fma_(x_r, sta, F::fma_(x_i, cna, y_i));
-            if (!cone) { ar = ar * c; ai = ai * c; br = br * c; bi = bi * c; }
-            if (perm) { Yr[i] = ar; Yi[i] = ai; Xr[i] = br; Xi[i] = bi; }
-            else { Xr[i] = ar; Xi[i] = ai; Yr[i] = br; Yi[i] = bi; }
-            if (!mat) {
-              if (perm) { rq[i] = ar; rqi[i] = ai; rp[i] = br; rpi[i] = bi; }
-              else { rp[i] = ar; rpi[i] = ai; rq[i] = br; rqi[i] = bi; }
-            }
-            if (!mat || TRACKV) { amax(mm, ar); amax(mm, ai); amax(mm, br); amax(mm, bi); }
-          }
+          if (!mat || TRACKV) { amax(mm, ar); amax(mm, ai); amax(mm, br); amax(mm, bi); }
         }
       }
     }
+  }
 }
 
 }  // namespace vj
