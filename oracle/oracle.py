@@ -128,6 +128,13 @@ class Restatement(_Lib):
         self.lib.vjo_pjs.restype = C.POINTER(C.c_uint)
         self.lib.vjo_dnorm.restype = C.c_double
         self.lib.vjo_snorm.restype = C.c_float
+        self.lib.vjo_last_swt.restype = C.c_uint
+
+    def last_swt(self):
+        """Transformed pairs per sweep of the last vjsvd call (first 64 sweeps)."""
+        out = (C.c_ulonglong * 64)()
+        k = self.lib.vjo_last_swt(out, C.c_uint(64))
+        return list(out[:min(k, 64)])
 
     def pjs(self, sid, n):
         stp = C.c_uint(0)

@@ -56,6 +56,19 @@ static inline float vjo_smul_rd(const float x, const float y)
   return r;
 }
 
+/* Transformed pairs per sweep of the last SVD call (the reference's JTRACE "sw swt" lines,
+ * src/dvjsvd.c:596), first 64 sweeps; read with vjo_last_swt. */
+static unsigned long long vjo_trace_swt[64];
+static unsigned vjo_trace_nsw;
+
+unsigned vjo_last_swt(unsigned long long *out, unsigned max)
+{
+  const unsigned k = (vjo_trace_nsw < max) ? vjo_trace_nsw : max;
+  for (unsigned i = 0u; i < k && i < 64u; ++i)
+    out[i] = vjo_trace_swt[i];
+  return vjo_trace_nsw;
+}
+
 /* ---------------- FP64: d / z ---------------- */
 #define R double
 #define LANES 8u

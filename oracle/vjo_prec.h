@@ -672,6 +672,7 @@ long long GSVD(const int cx, const unsigned long long *pm, const unsigned long l
   const R gst = H(scale2)(tol, (int)MAX_FIN_EXP);
   unsigned sw = 0u;
   long long ret = 0;
+  vjo_trace_nsw = 0u;
 
   while (sw < *swp) {
     unsigned long long swt = 0u;
@@ -908,6 +909,9 @@ long long GSVD(const int cx, const unsigned long long *pm, const unsigned long l
       MG = (R)fmax((double)MG, (double)nMG);
       MV = (R)fmax((double)MV, (double)nMV);
     }
+    if (sw < 64u)
+      vjo_trace_swt[sw] = swt;
+    vjo_trace_nsw = sw + 1u;
     if (!swt)
       break;
     ++sw;

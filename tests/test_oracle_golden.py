@@ -100,3 +100,16 @@ def test_bjac2_special_golden(rst, kind, tag, sgn):
     names = ["c", "at", "sat", "l1", "l2", "p"] if kind in "zc" else ["c", "at", "l1", "l2", "p"]
     for name, arr in zip(names, r[1:]):
         assert nan_same(arr, g[f"{tag}_{name}"]), (kind, tag, name)
+
+
+def test_swt_trace(rst):
+    """The restatement's per-sweep count of transformed pairs (the reference's JTRACE
+    "sw swt" lines): one entry per sweep run, all nonzero but the last, which ends the
+    run with nothing to transform."""
+    from vecjac_gb300 import workloads as W
+    A, _ = W.svd_matrix(128, 64, seed=1)
+    js, stp = rst.pjs(4, 64)
+    r = rst.vjsvd("d", A, js, stp)
+    t = rst.last_swt()
+    assert r[0] > 0 and len(t) == r[0] + 1 and t[-1] == 0 and all(x > 0 for x in t[:-1])
+    assert t[0] == stp * 32        # the first sweep transforms every pair of a random matrix

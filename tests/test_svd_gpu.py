@@ -151,6 +151,26 @@ def test_properties_large(vj, kind, m, n):
 
 
 @pytest.mark.late
+@pytest.mark.parametrize("kind,m,n,sid", [("d", 256, 128, 4), ("z", 128, 64, 2), ("s", 256, 128, 4)])
+def test_trace_matches_oracle(vj, rst, kind, m, n, sid):
+    """vj_last_trace (the counterpart of the reference's JTRACE per-sweep log): the GPU's
+    transformed pairs per sweep equal the restatement's, sweep for sweep."""
+    from vecjac_gb300 import api
+    from vecjac_gb300 import workloads as W
+    A, _ = W.svd_matrix(m, n, seed=3 * m + n, complex_=(kind in "zc"))
+    js, stp = rst.pjs(sid, n)
+    kw = dict(Gi=A.imag) if kind in "zc" else {}
+    ro = rst.vjsvd(kind, A.real, js, stp, **kw)
+    to = rst.last_swt()
+    rg = vj.vjsvd(kind, A.real, js, stp, **kw)
+    tg = api.last_trace()
+    assert rg[0] == ro[0] > 0
+    # one entry per sweep run (the last transforms nothing); the first 64 are kept
+    assert tg["sweeps"] == ro[0] + 1 and len(to) == min(ro[0] + 1, 64)
+    assert tg["rotations"] == to
+
+
+@pytest.mark.late
 def test_full_size_dvjsvd_1024(vj):
     """the benchmark's 1024 x 1024 FP64 matrix (sigma = 10^U(-6, 0), same seed) through the
     host entry: |sigma - sigma_exact| <= 4 n eps sigma_max, ||U^T U - I||_F <= 16 n eps,
