@@ -1,0 +1,53 @@
+/* A C11 caller of libvecjac_gb300.so written against include/vecjac_gb300.h the way the
+ * reference's drivers call VecJac (src/tdvjsvd.c: every scalar by pointer, caller-owned
+ * 64-byte aligned buffers). Without a GPU it checks the argument codes the library returns
+ * before touching the device and that a valid call reports VJ_ERR_NO_GPU; it prints
+ * "ok <int bits>" or the first failed check. Built with and without -DVJ_LP64. */
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "vecjac_gb300.h"
+
+#define CHECK(expr, want)                                                             \
+  do {                                                                                \
+    const long long got_ = (long long)(expr);                                         \
+    if (got_ != (long long)(want)) {                                                  \
+      printf("FAIL %s: %lld != %lld\n", #expr, got_, (long long)(want));              \
+      return 1;                                                                       \
+    }                                                                                 \
+  } while (0)
+
+int main(int argc, char **argv)
+{
+  const int gpu = (argc > 1) && !strcmp(argv[1], "gpu");
+  double *G = (double *)aligned_alloc(64, 64 * 32 * sizeof(double));
+  double *V = (double *)aligned_alloc(64, 32 * 32 * sizeof(double));
+  double *w = (double *)aligned_alloc(64, 7 * 32 * sizeof(double));
+  unsigned *iwork = (unsigned *)aligned_alloc(64, 64);
+  unsigned js[32 * 32];
+  if (!G || !V || !w || !iwork)
+    return 2;
+  memset(G, 0, 64 * 32 * sizeof(double));
+  memset(js, 0, sizeof(js));
+  iwork[0] = 0u;
+  vj_fnat m = 64, n = 32, ldG = 64, ldV = 32, bad = 36, odd = 33;
+  unsigned stp = 32, swp = 999;
+  CHECK(vj_abi_int_bits(), 8 * (int)sizeof(vj_fint));
+  CHECK(dvjsvd_(&bad, &n, G, &ldG, V, &ldV, w, w + 32, js, &stp, &swp, w + 64, iwork), -1);
+  CHECK(dvjsvd_(&m, &odd, G, &ldG, V, &ldV, w, w + 32, js, &stp, &swp, w + 64, iwork), -2);
+  CHECK(dvjsvd_(&m, &n, G + 1, &ldG, V, &ldV, w, w + 32, js, &stp, &swp, w + 64, iwork), -3);
+  CHECK(dvjsvd_(&m, &n, G, &bad, V, &ldV, w, w + 32, js, &stp, &swp, w + 64, iwork), -4);
+  CHECK(dvjsvd_(&m, &n, G, &ldG, V + 1, &ldV, w, w + 32, js, &stp, &swp, w + 64, iwork), -5);
+  CHECK(dvjsvd_(&m, &n, G, &ldG, V, &ldV, w, w + 32, js, &stp, &swp, w + 65, iwork), -12);
+  const vj_fint n2 = -12;
+  CHECK(dbjac2_(&n2, w, w, w, w, w, w, w, iwork), -1);
+  if (!gpu)
+    CHECK(dvjsvd_(&m, &n, G, &ldG, V, &ldV, w, w + 32, js, &stp, &swp, w + 64, iwork), VJ_ERR_NO_GPU);
+  printf("ok %d\n", vj_abi_int_bits());
+  free(iwork);
+  free(w);
+  free(V);
+  free(G);
+  return 0;
+}

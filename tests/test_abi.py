@@ -140,3 +140,21 @@ def test_bjac2_length_code(libpath, kind):
     args = [p] * (10 if kind in "zc" else 8)
     for bad in (L + 2, -(L + 2), L // 2):
         assert f(C.byref(C.c_longlong(bad)), *args) == -1, bad
+
+
+@pytest.mark.parametrize("lp64", [False, True])
+def test_c_caller(libpath, lp64_path, tmp_path, lp64):
+    """include/vecjac_gb300.h compiles as C11 and a C caller links and runs against the
+    library (ILP64 and LP64 flavours) with the reference's calling convention."""
+    import subprocess
+    import torch
+    lib = lp64_path if lp64 else libpath
+    exe = str(tmp_path / "c_caller")
+    cmd = ["gcc", "-std=c11", "-Wall", "-Werror", "-I" + os.path.join(ROOT, "include")]
+    cmd += (["-DVJ_LP64"] if lp64 else []) + [os.path.join(ROOT, "tests", "c_caller.c"), "-L" + os.path.dirname(lib),
+                                               "-lvecjac_gb300", "-Wl,-rpath," + os.path.dirname(lib), "-o", exe]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run([exe] + (["gpu"] if torch.cuda.is_available() else []), capture_output=True, text=True,
+                       timeout=120)
+    assert r.returncode == 0 and r.stdout.strip() == "ok %d" % (32 if lp64 else 64), r.stdout + r.stderr
