@@ -13,7 +13,8 @@ d / z / s / c: inputs, outputs and the permutation bitmask), whole job. The inpu
 Other workloads (--workload): "svd1024" (dvjsvd_ on a 1024x1024 FP64 matrix, matrices/s),
 "zsvd" (zvjsvd_ on 4096x2048 FP64 complex), "zsvd_mixed"/"dsvd_mixed" (the same matrix
 through the mixed-precision path, with the plain FP64 arm timed beside it), "batch_d"/
-"batch_s" (20,000 uneven real matrices in one persistent launch).
+"batch_s" (20,000 uneven real matrices in one persistent launch), "diff" (4096 FP32
+matrices 128x64: batched SVD forward and the hand-written adjoint, matrices/s).
 
 Timing follows the harness contract: W untimed warm-up steps, then K steps between CUDA
 events on the launching stream with a barrier and a device synchronize on both sides,
