@@ -53,6 +53,15 @@ def build(verbose=False, extra=(), lp64=False, out_dir=None):
     lib = os.path.join(out, "libvecjac_gb300.so")
     extra = list(extra) + (["-DVJ_LP64"] if lp64 else [])
     os.makedirs(out, exist_ok=True)
+    # objects built with other flags are not reused: a stamp records the flags of a folder
+    stamp, flags = os.path.join(out, "flags"), " ".join([nvcc()] + ARCH + FLAGS + extra)
+    old = open(stamp).read() if os.path.exists(stamp) else None
+    if old != flags:
+        for f in glob.glob(os.path.join(out, "*.o")) + [lib]:
+            if os.path.exists(f):
+                os.remove(f)
+        with open(stamp, "w") as f:
+            f.write(flags)
     srcs = sorted(glob.glob(os.path.join(CSRC, "*.cu")))
     with cf.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
         objs = list(ex.map(lambda s: _compile(s, extra, out), srcs))
