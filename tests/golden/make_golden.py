@@ -7,7 +7,7 @@ project's portable norm (oracle/vjo_nrm2.h), which makes every output reproducib
 for bit by the C restatement and by the GPU library; mode 1 keeps the stock OpenBLAS
 norm and libm hypot, whose singular values are stored for tolerance checks.
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [--new]
 """
 import os
 import sys
@@ -94,11 +94,31 @@ def svd_cases():
     cases.append(("z_32x16_presetV", "z", A.real, A.imag, V0.real, V0.imag, 4, 999))
     A, _ = W.svd_matrix(64, 32, seed=109, complex_=True)
     cases.append(("c_64x32", "c", A.real, A.imag, None, None, 2, 999))
+    # rescaling, shear and rank paths in the other precisions, a sweep cap in FP32, a
+    # preset V in FP32 complex, and a larger FP64 case
+    rng = np.random.default_rng(110)
+    ph = rng.uniform(0, 2 * np.pi, (16, 16))
+    g = W.graded16()
+    cases.append(("z_graded16", "z", g * np.cos(ph), g * np.sin(ph), None, None, 2, 999))
+    cases.append(("s_graded32", "s", W.graded32_f32(), None, None, None, 2, 999))
+    A, _ = W.svd_matrix(16, 16, seed=111, complex_=True)
+    A[:, 9] = 0.0
+    cases.append(("z_16x16_zerocol", "z", A.real, A.imag, None, None, 4, 999))
+    A, _ = W.svd_matrix(32, 32, seed=112, complex_=True)
+    rng = np.random.default_rng(112)
+    V0 = W.haar(32, rng, True) * 0.5
+    cases.append(("c_32x32_presetV", "c", A.real, A.imag, V0.real, V0.imag, 4, 999))
+    A, _ = W.svd_matrix(64, 32, seed=113)
+    cases.append(("s_64x32_swp1", "s", A, None, None, None, 4, 1))
+    A, _ = W.svd_matrix(128, 64, seed=114, lo=-8.0)
+    cases.append(("d_128x64", "d", A, None, None, None, 4, 999))
     return cases
 
 
-def svd_fixtures(ref, rst):
+def svd_fixtures(ref, rst, only_new=False):
     for name, kind, G, Gi, V, Vi, sid, swp in svd_cases():
+        if only_new and os.path.exists(os.path.join(HERE, f"svd_{name}.npz")):
+            continue
         m, n = G.shape
         js, stp = rst.pjs(sid, n)
         kw = dict(js=js, stp=stp, swp=swp, V=V)
@@ -128,9 +148,13 @@ def svd_fixtures(ref, rst):
 
 
 def main():
+    """All fixtures; with --new only the SVD fixtures whose files do not exist yet."""
     O.build(ref=True)
     ref = O.Reference()
     rst = O.Restatement()
+    if "--new" in sys.argv[1:]:
+        svd_fixtures(ref, rst, only_new=True)
+        return
     bjac2_fixtures(ref)
     bjac2_special_fixtures(ref)
     svd_fixtures(ref, rst)

@@ -13,6 +13,7 @@ these generators produce the same kinds of inputs from a seed:
 * ``graded16``: a 16x16 matrix whose entries span the whole exponent range, built by the
   rule of the reference's etc/dgsex.c (columns j < 8: 2^(1023-j-|i-j|); j >= 8:
   2^(-51-j-|i-j|)); it drives the rescaling and shear paths of the SVD.
+  ``graded32_f32`` is the same rule over the FP32 range.
 * ``uneven_shapes`` / ``uneven_batch``: shapes, matrices and singular values of the
   20,000-matrix uneven batch.
 """
@@ -85,6 +86,15 @@ def graded16():
     j = np.arange(16)[None, :]
     e = np.where(j < 8, 1023 - j - np.abs(i - j), -51 - j - np.abs(i - j))
     return np.ldexp(1.0, e)
+
+
+def graded32_f32():
+    """The graded16 rule carried to the FP32 exponent range, 32x32 (the FP32 drivers' shape
+    rules): columns j < 16: 2^(127-j-|i-j|); j >= 16: 2^(-23-j-|i-j|)."""
+    i = np.arange(32)[:, None]
+    j = np.arange(32)[None, :]
+    e = np.where(j < 16, 127 - j - np.abs(i - j), -23 - j - np.abs(i - j))
+    return np.ldexp(1.0, e).astype(np.float32)
 
 
 def uneven_shapes(count, seed, mmin=16, mmax=512, nmin=8):
