@@ -113,3 +113,28 @@ def test_swt_trace(rst):
     t = rst.last_swt()
     assert r[0] > 0 and len(t) == r[0] + 1 and t[-1] == 0 and all(x > 0 for x in t[:-1])
     assert t[0] == stp * 32        # the first sweep transforms every pair of a random matrix
+
+
+@pytest.mark.parametrize("kind,m,n,sid", [("d", 256, 128, 2), ("d", 192, 128, 4), ("s", 256, 128, 2),
+                                          ("z", 128, 64, 2), ("c", 128, 64, 4), ("z", 96, 48, 4)])
+def test_reference_vs_restatement(rst, kind, m, n, sid):
+    """The reference compiled from its own sources (oracle/_ref, x86 with AVX-512 only)
+    against the restatement on the seeded matrices of the GPU parity test
+    (test_svd_gpu.py::test_vs_oracle): bit for bit, sweep counts included, so that the GPU
+    results that equal the restatement there equal the reference's."""
+    import numpy as np
+    from oracle import oracle as O
+    from vecjac_gb300 import workloads as W
+    if not os.path.exists(O.REF_PATH):
+        pytest.skip("the reference is compiled only on an x86 host with AVX-512")
+    ref = O.Reference()
+    ref.mode(0)
+    A, _ = W.svd_matrix(m, n, seed=m + n + ord(kind), complex_=(kind in "zc"))
+    js, stp = rst.pjs(sid, n)
+    kw = dict(Gi=A.imag) if kind in "zc" else {}
+    rr = ref.vjsvd(kind, A.real, js=js, stp=stp, **kw)
+    ro = rst.vjsvd(kind, A.real, js, stp, **kw)
+    assert rr[0] == ro[0] > 0
+    for x, y in zip(rr[1:], ro[1:]):
+        x, y = np.ascontiguousarray(x), np.ascontiguousarray(y)
+        assert np.array_equal(x.view(np.uint8), y.view(np.uint8))
