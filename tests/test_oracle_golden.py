@@ -138,3 +138,30 @@ def test_reference_vs_restatement(rst, kind, m, n, sid):
     for x, y in zip(rr[1:], ro[1:]):
         x, y = np.ascontiguousarray(x), np.ascontiguousarray(y)
         assert np.array_equal(x.view(np.uint8), y.view(np.uint8))
+
+
+@pytest.mark.parametrize("kind", "dszc")
+def test_reference_vs_restatement_bjac2(rst, kind):
+    """The compiled reference against the restatement on the 2^18-element batches of the
+    GPU parity test (test_bjac2_gpu.py::test_vs_oracle, benchmark distribution), in its
+    three forms (sines, tangents, the masked secant variant): bit for bit."""
+    import numpy as np
+    from oracle import oracle as O
+    from vecjac_gb300 import workloads as W
+    if not os.path.exists(O.REF_PATH):
+        pytest.skip("the reference is compiled only on an x86 host with AVX-512")
+    ref = O.Reference()
+    ref.mode(0)
+    n = 1 << 18
+    ins = W.pairs2x2(kind, n, seed=3)
+    a21i = ins[3] if kind in "zc" else None
+    lanes = 8 if kind in "dz" else 16
+    for sgn, internal in ((-1, False), (1, False), (-1, True)):
+        pin = (np.arange(n // lanes, dtype=np.uint32) % 3) * np.uint32(0x10001) if internal else None
+        rr = ref.bjac2(kind, sgn * n, ins[0], ins[1], ins[2], a21i, internal=internal,
+                       p=None if pin is None else pin.copy())
+        ro = rst.bjac2(kind, sgn * n, ins[0], ins[1], ins[2], a21i, internal=internal,
+                       p=None if pin is None else pin.copy())
+        for x, y in zip(rr[1:], ro[1:]):
+            x, y = np.ascontiguousarray(x), np.ascontiguousarray(y)
+            assert np.array_equal(x.view(np.uint8), y.view(np.uint8)), (kind, sgn, internal)
