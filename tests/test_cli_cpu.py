@@ -17,6 +17,7 @@ import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 STUB = os.path.join(ROOT, "tests", "cli_stub.cpp")
+SVD_DRIVER = (("tvjsvd.cpp", "t%svjsvd.exe"),)
 KINDS = {"d": (np.float64, False, 8), "z": (np.float64, True, 8), "s": (np.float32, False, 16),
          "c": (np.float32, True, 16)}
 
@@ -25,7 +26,7 @@ KINDS = {"d": (np.float64, False, 8), "z": (np.float64, True, 8), "s": (np.float
 def stub_exes(tmp_path_factory):
     from vecjac_gb300 import build
     out = str(tmp_path_factory.mktemp("cli"))
-    exes = build.build_cli(out_dir=out, extra_sources=[STUB], link_lib=False)
+    exes = build.build_cli(out_dir=out, extra_sources=[STUB], link_lib=False, programs=SVD_DRIVER)
     return dict(zip(build.CLI_KINDS, exes))
 
 
@@ -195,7 +196,7 @@ def test_real_driver_fails_loudly_without_gpu(tmp_path):
         pytest.skip("a GPU is present")
     from vecjac_gb300 import build
     build.build()
-    exes = build.build_cli()
+    exes = build.build_cli(programs=SVD_DRIVER)
     base, G, m, n = make_input(str(tmp_path), "d")
     r = run(exes[0], 2, m, n, base)
     assert r.returncode != 0

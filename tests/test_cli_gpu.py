@@ -25,7 +25,7 @@ def env():
     import vecjac_gb300
     from vecjac_gb300 import build
     build.build()
-    exes = dict(zip(build.CLI_KINDS, build.build_cli()))
+    exes = dict(zip(build.CLI_KINDS, build.build_cli(programs=(("tvjsvd.cpp", "t%svjsvd.exe"),))))
     try:
         mode = subprocess.run(["nvidia-smi", "--query-gpu=compute_mode", "--format=csv,noheader", "-i", "0"],
                               capture_output=True, text=True, timeout=60).stdout.strip()

@@ -77,11 +77,13 @@ def build(verbose=False, extra=(), lp64=False, out_dir=None):
 
 
 CLI_KINDS = "dzsc"
+# the command-line drivers: source and executable name pattern (kind in 'dzsc')
+CLI_PROGRAMS = (("tvjsvd.cpp", "t%svjsvd.exe"), ("tbjac2.cpp", "t%sbjac2.exe"))
 
 
-def cli_path(kind):
-    """The command-line SVD driver t<kind>vjsvd.exe (kind in 'dzsc')."""
-    return os.path.join(OUT, "t%svjsvd.exe" % kind)
+def cli_path(kind, program="t%svjsvd.exe"):
+    """A command-line driver's path, e.g. t<kind>vjsvd.exe or t<kind>bjac2.exe."""
+    return os.path.join(OUT, program % kind)
 
 
 def _cuda_libdir():
@@ -91,12 +93,14 @@ def _cuda_libdir():
     return os.path.join(os.path.dirname(os.path.dirname(os.path.realpath(nv))), "lib64")
 
 
-def build_cli(verbose=False, lib=None, out_dir=None, extra_sources=(), link_lib=True):
-    """Compile csrc/tvjsvd.cpp once per precision into t?vjsvd.exe next to the library
-    (host C++ only, linked against libvecjac_gb300.so with an rpath to it and to the CUDA
-    runtime). Tests build the same source against a stub through extra_sources/link_lib."""
+def build_cli(verbose=False, lib=None, out_dir=None, extra_sources=(), link_lib=True, programs=CLI_PROGRAMS,
+              extra_flags=()):
+    """Compile each command-line driver (csrc/tvjsvd.cpp: t?vjsvd.exe, csrc/tbjac2.cpp:
+    t?bjac2.exe) once per precision next to the library (host C++ only, linked against
+    libvecjac_gb300.so with an rpath to it and to the CUDA runtime). Returns the
+    executables in the order of `programs` x CLI_KINDS. Tests build the same sources
+    against a stand-in library through extra_sources/extra_flags/link_lib."""
     import shutil
-    src = os.path.join(CSRC, "tvjsvd.cpp")
     hdr = os.path.join(os.path.dirname(HERE), "include", "vecjac_gb300.h")
     out_dir = out_dir or OUT
     os.makedirs(out_dir, exist_ok=True)
@@ -104,14 +108,15 @@ def build_cli(verbose=False, lib=None, out_dir=None, extra_sources=(), link_lib=
     base = [cxx] if cxx else [nvcc(), "-x", "c++"]
     # linker options: -Wl for a C++ driver, -Xlinker for nvcc
     lk = (lambda o: ["-Wl," + o]) if cxx else (lambda o: ["-Xlinker", o])
-    deps = [src, hdr, __file__] + list(extra_sources) + ([lib or LIB] if link_lib else [])
-
-    def one(kind):
-        exe = os.path.join(out_dir, "t%svjsvd.exe" % kind)
+    def one(job):
+        (srcname, pattern), kind = job
+        src = os.path.join(CSRC, srcname)
+        deps = [src, hdr, __file__] + list(extra_sources) + ([lib or LIB] if link_lib else [])
+        exe = os.path.join(out_dir, pattern % kind)
         if os.path.exists(exe) and os.path.getmtime(exe) >= max(os.path.getmtime(d) for d in deps):
             return exe
         cmd = base + ["-O2", "-std=c++17", "-DVJ_CLI_KIND='%s'" % kind, "-I" + os.path.dirname(hdr), src]
-        cmd += list(extra_sources)
+        cmd += list(extra_sources) + list(extra_flags)
         if link_lib:
             ld = os.path.dirname(lib or LIB)
             here = "$ORIGIN" if os.path.realpath(ld) == os.path.realpath(out_dir) else ld
@@ -123,8 +128,9 @@ def build_cli(verbose=False, lib=None, out_dir=None, extra_sources=(), link_lib=
             raise RuntimeError("compiling the command-line driver failed:\n%s\n%s" % (" ".join(cmd), r.stderr))
         return exe
 
-    with cf.ThreadPoolExecutor(max_workers=len(CLI_KINDS)) as ex:
-        exes = list(ex.map(one, CLI_KINDS))
+    jobs = [(prog, kind) for prog in programs for kind in CLI_KINDS]
+    with cf.ThreadPoolExecutor(max_workers=min(8, len(jobs))) as ex:
+        exes = list(ex.map(one, jobs))
     if verbose:
         print("built", " ".join(os.path.basename(e) for e in exes))
     return exes
