@@ -56,10 +56,11 @@ def encode_wide(x, fmt="q"):
     """16 little-endian bytes of the finite value x (a float, int or Fraction) in the wide
     type, rounded to nearest even: binary128 ("q") or x87 extended ("l", 6 zero padding
     bytes). Exact for the product of two doubles in binary128."""
+    import math
     from fractions import Fraction
-    x = Fraction(x)
-    sign = 1 if x < 0 else 0
-    x = abs(x)
+    # the sign of a float zero is kept (a Fraction has none)
+    sign = 1 if (x < 0 or (isinstance(x, float) and math.copysign(1.0, x) < 0)) else 0
+    x = abs(Fraction(x))
     P, EMIN = (113, -16382) if fmt == "q" else (64, -16382)
     if x == 0:
         sig, e = 0, None
