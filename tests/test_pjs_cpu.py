@@ -5,7 +5,6 @@ the oracle's loop-built table and the pair contract holds."""
 import os
 import subprocess
 
-import pytest
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 
