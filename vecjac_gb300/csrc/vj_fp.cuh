@@ -203,7 +203,6 @@ template <typename T> __device__ __forceinline__ T getmant_fin(T x)
 
 template <typename T> __device__ __forceinline__ T getmant(T x)
 {
-  using F = fp<T>;
   if (visnan(x))
     return vquiet(x);
   if (x == (T)0)
