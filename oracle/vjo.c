@@ -92,6 +92,16 @@ unsigned vjo_last_swt(unsigned long long *out, unsigned max)
 #define RSVD vjo_dvjsvd_
 #define CSVD vjo_zvjsvd_
 #include "vjo_prec.h"
+/* the scaled compensated dot products on their own, for the tests of the device code */
+double vjo_ddpscl_x(long long m, const double *x, const double *y, double ex, double ey, double fx, double fy)
+{
+  return vjo_ddpscl(m, x, y, ex, ey, fx, fy);
+}
+void vjo_zdpscl_x(long long m, const double *xr, const double *xi, const double *yr, const double *yi, double ex,
+                  double ey, double fx, double fy, double *zr, double *zi)
+{
+  vjo_dzdpscl(m, xr, xi, yr, yi, ex, ey, fx, fy, zr, zi);
+}
 #undef R
 #undef LANES
 #undef LOWMASK
@@ -137,6 +147,15 @@ unsigned vjo_last_swt(unsigned long long *out, unsigned max)
 #define RSVD vjo_svjsvd_
 #define CSVD vjo_cvjsvd_
 #include "vjo_prec.h"
+float vjo_sdpscl_x(long long m, const float *x, const float *y, float ex, float ey, float fx, float fy)
+{
+  return vjo_sdpscl(m, x, y, ex, ey, fx, fy);
+}
+void vjo_cdpscl_x(long long m, const float *xr, const float *xi, const float *yr, const float *yi, float ex,
+                  float ey, float fx, float fy, float *zr, float *zi)
+{
+  vjo_szdpscl(m, xr, xi, yr, yi, ex, ey, fx, fy, zr, zi);
+}
 
 /* exported column norms (for tests of the norm itself) */
 double vjo_dnorm(const long long m, const double *x) { return vjo_dnrm2(m, x); }

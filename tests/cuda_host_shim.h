@@ -4,9 +4,10 @@
 // built with --fmad=false). Each model is exact: bit casts, IEEE operations that round to
 // nearest (host division, square root and fma are correctly rounded), conversions with
 // the named rounding. The FP64 division counts its calls (the integer-pipe division's
-// fallbacks). The round-down products of the dot products are not modelled (abort).
+// fallbacks). The round-down products of the dot products use the host's rounding modes.
 #pragma once
 #include <algorithm>
+#include <cfenv>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
@@ -27,11 +28,29 @@ static inline int __clz(int u) { return u ? __builtin_clz((unsigned)u) : 32; }
 static inline double __ddiv_rn(double a, double b) { ++g_host_ddiv_calls; return a / b; }
 static inline double __dsqrt_rn(double a) { return std::sqrt(a); }
 static inline double __fma_rn(double a, double b, double c) { return std::fma(a, b, c); }
-static inline double __dmul_rd(double, double) { abort(); }
+// products rounded toward -inf: the host's multiply under a temporary FE_DOWNWARD
+// (the harnesses are built with -frounding-math, so the multiply is not moved or folded)
+static inline double __dmul_rd(double a, double b)
+{
+  const int rm = fegetround();
+  fesetround(FE_DOWNWARD);
+  volatile double x = a, y = b;
+  const double r = x * y;
+  fesetround(rm);
+  return r;
+}
 static inline float __fdiv_rn(float a, float b) { return a / b; }
 static inline float __fsqrt_rn(float a) { return std::sqrt(a); }
 static inline float __fmaf_rn(float a, float b, float c) { return std::fma(a, b, c); }
-static inline float __fmul_rd(float, float) { abort(); }
+static inline float __fmul_rd(float a, float b)
+{
+  const int rm = fegetround();
+  fesetround(FE_DOWNWARD);
+  volatile float x = a, y = b;
+  const float r = x * y;
+  fesetround(rm);
+  return r;
+}
 // unsigned -> float toward zero (keep the top 24 significant bits), to nearest
 static inline float __uint2float_rz(unsigned x)
 {
