@@ -3,8 +3,8 @@
 xGESVJ (Drmac and Veselic's one-sided Jacobi SVD, LAPACK 3.2+) is an implementation
 independent of VecJac and of the restatement in this folder: different pivoting (de Rijk),
 different rotations and convergence test, the same kind of relative accuracy. It comes
-from the OpenBLAS that numpy bundles (symbols scipy_?gesvj_64_, ILP64), else from scipy's
-(scipy_?gesvj_, LP64). The tests compare singular values -- of the restatement on CPU and
+from the OpenBLAS that numpy bundles (symbols scipy_?gesvj_64_, ILP64), else from another
+bundled OpenBLAS or the system LAPACK (?gesvj_, LP64). The tests compare singular values -- of the restatement on CPU and
 of the GPU library -- with it; nothing in the library uses it.
 
 `python -m oracle.lapack M N BaseName [kind]` mirrors the reference's LAPACK driver
@@ -26,26 +26,30 @@ _LIB = None
 
 
 def _find():
-    """(CDLL, symbol suffix, integer type) of an OpenBLAS with xGESVJ, or None."""
-    cands = []
-    try:
-        d = os.path.join(os.path.dirname(os.path.dirname(np.__file__)), "numpy.libs")
-        cands += [(p, "_64_", C.c_int64) for p in sorted(glob.glob(os.path.join(d, "libscipy_openblas64_*.so")))]
-    except Exception:
-        pass
-    try:
-        import scipy
-        d = os.path.join(os.path.dirname(os.path.dirname(scipy.__file__)), "scipy.libs")
-        cands += [(p, "_", C.c_int32) for p in sorted(glob.glob(os.path.join(d, "libscipy_openblas*.so")))]
-    except Exception:
-        pass
-    for path, suf, it in cands:
+    """(CDLL, symbol prefix, symbol suffix, integer type) of a LAPACK with xGESVJ, or None:
+    the OpenBLAS that numpy or scipy bundles (scipy-openblas or older openblas builds,
+    ILP64 or LP64), else the system LAPACK."""
+    import ctypes.util
+    libs = []
+    for mod, sub in (("numpy", "numpy.libs"), ("scipy", "scipy.libs")):
+        try:
+            m = __import__(mod)
+            d = os.path.join(os.path.dirname(os.path.dirname(m.__file__)), sub)
+            libs += sorted(glob.glob(os.path.join(d, "lib*openblas*.so*")))
+        except Exception:
+            pass
+    sysl = ctypes.util.find_library("lapack")
+    if sysl:
+        libs.append(sysl)
+    names = (("scipy_", "_64_", C.c_int64), ("", "_64_", C.c_int64), ("scipy_", "_", C.c_int32), ("", "_", C.c_int32))
+    for path in libs:
         try:
             lib = C.CDLL(path)
-            getattr(lib, "scipy_dgesvj" + suf)
-            return lib, suf, it
-        except (OSError, AttributeError):
+        except OSError:
             continue
+        for pre, suf, it in names:
+            if hasattr(lib, pre + "dgesvj" + suf):
+                return lib, pre, suf, it
     return None
 
 
@@ -69,7 +73,7 @@ def gesvj(kind, A):
     sweeps, max |cos| and max |sin| of the last sweep), sva = SVA as returned."""
     if not available():
         raise RuntimeError("no LAPACK with xGESVJ found")
-    lib, suf, I = _LIB
+    lib, pre, suf, I = _LIB
     real = np.float64 if kind in "dz" else np.float32
     cplx = kind in "zc"
     dt = (np.complex128 if kind == "z" else np.complex64) if cplx else real
@@ -80,7 +84,7 @@ def gesvj(kind, A):
     info = I(0)
     mi, ni = I(m), I(n)
     hidden = (C.c_size_t(1), C.c_size_t(1), C.c_size_t(1))
-    f = getattr(lib, "scipy_%sgesvj%s" % (kind, suf))
+    f = getattr(lib, "%s%sgesvj%s" % (pre, kind, suf))
     jobs = (C.c_char_p(b"G"), C.c_char_p(b"U"), C.c_char_p(b"V"))
     if not cplx:
         lwork = max(6, m + n)
