@@ -3,6 +3,7 @@
  * 64-byte aligned buffers). Without a GPU it checks the argument codes the library returns
  * before touching the device and that a valid call reports VJ_ERR_NO_GPU; it prints
  * "ok <int bits>" or the first failed check. Built with and without -DVJ_LP64. */
+#include <fenv.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
@@ -42,6 +43,19 @@ int main(int argc, char **argv)
   CHECK(dvjsvd_(&m, &n, G, &ldG, V, &ldV, w, w + 32, js, &stp, &swp, w + 65, iwork), -12);
   const vj_fint n2 = -12;
   CHECK(dbjac2_(&n2, w, w, w, w, w, w, w, iwork), -1);
+  /* the reference's floating-point environment check comes first: a rounding mode other
+   * than to-nearest gives -14 (real) / -18 (complex), and the caller's mode is kept */
+  fesetround(FE_UPWARD);
+  CHECK(dvjsvd_(&m, &n, G, &ldG, V, &ldV, w, w + 32, js, &stp, &swp, w + 64, iwork), -14);
+  CHECK(zvjsvd_(&m, &n, G, &ldG, G, &ldG, V, &ldV, V, &ldV, w, w + 32, js, &stp, &swp, w + 64, iwork), -18);
+  CHECK(fegetround(), FE_UPWARD);
+  if (!gpu) {
+    /* the device-pointer form computes its host-side values to nearest and restores the
+     * caller's mode on return (here it returns at once: no GPU) */
+    CHECK(vj_dvjsvd_dev(m, n, G, ldG, V, ldV, w, w + 32, js, stp, swp, 0, NULL), VJ_ERR_NO_GPU);
+    CHECK(fegetround(), FE_UPWARD);
+  }
+  fesetround(FE_TONEAREST);
   if (!gpu)
     CHECK(dvjsvd_(&m, &n, G, &ldG, V, &ldV, w, w + 32, js, &stp, &swp, w + 64, iwork), VJ_ERR_NO_GPU);
   printf("ok %d\n", vj_abi_int_bits());

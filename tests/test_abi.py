@@ -152,7 +152,7 @@ def test_c_caller(libpath, lp64_path, tmp_path, lp64):
     exe = str(tmp_path / "c_caller")
     cmd = ["gcc", "-std=c11", "-Wall", "-Werror", "-I" + os.path.join(ROOT, "include")]
     cmd += (["-DVJ_LP64"] if lp64 else []) + [os.path.join(ROOT, "tests", "c_caller.c"), "-L" + os.path.dirname(lib),
-                                               "-lvecjac_gb300", "-Wl,-rpath," + os.path.dirname(lib), "-o", exe]
+                                               "-lvecjac_gb300", "-Wl,-rpath," + os.path.dirname(lib), "-lm", "-o", exe]
     r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
     r = subprocess.run([exe] + (["gpu"] if torch.cuda.is_available() else []), capture_output=True, text=True,

@@ -428,6 +428,7 @@ static vj_fint svd_dev(vj_fnat m_, vj_fnat n_, T *G, vj_fnat ldG, T *Gi, vj_fnat
                        cudaStream_t s, unsigned char *scratch = nullptr)
 {
   constexpr int L = svdc<T>::LANES;
+  const host::NearestRounding rn;
   const long long m = (long long)m_, n = (long long)n_;
   const long long n_2 = n >> 1;
   if (!n)
@@ -628,7 +629,13 @@ static vj_fint svd_host(const vj_fnat *m, const vj_fnat *n, T *G, const vj_fnat 
 {
   constexpr int L = svdc<T>::LANES;
   const long long mm = (long long)*m, nn = (long long)*n;
-  // the reference's argument checks, in its order (src/dvjsvd.c:43-68, src/zvjsvd.c:43-80)
+  // the reference's argument checks, in its order (src/dvjsvd.c:43-68, src/zvjsvd.c:43-80);
+  // first its floating-point environment check (IS_NOT_VFPENV, src/vec.h): the rounding
+  // control of the caller's thread must be round-to-nearest (the MXCSR flush-to-zero and
+  // denormals-are-zero bits it also checks have no portable reading and do not change
+  // these results)
+  if (fegetround() != FE_TONEAREST)
+    return CPLX ? -18 : -14;
   if (!nn)
     return 0;
   if (*m < *n || (mm % L))

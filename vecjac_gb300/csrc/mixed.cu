@@ -525,6 +525,7 @@ static vj_fint mixed_dev(vj_fnat m_, vj_fnat n_, double *G, vj_fnat ldG, double 
                          vj_fnat ldV, double *Vi, vj_fnat ldVi, double *eS, double *fS, const unsigned *js,
                          unsigned stp, unsigned swp, unsigned stages, cudaStream_t s, unsigned *presweeps)
 {
+  const host::NearestRounding rn;
   const long long m = (long long)m_, n = (long long)n_;
   if (presweeps)
     presweeps[0] = presweeps[1] = 0;

@@ -1,6 +1,7 @@
 // Host-side services shared by the entry points: device discovery, a growable device
 // staging buffer for the host-pointer forms, and a pair of library-owned streams.
 #pragma once
+#include <cfenv>
 #include <cstddef>
 #include <cuda_runtime.h>
 
@@ -8,6 +9,24 @@
 
 namespace vj {
 namespace host {
+
+// Round-to-nearest for the host-side arithmetic of one call (tolerances, rescaling
+// bounds), whatever rounding mode the caller's thread has; the caller's mode is restored.
+struct NearestRounding {
+  int saved;
+  NearestRounding() : saved(fegetround())
+  {
+    if (saved != FE_TONEAREST)
+      fesetround(FE_TONEAREST);
+  }
+  ~NearestRounding()
+  {
+    if (saved != FE_TONEAREST)
+      fesetround(saved);
+  }
+  NearestRounding(const NearestRounding &) = delete;
+  NearestRounding &operator=(const NearestRounding &) = delete;
+};
 
 // true when a CUDA device is usable (checked once; the current device is used)
 bool gpu_ready();
