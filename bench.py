@@ -9,6 +9,11 @@ data set). One step = one pass of all four batches (n < 0: cosines and sines).
 Metric: GB/s of algorithmic HBM traffic (56.5 / 72.5 / 28.25 / 36.25 bytes per element for
 d / z / s / c: inputs, outputs and the permutation bitmask), whole job. The inputs
 (37 GB) exceed the 129 MB L2 many times over, so no L2 flush is needed between steps.
+The same line carries the SVD half of the metric in its "svd" object (--no-svd leaves it
+out): dvjsvd 1024x1024 FP64 and zvjsvd 4096x2048 FP64 complex, mixed-precision and plain,
+in matrices/s with sweeps, the mixed/plain ratio and the errors against the exact singular
+values and against the FP64 oracle (the plain path, the reference's algorithm bit for bit);
+the plain 4096x2048 run takes about a minute (--svd-plain-steps 0 skips it).
 
 Other workloads (--workload): "svd1024" (dvjsvd_ on a 1024x1024 FP64 matrix, matrices/s),
 "zsvd" (zvjsvd_ on 4096x2048 FP64 complex), "zsvd_mixed"/"dsvd_mixed" (the same matrix
@@ -171,11 +176,36 @@ class Batch:
 # thread instructions per element of k_bjac2 (ncu smsp__inst_executed.sum x 32 / elements,
 # 2^24 real and 2^23 complex launches; the profile summary k_bjac2_2e24_full)
 BJAC2_INST_PER_ELEM = {"d": 1243.0, "z": 1946.0}
+# thread instructions per element that execute on the FP64 pipe (ncu
+# smsp__inst_executed_pipe_fp64.sum x 32 / elements; profile summary k_bjac2_fp64_pipe_2e24)
+BJAC2_FP64_PIPE_PER_ELEM = {"d": None, "z": None}
 # DRAM bytes (read + write) of one 2^24-element real FP64 launch, from the same capture
 BJAC2_D_DRAM_2E24 = 402.791680e6 + 487.371776e6
+# the reference's own AVX-512 dbjac2_/zbjac2_ (src/dbjac2.c, src/zbjac2.c, compiled from its
+# sources) on an x86-64 host with AVX-512, 8 threads, 2^24 elements of the same distribution,
+# best of 5; it cannot be built on this Arm host (src/vec.h:11), so the figure is not measured
+# in this run
+X86_REFERENCE_BJAC2 = {"dbjac2_": {"gbs": 50.6, "threads": 8}, "zbjac2_": {"gbs": 50.5, "threads": 8},
+                       "host": "x86-64 Sapphire Rapids (AVX-512), gcc 13.3 -O3 -march=native -fopenmp"}
 
 
-def issue_bound(kind, sm_mhz, sms=152):
+def device_info():
+    """SM count (from the device) and the measured FMA rates of its FP64 and FP32 pipes
+    (vj_measure_fma_rate: a kernel of independent FMA chains on every SM)."""
+    import ctypes as C
+    import torch
+    import vecjac_gb300 as vj
+    props = torch.cuda.get_device_properties(torch.cuda.current_device())
+    out = {"sms": int(props.multi_processor_count), "name": props.name}
+    L = vj.lib()
+    for key, f64 in (("fp64_fma_per_s", 1), ("fp32_fma_per_s", 0)):
+        v = C.c_double(0.0)
+        r = L.vj_measure_fma_rate(C.c_int(f64), C.byref(v), None)
+        out[key] = float(v.value) if r == 0 else None
+    return out
+
+
+def issue_bound(kind, sm_mhz, sms):
     """Element-rate bound of the FP64 2x2 from instruction issue: each SM issues at most one
     warp instruction per clock on each of its 4 sub-partitions (128 thread instructions per
     clock), and the kernel executes BJAC2_INST_PER_ELEM[kind] thread instructions per
@@ -220,13 +250,42 @@ def bench_bjac2(args, vj, dist, rank, world):
     value = world * total_bytes / (ms * 1e-3) / 1e9
     clocks = clk.summary()
     pk, pk_src = peaks()
+    dev = device_info()
     # dominant kernel: the FP64 real batch
     dom = batches[0]
     dom_gbs = dom.bytes() / (per_ms["d"] * 1e-3) / 1e9
     sm_mhz = clocks["sm_mhz"] or pk.get("sm_max_mhz", 2070.0)
-    fb = issue_bound("d", sm_mhz)
+    fb = issue_bound("d", sm_mhz, dev["sms"])
     per_kernel = {k: {"ms": round(per_ms[k], 4), "elements": b.n,
-                      "gbs": round(b.bytes() / (per_ms[k] * 1e-3) / 1e9, 1)} for k, b in zip(kinds, batches)}
+                      "gbs": round(b.bytes() / (per_ms[k] * 1e-3) / 1e9, 1),
+                      "hbm_frac": round(b.bytes() / (per_ms[k] * 1e-3) / 1e9 / pk["hbm_gbs"], 4)}
+                  for k, b in zip(kinds, batches)}
+    # the FP64 kinds are bound by the FP64 pipe: FP64-pipe instructions per element (ncu) x
+    # elements/s against the measured DFMA rate of this GPU
+    for k in "dz":
+        if BJAC2_FP64_PIPE_PER_ELEM[k] and dev["fp64_fma_per_s"]:
+            eps_ = per_kernel[k]["elements"] / (per_kernel[k]["ms"] * 1e-3)
+            per_kernel[k]["fp64_pipe_frac"] = round(eps_ * BJAC2_FP64_PIPE_PER_ELEM[k] / dev["fp64_fma_per_s"], 4)
+    if BJAC2_FP64_PIPE_PER_ELEM["d"] and dev["fp64_fma_per_s"]:
+        ach = dom.n / (per_ms["d"] * 1e-3) * BJAC2_FP64_PIPE_PER_ELEM["d"]
+        roof = {"bound": "fp64_pipe", "kernel": "k_bjac2<double,real,sine>", "achieved": round(ach / 1e12, 5),
+                "peak": round(dev["fp64_fma_per_s"] / 1e12, 5), "unit": "Tinst/s",
+                "frac": round(ach / dev["fp64_fma_per_s"], 4),
+                "peak_source": "measured live: vj_measure_fma_rate (DFMA chains on all %d SMs)" % dev["sms"],
+                "achieved_source": "%.1f FP64-pipe thread instructions per element (ncu) x elements/s"
+                                   % BJAC2_FP64_PIPE_PER_ELEM["d"]}
+    else:
+        roof = {"bound": "fp64_pipe", "kernel": "k_bjac2<double,real,sine>", "achieved": None, "peak": None,
+                "unit": "Tinst/s", "frac": None}
+    roof["hbm"] = {"achieved": round(dom_gbs, 1), "peak": pk["hbm_gbs"], "unit": "GB/s",
+                   "frac": round(dom_gbs / pk["hbm_gbs"], 4), "peak_source": pk_src,
+                   "traffic": round(BJAC2_D_DRAM_2E24 * dom.n / 2 ** 24),
+                   "traffic_source": "ncu dram__bytes_read+write of a 2^24-element launch, scaled to this launch"}
+    roof["issue"] = {"elements_per_s": round(dom.n / (per_ms["d"] * 1e-3), 1),
+                     "bound_elements_per_s": round(fb, 1),
+                     "frac": round(dom.n / (per_ms["d"] * 1e-3) / fb, 4),
+                     "note": "%d thread instructions per element (ncu), 128 per clock per SM, %d SMs"
+                             % (BJAC2_INST_PER_ELEM["d"], dev["sms"])}
     out = {
         "metric": "batched 2x2 Hermitian EVD throughput (GB/s of HBM traffic)",
         "value": round(value, 2), "unit": "GB/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -237,17 +296,8 @@ def bench_bjac2(args, vj, dist, rank, world):
                    "bytes_per_step": total_bytes, "l2": "inputs larger than L2 (no flush)",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "per_kernel": per_kernel,
-        "roofline": {"bound": "hbm", "kernel": "k_bjac2<double,real,sine>", "achieved": round(dom_gbs, 1),
-                     "peak": pk["hbm_gbs"], "unit": "GB/s", "frac": round(dom_gbs / pk["hbm_gbs"], 4),
-                     "peak_source": pk_src,
-                     "traffic": round(BJAC2_D_DRAM_2E24 * dom.n / 2 ** 24),
-                     "traffic_source": "ncu dram__bytes_read+write of a 2^24-element launch, scaled to this launch",
-                     "binding": "FP64 pipe (75% active) and instruction issue (49%), ncu",
-                     "issue": {"elements_per_s": round(dom.n / (per_ms["d"] * 1e-3), 1),
-                               "bound_elements_per_s": round(fb, 1),
-                               "frac": round(dom.n / (per_ms["d"] * 1e-3) / fb, 4),
-                               "note": "%d thread instructions per element (ncu), 128 per clock per SM"
-                                       % BJAC2_INST_PER_ELEM["d"]}},
+        "roofline": roof,
+        "device": dev,
         "clocks": clocks,
         "gpu_launches": args.steps * len(batches),
     }
@@ -258,6 +308,9 @@ def bench_bjac2(args, vj, dist, rank, world):
         out["e2e"] = e2e_bjac2(args, vj, dist, world)
     if rank == 0 and args.cpu_baseline:
         out["cpu_baseline"] = cpu_baseline_bjac2(args.cpu_elems)
+        out["cpu_baseline"]["x86_reference"] = X86_REFERENCE_BJAC2
+    if args.svd:
+        out["svd"] = bench_svd_suite(args, vj, dist, rank, world)
     return out
 
 
@@ -417,22 +470,128 @@ def reference_arm(args, dist, rank):
 # mixed_zsvd4096x2048_kernels_full)
 MIXED_F32_STEP_DRAM = 100.695296e6 + 39.812864e6
 
-# FP64 and FP32 FMA rates measured on this GB300 (operations per clock per SM)
-FP64_FMA_PER_CLK_SM = 1.68
-FP32_FMA_PER_CLK_SM = 116.0
-
-
-def svd_roofline(flops_per_s, fp64, sm_mhz, kernel, sms=152):
+def svd_roofline(flops_per_s, fp64, kernel, dev=None):
     """Roofline object for the Jacobi SVD workloads: algorithmic FLOP rate (12m + 6n real,
-    36m + 20n complex per pair and sweep) against the FMA pipe's peak at the sampled clock."""
-    per = FP64_FMA_PER_CLK_SM if fp64 else FP32_FMA_PER_CLK_SM
-    peak = 2.0 * per * sms * sm_mhz * 1e6 / 1e12
+    36m + 20n complex per pair and sweep) against the FMA pipe's peak, measured live on this
+    GPU (vj_measure_fma_rate; 2 flops per FMA)."""
+    dev = dev or device_info()
+    fma = dev["fp64_fma_per_s" if fp64 else "fp32_fma_per_s"]
+    peak = 2.0 * fma / 1e12 if fma else None
     ach = flops_per_s / 1e12
     return {"bound": "fp64_pipe" if fp64 else "fp32_pipe", "kernel": kernel, "achieved": round(ach, 5),
-            "peak": round(peak, 3), "unit": "TFLOP/s", "frac": round(ach / peak, 4), "traffic": None,
-            "peak_source": "measured FMA rate per SM x %d SMs x sampled clock" % sms,
+            "peak": round(peak, 3) if peak else None, "unit": "TFLOP/s",
+            "frac": round(ach / peak, 4) if peak else None, "traffic": None,
+            "peak_source": "measured live: vj_measure_fma_rate (FMA chains on all %d SMs)" % dev["sms"],
             "note": "algorithmic FLOPs; the reference's scaled compensated dot product executes ~9 operations "
                     "per element and accumulator chain, so the pipe is busier than this fraction"}
+
+
+def svd_case(args, vj, dist, kind, m, n, lo, mixed_steps, plain_steps, warmup, seed=2024):
+    """One SVD configuration timed through the device entry points (CUDA events on the
+    launching stream): the mixed-precision path (FP32 presweeps, FP64 finish) and the plain
+    FP64 path (the reference's algorithm, bit-identical to the compiled reference and the
+    oracle). Errors: singular values against the exact ones of the construction, mixed
+    against plain (the FP64 oracle's result), and ||U^H U - I||_F, ||V^H V - I||_F in units
+    of n eps."""
+    import torch
+    from vecjac_gb300 import workloads as W
+    cx = kind == "z"
+    A, s = W.svd_matrix(m, n, seed=seed, lo=lo, complex_=cx)
+    js, stp = vj.pjs(args.pivot, n)
+    Gt = torch.tensor(np.ascontiguousarray(A.real.T), dtype=torch.float64, device="cuda")
+    Git = torch.tensor(np.ascontiguousarray(A.imag.T), dtype=torch.float64, device="cuda") if cx else None
+    G, Gi = torch.empty_like(Gt), (torch.empty_like(Gt) if cx else None)
+    V = torch.empty((n, n), dtype=torch.float64, device="cuda")
+    Vi = torch.empty_like(V) if cx else None
+    eS = torch.empty(n, dtype=torch.float64, device="cuda")
+    fS = torch.empty_like(eS)
+    djs = torch.tensor(js.astype(np.int32), device="cuda")
+    stream = torch.cuda.current_stream()
+    eps = float(np.finfo(np.float64).eps)
+
+    def reset():
+        G.copy_(Gt)
+        if cx:
+            Gi.copy_(Git)
+
+    def mixed():
+        reset()
+        return vj.vjsvd_mixed_dev(kind, m, n, G, m, V, n, eS, fS, djs, stp, Gi=Gi, ldGi=m, Vi=Vi, ldVi=n,
+                                  stream=stream.cuda_stream)
+
+    def plain():
+        reset()
+        return vj.vjsvd_dev(kind, m, n, G, m, V, n, eS, fS, djs, stp, Gi=Gi, ldGi=m, Vi=Vi, ldVi=n,
+                            stream=stream.cuda_stream)
+
+    def timed(fn, k):
+        torch.cuda.synchronize()
+        barrier(dist)
+        t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0.record(stream)
+        for _ in range(k):
+            r = fn()
+        t1.record(stream)
+        torch.cuda.synchronize()
+        return allmax(dist, t0.elapsed_time(t1)) / k, r
+
+    def results():
+        sig = (fS * torch.exp2(eS)).cpu().numpy()
+        U = torch.complex(G, Gi) if cx else G
+        Vm = torch.complex(V, Vi) if cx else V
+        # stored column-major: row j of the tensor is column j of the matrix
+        ou = float(torch.linalg.norm(U.conj() @ U.T - torch.eye(n, dtype=U.dtype, device="cuda")))
+        ov = float(torch.linalg.norm(Vm.conj() @ Vm.T - torch.eye(n, dtype=Vm.dtype, device="cuda")))
+        srt = np.sort(sig)[::-1]
+        return sig, {"max_rel_sigma_err_vs_exact": float(np.max(np.abs(srt - s) / s)),
+                     "max_sigma_err_over_sigma_max": float(np.max(np.abs(srt - s)) / s[0]),
+                     "orth_U_fro_over_n_eps": round(ou / (n * eps), 3),
+                     "orth_V_fro_over_n_eps": round(ov / (n * eps), 3)}
+
+    per_pair = (36 * m + 20 * n) if cx else (12 * m + 6 * n)
+    out = {"config": "%svjsvd %dx%d, sigma log-uniform in [1e%d, 1], pivot strategy id %d" % (kind, m, n, lo, args.pivot),
+           "bound_64_n_eps": 64 * n * eps}
+    for _ in range(warmup):
+        mixed()
+    ms, (sw, sw32, swf) = timed(mixed, mixed_steps)
+    ph = vj.last_mixed_phases()
+    sig_m, err_m = results()
+    out["mixed"] = dict({"ms_per_matrix": round(ms, 2), "matrices_per_s": round(1000.0 / ms, 4),
+                         "steps": mixed_steps, "sweeps_fp32": int(sw32), "sweeps_fp64_plain_dot": int(swf),
+                         "sweeps_fp64_reference": int(sw),
+                         "phases_ms": {k: round(v, 1) for k, v in ph.items() if k.endswith("_ms")}}, **err_m)
+    if plain_steps > 0:
+        pms, psw = timed(plain, plain_steps)
+        sig_p, err_p = results()
+        out["plain"] = dict({"ms_per_matrix": round(pms, 2), "matrices_per_s": round(1000.0 / pms, 5),
+                             "steps": plain_steps, "sweeps": int(psw),
+                             "flops_per_s": psw * (n * (n - 1) / 2) * per_pair / (pms * 1e-3)}, **err_p)
+        rel = float(np.max(np.abs(np.sort(sig_m) - np.sort(sig_p)) / np.sort(sig_p)))
+        out["mixed"]["max_rel_sigma_err_vs_fp64_oracle"] = rel
+        out["mixed"]["within_64_n_eps_of_fp64_oracle"] = bool(rel <= 64 * n * eps)
+        out["mixed_over_plain"] = round(pms / ms, 3)
+    return out
+
+
+def bench_svd_suite(args, vj, dist, rank, world):
+    """The SVD half of the metric beside the 2x2 line: dvjsvd 1024x1024 FP64 (sigma in
+    [1e-6, 1]) and zvjsvd 4096x2048 FP64 complex (sigma in [1e-8, 1]), each mixed-precision
+    and plain, with matrices/s, sweeps, the mixed/plain ratio and the errors against the
+    exact singular values and the FP64 oracle (the plain path, which is the reference's
+    algorithm bit for bit)."""
+    import torch
+    with Clocks(torch.cuda.current_device()) as clk:
+        d = svd_case(args, vj, dist, "d", 1024, 1024, -6, mixed_steps=3, plain_steps=1, warmup=1, seed=2024 + rank)
+        z = svd_case(args, vj, dist, "z", 4096, 2048, -8, mixed_steps=1, plain_steps=args.svd_plain_steps,
+                     warmup=1, seed=2024 + rank)
+    dev = device_info()
+    for c, cx in ((d, False), (z, True)):
+        if "plain" in c:
+            c["plain"]["roofline"] = svd_roofline(c["plain"]["flops_per_s"], True,
+                                                  "k_step<double,%s>" % ("cplx" if cx else "real"), dev)
+    return {"metric": "Jacobi SVD matrices/s at FP64 accuracy, mixed vs plain", "unit": "matrices/s",
+            "timing": "CUDA events on the launching stream around each call (inputs resident on the GPU)",
+            "dvjsvd_1024x1024": d, "zvjsvd_4096x2048": z, "clocks": clk.summary()}
 
 
 def cpu_baseline_svd(kind, A, js, stp, sweeps, budget_s=10.0):
@@ -515,8 +674,7 @@ def bench_svd(args, vj, dist, rank, world, kind, m, n):
                        "sweeps": int(sweeps), "max_rel_sigma_err_vs_exact": err},
             "flops_per_s": flops / (ms * 1e-3), "clocks": clk.summary(),
             "gpu_launches": int(sweeps + 1) * stp}
-    csum = out["clocks"]
-    out["roofline"] = svd_roofline(out["flops_per_s"], kind in "dz", csum.get("sm_mhz") or 2070.0,
+    out["roofline"] = svd_roofline(out["flops_per_s"], kind in "dz",
                                    "k_step<%s,%s>" % ("double" if kind in "dz" else "float",
                                                       "cplx" if cx else "real"))
     if rank == 0 and args.cpu_baseline:
@@ -813,7 +971,7 @@ def bench_batch(args, vj, dist, rank, world, kind):
             "one_launch_per_matrix_s_estimate": round(per_launch, 2),
             "speedup_vs_per_matrix_launches": round(per_launch / (ms * 1e-3), 2),
             "clocks": clk.summary(), "gpu_launches": 2 * args.steps}
-    out["roofline"] = svd_roofline(out["flops_per_s"], kind == "d", out["clocks"].get("sm_mhz") or 2070.0,
+    out["roofline"] = svd_roofline(out["flops_per_s"], kind == "d",
                                    "k_batch<%s>" % ("double" if kind == "d" else "float"))
     if rank == 0 and args.cpu_baseline:
         out["cpu_baseline"] = cpu_baseline_batch(mats, kind, args.pivot)
@@ -873,6 +1031,10 @@ def main():
     ap.add_argument("--e2e-shift", type=int, default=0, help="further shrink of the e2e batches")
     ap.add_argument("--no-e2e", dest="e2e", action="store_false")
     ap.add_argument("--no-cpu", dest="cpu_baseline", action="store_false")
+    ap.add_argument("--no-svd", dest="svd", action="store_false",
+                    help="leave the SVD object (dvjsvd 1024^2 and zvjsvd 4096x2048) out of the default line")
+    ap.add_argument("--svd-plain-steps", type=int, default=1,
+                    help="timed runs of the plain zvjsvd 4096x2048 in the SVD object (0: skip, ~1 min each)")
     ap.add_argument("--cpu-elems", type=int, default=24)
     ap.add_argument("--pivot", type=int, default=4, help="pivot strategy id for the SVD workloads")
     args = ap.parse_args()

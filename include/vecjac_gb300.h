@@ -36,7 +36,9 @@ typedef unsigned long long vj_fnat;  /* fnat under MKL_ILP64 */
  *   [c  -s'] [a11  a21'] [ c  s]  = diag(l1, l2) with s = at (real) or cat + i*sat (complex)
  * p[i/8] (FP64) or p[i/16] (FP32) bit (i%8 or i%16) = (L1 < L2) of the scaled eigenvalues.
  * |n| must be a multiple of 8 (d, z) or 16 (s, c); returns 1 on success (like the
- * reference's OpenMP build), -1 if |n| is not such a multiple.
+ * reference's OpenMP build), -1 if |n| is not such a multiple, and (host forms, checked
+ * first, as the reference's IS_NOT_VFPENV) -10 (d, s) / -12 (z, c) when the calling
+ * thread's rounding mode is not round-to-nearest.
  *   replaces dbjac2_  src/dbjac2.h:6,  src/dbjac2.c:81
  *            zbjac2_  src/zbjac2.h:6,  src/zbjac2.c:108
  *            sbjac2_  src/sbjac2.h:6,  src/sbjac2.c:81
@@ -180,17 +182,49 @@ vj_fint vj_svjsvd_batch_dev(vj_fint count, const long long *m, const long long *
                             const int *order, long strategy, unsigned swp, long long *info, int block, void *stream);
 
 /* Allocation-free FP64 SVD. No counterpart in the reference. For callers that must not
- * allocate GPU memory while they run -- for example code that is being captured into a
- * CUDA graph, or an application whose memory pool owns the whole device -- this form
- * takes only the matrices and the outputs: the pivot table (strategy 2 or 4, generated on
- * the GPU) and the control block live in a fixed 1 MiB + 512 B device array inside the
- * library, present on every GPU that loads it until the process exits. n must not exceed
- * 512 (VJ_ERR_ARG otherwise); the other arguments and the result are those of
- * vj_dvjsvd_dev. The first call on a device looks up that array's address (do it before
- * any stream capture). Every call shares the array: calls that overlap on the GPU, on any
- * stream or thread, race and must be serialised by the caller. */
+ * allocate GPU memory while they run -- for example an application whose memory pool owns
+ * the whole device, or a service that must not call cudaMalloc (which can synchronise the
+ * device or fail for lack of memory) in the middle of its work -- this form takes only the
+ * matrices and the outputs: the pivot table (strategy 2 or 4, generated on the GPU) and
+ * the control block live in a fixed 1 MiB + 512 B device array inside the library, present
+ * on every GPU that loads it until the process exits. n must not exceed 512 (VJ_ERR_ARG
+ * otherwise); the other arguments and the result are those of vj_dvjsvd_dev (it also
+ * synchronises `stream` once per sweep). The first call on a device looks up that array's
+ * address for that device and keeps it. Every call shares the array: calls that overlap on
+ * the GPU, on any stream or thread, race and must be serialised by the caller. */
 vj_fint vj_dvjsvd_dev_noalloc(vj_fnat m, vj_fnat n, double *G, vj_fnat ldG, double *V, vj_fnat ldV, double *eS,
                               double *fS, long strategy, unsigned swp, int preset, void *stream);
+
+/* ---------------- interleaved <-> split complex matrices ----------------
+ * zsplit_ copies an m x n interleaved complex matrix A (re, im pairs: a C `double complex`
+ * array, leading dimension ldA in complex elements) into the planes Ar = Re A and
+ * Ai = Im A (leading dimensions ldAr, ldAi); zmerge_ is its inverse. c* are the FP32 forms.
+ * Checks in the reference's order: -9 a rounding mode other than to-nearest, -1 m not a
+ * multiple of 4 (z) / 8 (c), then each leading dimension below m or not a multiple of 4 / 8
+ * complex (interleaved) or 8 / 16 real (planes) elements: split -4 ldA, -6 ldAr, -8 ldAi;
+ * merge -4 ldAr, -6 ldAi, -8 ldA. Returns 1 (the reference's OpenMP build). Host pointers,
+ * synchronous; the vj_*_dev forms take device pointers and a stream (their alignment codes:
+ * split -3 A, -5 Ar, -7 Ai; merge -3 Ar, -5 Ai, -7 A, natural alignment of the element).
+ *   replaces zsplit_  src/zsplit.h:6, src/zsplit.c:3
+ *            zmerge_  src/zmerge.h:6, src/zmerge.c:3
+ *            csplit_  src/csplit.h:6, src/csplit.c:3
+ *            cmerge_  src/cmerge.h:6, src/cmerge.c:3 */
+vj_fint zsplit_(const vj_fnat m[1], const vj_fnat n[1], const double A[], const vj_fnat ldA[1], double Ar[],
+                const vj_fnat ldAr[1], double Ai[], const vj_fnat ldAi[1]);
+vj_fint zmerge_(const vj_fnat m[1], const vj_fnat n[1], const double Ar[], const vj_fnat ldAr[1], const double Ai[],
+                const vj_fnat ldAi[1], double A[], const vj_fnat ldA[1]);
+vj_fint csplit_(const vj_fnat m[1], const vj_fnat n[1], const float A[], const vj_fnat ldA[1], float Ar[],
+                const vj_fnat ldAr[1], float Ai[], const vj_fnat ldAi[1]);
+vj_fint cmerge_(const vj_fnat m[1], const vj_fnat n[1], const float Ar[], const vj_fnat ldAr[1], const float Ai[],
+                const vj_fnat ldAi[1], float A[], const vj_fnat ldA[1]);
+vj_fint vj_zsplit_dev(vj_fnat m, vj_fnat n, const double *A, vj_fnat ldA, double *Ar, vj_fnat ldAr, double *Ai,
+                      vj_fnat ldAi, void *stream);
+vj_fint vj_zmerge_dev(vj_fnat m, vj_fnat n, const double *Ar, vj_fnat ldAr, const double *Ai, vj_fnat ldAi,
+                      double *A, vj_fnat ldA, void *stream);
+vj_fint vj_csplit_dev(vj_fnat m, vj_fnat n, const float *A, vj_fnat ldA, float *Ar, vj_fnat ldAr, float *Ai,
+                      vj_fnat ldAi, void *stream);
+vj_fint vj_cmerge_dev(vj_fnat m, vj_fnat n, const float *Ar, vj_fnat ldAr, const float *Ai, vj_fnat ldAi, float *A,
+                      vj_fnat ldA, void *stream);
 
 /* ---------------- pivot strategy tables ----------------
  * replaces pjs() src/pjs.h:21, src/pjs.c:9: returns a malloc'ed table of *stp rows of n
@@ -215,6 +249,11 @@ typedef struct vj_trace {
 } vj_trace;
 vj_fint vj_last_trace(vj_trace *out);
 const char *vj_version(void);
+/* Measured peak of the current GPU's FMA pipe: fp64 != 0 DFMA, else FFMA. Writes the
+ * thread-level FMA operations per second of a kernel of independent FMA chains over every
+ * SM (CUDA-event timed, best of 3) to *ops_per_s; the roofline denominator of the kernels
+ * bound by arithmetic. Returns 0 or a VJ_ERR_* code. No counterpart in the reference. */
+vj_fint vj_measure_fma_rate(int fp64, double *ops_per_s, void *stream);
 /* Width in bits of vj_fint / vj_fnat in this build: 64 (ILP64, the default, as the
  * reference's ABI=ilp64) or 32 (built with -DVJ_LP64, as the reference's ABI=lp64). */
 int vj_abi_int_bits(void);

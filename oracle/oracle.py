@@ -120,6 +120,33 @@ class _Lib:
         return r, G, V, eS, fS
 
 
+    # ----- interleaved <-> split complex -----
+    def split(self, kind, A):
+        """?split_ of a complex matrix (kind 'z' or 'c'). Returns (ret, Ar, Ai)."""
+        dt = np.float64 if kind == "z" else np.float32
+        m, n = A.shape
+        Ac = acopy(A, np.complex128 if kind == "z" else np.complex64, order="F")
+        Ar = aligned((m, n), dt, order="F")
+        Ai = aligned((m, n), dt, order="F")
+        f = self.fn(kind + "split_")
+        f.restype = _ll
+        mm, nn = _ull(m), _ull(n)
+        r = f(C.byref(mm), C.byref(nn), _ptr(Ac), C.byref(mm), _ptr(Ar), C.byref(mm), _ptr(Ai), C.byref(mm))
+        return r, Ar, Ai
+
+    def merge(self, kind, Ar, Ai):
+        """?merge_ of two planes (kind 'z' or 'c'). Returns (ret, A)."""
+        dt = np.float64 if kind == "z" else np.float32
+        m, n = Ar.shape
+        Arc, Aic = acopy(Ar, dt, order="F"), acopy(Ai, dt, order="F")
+        A = aligned((m, n), np.complex128 if kind == "z" else np.complex64, order="F")
+        f = self.fn(kind + "merge_")
+        f.restype = _ll
+        mm, nn = _ull(m), _ull(n)
+        r = f(C.byref(mm), C.byref(nn), _ptr(Arc), C.byref(mm), _ptr(Aic), C.byref(mm), _ptr(A), C.byref(mm))
+        return r, A
+
+
 class Restatement(_Lib):
     def __init__(self):
         if not os.path.exists(VJO_PATH):

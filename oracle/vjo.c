@@ -223,4 +223,39 @@ unsigned *vjo_pjs(const long id, const unsigned n, unsigned *stp)
   return t;
 }
 
+/* ---------------- interleaved <-> split complex matrices ----------------
+ * zsplit_/zmerge_ (src/zsplit.c:3-56, src/zmerge.c:3-52) and csplit_/cmerge_: column by
+ * column, Ar(i,j) = Re A(i,j), Ai(i,j) = Im A(i,j) and back. The reference permutes whole
+ * vectors; the element values are moved unchanged. Its release build does no argument
+ * checks and returns 1 (OpenMP build). A holds interleaved (re, im) pairs, ldA in complex
+ * elements. */
+#define VJO_SPLIT(NAME, T)                                                                          \
+  long long NAME(const unsigned long long *m, const unsigned long long *n, const T *A,            \
+                 const unsigned long long *ldA, T *Ar, const unsigned long long *ldAr, T *Ai,      \
+                 const unsigned long long *ldAi)                                                   \
+  {                                                                                                \
+    for (unsigned long long j = 0u; j < *n; ++j)                                                   \
+      for (unsigned long long i = 0u; i < *m; ++i) {                                               \
+        Ar[j * *ldAr + i] = A[2u * (j * *ldA + i)];                                                \
+        Ai[j * *ldAi + i] = A[2u * (j * *ldA + i) + 1u];                                           \
+      }                                                                                            \
+    return 1;                                                                                      \
+  }
+#define VJO_MERGE(NAME, T)                                                                          \
+  long long NAME(const unsigned long long *m, const unsigned long long *n, const T *Ar,           \
+                 const unsigned long long *ldAr, const T *Ai, const unsigned long long *ldAi, T *A, \
+                 const unsigned long long *ldA)                                                    \
+  {                                                                                                \
+    for (unsigned long long j = 0u; j < *n; ++j)                                                   \
+      for (unsigned long long i = 0u; i < *m; ++i) {                                               \
+        A[2u * (j * *ldA + i)] = Ar[j * *ldAr + i];                                                \
+        A[2u * (j * *ldA + i) + 1u] = Ai[j * *ldAi + i];                                           \
+      }                                                                                            \
+    return 1;                                                                                      \
+  }
+VJO_SPLIT(vjo_zsplit_, double)
+VJO_MERGE(vjo_zmerge_, double)
+VJO_SPLIT(vjo_csplit_, float)
+VJO_MERGE(vjo_cmerge_, float)
+
 void vjo_free(void *p) { free(p); }

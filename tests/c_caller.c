@@ -48,6 +48,16 @@ int main(int argc, char **argv)
   fesetround(FE_UPWARD);
   CHECK(dvjsvd_(&m, &n, G, &ldG, V, &ldV, w, w + 32, js, &stp, &swp, w + 64, iwork), -14);
   CHECK(zvjsvd_(&m, &n, G, &ldG, G, &ldG, V, &ldV, V, &ldV, w, w + 32, js, &stp, &swp, w + 64, iwork), -18);
+  /* the same check heads the 2x2 EVD (-10 real, -12 complex, src/dbjac2.c:84,
+   * src/zbjac2.c:111) and the complex split/merge (-9, src/zsplit.c:8) */
+  const vj_fint n8 = -8;
+  CHECK(dbjac2_(&n8, w, w, w, w, w, w, w, iwork), -10);
+  CHECK(zbjac2_(&n8, w, w, w, w, w, w, w, w, w, iwork), -12);
+  CHECK(sbjac2i(&n8, (float *)w, (float *)w, (float *)w, (float *)w, (float *)w, (float *)w, (float *)w, iwork), -10);
+  CHECK(cbjac2i(&n8, (float *)w, (float *)w, (float *)w, (float *)w, (float *)w, (float *)w, (float *)w, (float *)w,
+                (float *)w, iwork), -12);
+  CHECK(zsplit_(&m, &n, G, &ldG, V, &ldV, V, &ldV), -9);
+  CHECK(cmerge_(&m, &n, (float *)V, &ldV, (float *)V, &ldV, (float *)G, &ldG), -9);
   CHECK(fegetround(), FE_UPWARD);
   if (!gpu) {
     /* the device-pointer form computes its host-side values to nearest and restores the
@@ -56,6 +66,23 @@ int main(int argc, char **argv)
     CHECK(fegetround(), FE_UPWARD);
   }
   fesetround(FE_TONEAREST);
+  /* split/merge argument codes in the reference's order (src/zsplit.c:8-27,
+   * src/zmerge.c:8-27): rows in whole vectors, then each leading dimension */
+  {
+    vj_fnat m6 = 6, ld4 = 4, ld12 = 12, ld32 = 32, ld36 = 36, n1 = 1;
+    CHECK(zsplit_(&m6, &n1, G, &ld32, V, &ld32, V, &ld32), -1);
+    CHECK(zsplit_(&ld32, &n1, G, &ld4, V, &ld32, V, &ld32), -4);
+    CHECK(zsplit_(&ld32, &n1, G, &ld32, V, &ld36, V, &ld32), -6);
+    CHECK(zsplit_(&ld32, &n1, G, &ld32, V, &ld32, V, &ld12), -8);
+    CHECK(zmerge_(&ld32, &n1, V, &ld36, V, &ld32, G, &ld32), -4);
+    CHECK(zmerge_(&ld32, &n1, V, &ld32, V, &ld4, G, &ld32), -6);
+    CHECK(zmerge_(&ld32, &n1, V, &ld32, V, &ld32, G, &ld4), -8);
+    CHECK(csplit_(&ld12, &n1, (float *)G, &ld32, (float *)V, &ld32, (float *)V, &ld32), -1);
+    CHECK(csplit_(&ld32, &n1, (float *)G, &ld36, (float *)V, &ld32, (float *)V, &ld32), -4);
+    CHECK(cmerge_(&ld32, &n1, (float *)V, &ld32, (float *)V, &ld36, (float *)G, &ld32), -6);
+    if (!gpu)
+      CHECK(zsplit_(&ld32, &n1, G, &ld32, V, &ld32, V, &ld32), VJ_ERR_NO_GPU);
+  }
   if (!gpu)
     CHECK(dvjsvd_(&m, &n, G, &ldG, V, &ldV, w, w + 32, js, &stp, &swp, w + 64, iwork), VJ_ERR_NO_GPU);
   printf("ok %d\n", vj_abi_int_bits());

@@ -1,5 +1,6 @@
 // A stand-in for libvecjac_gb300.so that the command-line drivers are linked against in
-// the CPU tests: pjs and the four ?vjsvd_ entry points with the library's prototypes,
+// the CPU tests: pjs, the four ?vjsvd_ entry points and the complex split/merge with the
+// library's prototypes,
 // checking the arguments the drivers pass and writing known patterns, so that a test can
 // check every byte the drivers read and write without a GPU. Not an SVD.
 //
@@ -99,9 +100,56 @@ vj_fint cplx_svd(const vj_fnat *m, const vj_fnat *n, T *Gr, const vj_fnat *ldGr,
   return 9;
 }
 
+// interleaved <-> planes, element by element (the library's zsplit_/zmerge_ semantics)
+template <typename T> vj_fint split_host(vj_fnat m, vj_fnat n, const T *A, vj_fnat ld, T *Ar, vj_fnat ldr, T *Ai,
+                                         vj_fnat ldi)
+{
+  for (vj_fnat j = 0; j < n; ++j)
+    for (vj_fnat i = 0; i < m; ++i) {
+      Ar[j * ldr + i] = A[2 * (j * ld + i)];
+      Ai[j * ldi + i] = A[2 * (j * ld + i) + 1];
+    }
+  return 1;
+}
+
+template <typename T> vj_fint merge_host(vj_fnat m, vj_fnat n, const T *Ar, vj_fnat ldr, const T *Ai, vj_fnat ldi,
+                                         T *A, vj_fnat ld)
+{
+  for (vj_fnat j = 0; j < n; ++j)
+    for (vj_fnat i = 0; i < m; ++i) {
+      A[2 * (j * ld + i)] = Ar[j * ldr + i];
+      A[2 * (j * ld + i) + 1] = Ai[j * ldi + i];
+    }
+  return 1;
+}
+
 }  // namespace
 
 extern "C" {
+
+vj_fint zsplit_(const vj_fnat m[1], const vj_fnat n[1], const double A[], const vj_fnat ldA[1], double Ar[],
+                const vj_fnat ldAr[1], double Ai[], const vj_fnat ldAi[1])
+{
+  return split_host<double>(*m, *n, A, *ldA, Ar, *ldAr, Ai, *ldAi);
+}
+
+vj_fint zmerge_(const vj_fnat m[1], const vj_fnat n[1], const double Ar[], const vj_fnat ldAr[1], const double Ai[],
+                const vj_fnat ldAi[1], double A[], const vj_fnat ldA[1])
+{
+  return merge_host<double>(*m, *n, Ar, *ldAr, Ai, *ldAi, A, *ldA);
+}
+
+vj_fint csplit_(const vj_fnat m[1], const vj_fnat n[1], const float A[], const vj_fnat ldA[1], float Ar[],
+                const vj_fnat ldAr[1], float Ai[], const vj_fnat ldAi[1])
+{
+  return split_host<float>(*m, *n, A, *ldA, Ar, *ldAr, Ai, *ldAi);
+}
+
+vj_fint cmerge_(const vj_fnat m[1], const vj_fnat n[1], const float Ar[], const vj_fnat ldAr[1], const float Ai[],
+                const vj_fnat ldAi[1], float A[], const vj_fnat ldA[1])
+{
+  return merge_host<float>(*m, *n, Ar, *ldAr, Ai, *ldAi, A, *ldA);
+}
 
 unsigned *pjs(long id, unsigned n, unsigned stp[1])
 {

@@ -7,7 +7,7 @@ project's portable norm (oracle/vjo_nrm2.h), which makes every output reproducib
 for bit by the C restatement and by the GPU library; mode 1 keeps the stock OpenBLAS
 norm and libm hypot, whose singular values are stored for tolerance checks.
 
-    python tests/golden/make_golden.py [--new]
+    python tests/golden/make_golden.py [--new | --split]
 """
 import os
 import sys
@@ -147,6 +147,38 @@ def svd_fixtures(ref, rst, only_new=False):
         print(name, "sweeps", r[0], "(stock BLAS norm:", out.get("blas_ret"), ")")
 
 
+def split_matrix(kind, m, n, seed):
+    """real and imaginary planes of an m x n complex matrix with special values (signed
+    zeros, infinities, a NaN with a payload) among random ones"""
+    rng = np.random.default_rng(seed)
+    dt = np.float64 if kind == "z" else np.float32
+    re, im = rng.standard_normal((m, n)).astype(dt), rng.standard_normal((m, n)).astype(dt)
+    sp = np.array([0.0, -0.0, np.inf, -np.inf, np.nan], dt)
+    re.flat[::7] = rng.choice(sp, re.flat[::7].size)
+    im.flat[3::11] = rng.choice(sp, im.flat[3::11].size)
+    nanp = np.array([0x7ff4000000000123 if kind == "z" else 0x7fa00123], np.uint64 if kind == "z" else np.uint32)
+    re.flat[5] = nanp.view(dt)[0]
+    return re, im
+
+
+def split_fixtures(ref):
+    """zsplit_/zmerge_ and csplit_/cmerge_ of the compiled reference"""
+    out = {}
+    for kind in "zc":
+        m, n = (24, 7) if kind == "z" else (48, 5)
+        re, im = split_matrix(kind, m, n, 31 + ord(kind))
+        # the interleaved input assembled from the planes' bits (complex arithmetic would not
+        # keep the NaN payloads)
+        Ai = np.empty((m, n), np.complex128 if kind == "z" else np.complex64)
+        Ai.real, Ai.imag = re, im
+        r, Ar, Aim = ref.split(kind, Ai)
+        q, B = ref.merge(kind, re, im)
+        out.update({f"{kind}_A": Ai, f"{kind}_re": re, f"{kind}_im": im, f"{kind}_split_ret": r,
+                    f"{kind}_Ar": np.array(Ar), f"{kind}_Ai": np.array(Aim), f"{kind}_merge_ret": q,
+                    f"{kind}_B": np.array(B)})
+    np.savez_compressed(os.path.join(HERE, "split_merge.npz"), **out)
+
+
 def main():
     """All fixtures; with --new only the SVD fixtures whose files do not exist yet."""
     O.build(ref=True)
@@ -155,6 +187,10 @@ def main():
     if "--new" in sys.argv[1:]:
         svd_fixtures(ref, rst, only_new=True)
         return
+    if "--split" in sys.argv[1:]:
+        split_fixtures(ref)
+        return
+    split_fixtures(ref)
     bjac2_fixtures(ref)
     bjac2_special_fixtures(ref)
     svd_fixtures(ref, rst)

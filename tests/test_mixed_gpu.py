@@ -78,6 +78,50 @@ def test_mixed_vs_oracle(vj, rst, kind, m, n):
     check_props(A, U, V, sig)
 
 
+@pytest.mark.parametrize("kind,m,n", [("d", 512, 256), ("z", 256, 128)])
+def test_mixed_relative_accuracy_vs_oracle(vj, rst, kind, m, n):
+    """The target accuracy of the mixed path: with a column-scaled condition number <= 1e3
+    (sigma log-uniform in [1e-3, 1], Haar factors, so every column mixes all of them) each
+    singular value is within 64 n eps RELATIVE of the FP64 oracle's (the reference's
+    algorithm in FP64, restated)."""
+    from vecjac_gb300 import workloads as W
+    A, _ = W.svd_matrix(m, n, seed=41 + n, lo=-3.0, complex_=(kind == "z"))
+    r, r32, U, V, sig = run_mixed(vj, kind, A)
+    assert r >= 0 and r32 > 0, (r, r32)
+    js, stp = rst.pjs(4, n)
+    ro = rst.vjsvd("z", A.real, js, stp, Gi=A.imag) if kind == "z" else rst.vjsvd("d", A, js, stp)
+    assert ro[0] >= 0
+    so = np.sort(ro[4] * np.exp2(ro[3]))
+    rel = np.max(np.abs(np.sort(sig) - so) / so)
+    assert rel <= 64 * n * EPS, rel
+    check_props(A, U, V, sig)
+
+
+@pytest.mark.parametrize("kind,m,n", [("d", 1024, 1024), ("z", 1024, 512)])
+def test_mixed_relative_accuracy_vs_plain(vj, kind, m, n):
+    """The same bound at larger sizes against the plain FP64 path, which computes the
+    reference's algorithm bit for bit (the FP64 oracle's result)."""
+    import torch
+    from vecjac_gb300 import workloads as W
+    A, _ = W.svd_matrix(m, n, seed=43 + n, lo=-3.0, complex_=(kind == "z"))
+    r, r32, U, V, sig = run_mixed(vj, kind, A)
+    assert r >= 0 and r32 > 0, (r, r32)
+    js, stp = vj.pjs(4, n)
+    G = torch.tensor(np.ascontiguousarray(A.real.T), dtype=torch.float64, device="cuda")
+    Gi = torch.tensor(np.ascontiguousarray(A.imag.T), dtype=torch.float64, device="cuda") if kind == "z" else None
+    Vd = torch.empty((n, n), dtype=torch.float64, device="cuda")
+    Vdi = torch.empty_like(Vd) if kind == "z" else None
+    eS = torch.empty(n, dtype=torch.float64, device="cuda")
+    fS = torch.empty_like(eS)
+    djs = torch.tensor(js.astype(np.int32), device="cuda")
+    rp = vj.vjsvd_dev(kind, m, n, G, m, Vd, n, eS, fS, djs, stp, Gi=Gi, ldGi=m, Vi=Vdi, ldVi=n)
+    torch.cuda.synchronize()
+    assert rp > 0
+    sp = np.sort(fS.cpu().numpy() * np.exp2(eS.cpu().numpy()))
+    rel = np.max(np.abs(np.sort(sig) - sp) / sp)
+    assert rel <= 64 * n * EPS, rel
+
+
 @pytest.mark.parametrize("kind,m,n", [("d", 1024, 512), ("z", 512, 256)])
 def test_mixed_large(vj, kind, m, n):
     from vecjac_gb300 import workloads as W

@@ -165,3 +165,16 @@ def test_reference_vs_restatement_bjac2(rst, kind):
         for x, y in zip(rr[1:], ro[1:]):
             x, y = np.ascontiguousarray(x), np.ascontiguousarray(y)
             assert np.array_equal(x.view(np.uint8), y.view(np.uint8)), (kind, sgn, internal)
+
+
+@pytest.mark.parametrize("kind", "zc")
+def test_split_merge_golden(rst, kind):
+    """zsplit_/zmerge_ (csplit_/cmerge_) of the restatement equal the compiled reference's
+    outputs bit for bit, signed zeros, infinities and a NaN payload included."""
+    g = np.load(os.path.join(GOLD, "split_merge.npz"))
+    r, Ar, Ai = rst.split(kind, g[kind + "_A"])
+    assert r == int(g[kind + "_split_ret"]) == 1
+    assert same_bits(Ar, g[kind + "_Ar"]) and same_bits(Ai, g[kind + "_Ai"])
+    q, B = rst.merge(kind, g[kind + "_re"], g[kind + "_im"])
+    assert q == int(g[kind + "_merge_ret"]) == 1
+    assert same_bits(B, g[kind + "_B"])

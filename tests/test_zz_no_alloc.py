@@ -1,8 +1,9 @@
 """The allocation-free SVD entry point (vj_dvjsvd_dev_noalloc) against the regular one.
 
-Some callers cannot allocate GPU memory while they run (for instance while a stream is
-being captured into a CUDA graph, or when their own pool owns the device); this entry
-point keeps its scratch in a fixed array inside the library instead. Two calls in a row
+Some callers cannot allocate GPU memory while they run (for instance when their own pool
+owns the device, or when a cudaMalloc, which can synchronise the device or fail for lack
+of memory, is not allowed in the middle of their work); this entry point keeps its scratch
+in a fixed array inside the library instead. Two calls in a row
 must each give exactly what vj_dvjsvd_dev gives for the same input, which also shows
 that the second call does not see the first call's leftovers in the shared array.
 """

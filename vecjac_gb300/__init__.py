@@ -8,6 +8,6 @@ There is no CPU fallback: when the library or a GPU is missing, calls raise.
 """
 from .api import (  # noqa: F401
     VJ_ERR_ARG, VJ_ERR_CUDA, VJ_ERR_NO_GPU, VJ_ERR_NOMEM, bjac2, bjac2_dev, last_mixed_phases, last_trace, lib, lib_path,
-    pjs, pjs_dev,
+    merge, merge_dev, pjs, pjs_dev, split, split_dev,
     vjsvd, vjsvd_dev, vjsvd_mixed_dev,
 )

@@ -44,7 +44,8 @@ def lib():
                      "svjsvd_", "cvjsvd_", "vj_dvjsvd_dev", "vj_zvjsvd_dev", "vj_svjsvd_dev", "vj_cvjsvd_dev",
                      "vj_pjs_dev", "vj_dvjsvd_mixed_dev", "vj_zvjsvd_mixed_dev",
                      "vj_ssvd_adjoint_batch_dev", "vj_dsvd_adjoint_batch_dev", "vj_dvjsvd_batch_dev",
-                     "vj_svjsvd_batch_dev", "vj_last_mixed_phases"):
+                     "vj_svjsvd_batch_dev", "vj_last_mixed_phases", "zsplit_", "zmerge_", "csplit_", "cmerge_",
+                     "vj_zsplit_dev", "vj_zmerge_dev", "vj_csplit_dev", "vj_cmerge_dev"):
             if hasattr(_LIB, name):
                 getattr(_LIB, name).restype = _ll
         if hasattr(_LIB, "pjs"):
@@ -177,6 +178,50 @@ def vjsvd_mixed_dev(kind, m, n, G, ldG, V, ldV, eS, fS, js, stp, swp=999, Gi=Non
         r = f(_ull(m), _ull(n), _p(G), _ull(ldG), _p(V), _ull(ldV), _p(eS), _p(fS), _p(js), C.c_uint(int(stp)),
               C.c_uint(int(swp)), C.c_uint(int(stages)), pre, s)
     return r, pre[0], pre[1]
+
+
+def split(kind, A, Ar=None, Ai=None):
+    """Host call of zsplit_ (kind "z") or csplit_ ("c") on a Fortran-ordered complex matrix.
+    Returns (ret, Ar, Ai), the planes Fortran-ordered with leading dimension m."""
+    L = lib()
+    dt = _dtype(kind)
+    A = np.asfortranarray(A, np.complex128 if kind == "z" else np.complex64)
+    m, n = A.shape
+    Ar = np.empty((m, n), dt, order="F") if Ar is None else Ar
+    Ai = np.empty((m, n), dt, order="F") if Ai is None else Ai
+    mm, nn = _ull(m), _ull(n)
+    r = getattr(L, kind + "split_")(C.byref(mm), C.byref(nn), _p(A), C.byref(mm), _p(Ar), C.byref(mm), _p(Ai),
+                                    C.byref(mm))
+    return r, Ar, Ai
+
+
+def merge(kind, Ar, Ai, A=None):
+    """Host call of zmerge_ / cmerge_: two Fortran-ordered planes into an interleaved complex
+    matrix. Returns (ret, A)."""
+    L = lib()
+    dt = _dtype(kind)
+    Ar = np.asfortranarray(Ar, dt)
+    Ai = np.asfortranarray(Ai, dt)
+    m, n = Ar.shape
+    A = np.empty((m, n), np.complex128 if kind == "z" else np.complex64, order="F") if A is None else A
+    mm, nn = _ull(m), _ull(n)
+    r = getattr(L, kind + "merge_")(C.byref(mm), C.byref(nn), _p(Ar), C.byref(mm), _p(Ai), C.byref(mm), _p(A),
+                                    C.byref(mm))
+    return r, A
+
+
+def split_dev(kind, m, n, A, ldA, Ar, ldAr, Ai, ldAi, stream=None):
+    """vj_zsplit_dev / vj_csplit_dev on CUDA tensors (A interleaved, ldA in complex elements)."""
+    s = C.c_void_p(stream) if stream else None
+    return getattr(lib(), "vj_%ssplit_dev" % kind)(_ull(m), _ull(n), _p(A), _ull(ldA), _p(Ar), _ull(ldAr), _p(Ai),
+                                                   _ull(ldAi), s)
+
+
+def merge_dev(kind, m, n, Ar, ldAr, Ai, ldAi, A, ldA, stream=None):
+    """vj_zmerge_dev / vj_cmerge_dev on CUDA tensors."""
+    s = C.c_void_p(stream) if stream else None
+    return getattr(lib(), "vj_%smerge_dev" % kind)(_ull(m), _ull(n), _p(Ar), _ull(ldAr), _p(Ai), _ull(ldAi), _p(A),
+                                                   _ull(ldA), s)
 
 
 def pjs(sid, n):

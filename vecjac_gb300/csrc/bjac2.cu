@@ -7,6 +7,7 @@
 // its lanes with vj::rjac2/cjac2, and the quad ORs its permutation bits into the
 // group's word with two xor-shuffles. The grid is a multiple of the SM count and
 // strides over the arrays, so every byte of HBM is touched exactly once.
+#include <cfenv>
 #include <cuda_runtime.h>
 
 #include "jac2.cuh"
@@ -141,6 +142,10 @@ static vj_fint bjac2_host(vj_fint n, int internal, const T *a11, const T *a22, c
                           T *cat, T *sat, T *l1, T *l2, unsigned *p)
 {
   constexpr int LANES = grp<T>::LANES;
+  // the reference's first check (IS_NOT_VFPENV, src/dbjac2.c:84, src/zbjac2.c:111): the
+  // calling thread must round to nearest; -10 for real, -12 for complex data
+  if (fegetround() != FE_TONEAREST)
+    return CPLX ? -12 : -10;
   if (n % LANES)
     return -1;
   if (!host::gpu_ready())

@@ -19,12 +19,18 @@ bool gpu_ready()
 
 int sm_count()
 {
-  static int n = 0;
+  // per device: a process may drive GPUs of different sizes (grids are sized for the
+  // current device of each call)
+  static int cnt[64] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0)
+    dev = 0;
+  int &n = cnt[dev & 63];
   if (!n) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || n <= 0)
-      n = 1;
+    int v = 0;
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0)
+      v = 1;
+    n = v;
   }
   return n;
 }

@@ -808,9 +808,10 @@ vj_fint vj_cvjsvd_dev(vj_fnat m, vj_fnat n, float *Gr, vj_fnat ldGr, float *Gi, 
 }  // extern "C"
 
 // ---------------- allocation-free FP64 SVD ----------------
-// Callers that cannot allocate device memory at run time (code running inside a stream
-// being captured into a CUDA graph, or an application that owns every byte of the GPU
-// through its own pool and forbids library allocations) can still run the SVD through
+// Callers that cannot allocate device memory at run time (an application that owns every
+// byte of the GPU through its own pool and forbids library allocations, or a latency-bound
+// service that must not take the driver's allocator -- cudaMalloc can synchronise the device
+// and fail with out-of-memory in the middle of a pipeline) can still run the SVD through
 // vj_dvjsvd_dev_noalloc. It needs no table and no scratch from the caller: its scratch --
 // the control block of the call, the max |a_ij| cell and the pivot table it generates on
 // the GPU -- lives in the file-scope device array below, 1 MiB + 512 bytes that every GPU

@@ -199,23 +199,31 @@ vj_fint svd_call(vj_fnat m, vj_fnat n, T *Gr, vj_fnat ldGr, T *Gi, vj_fnat ldGi,
 #endif
 }
 
-// interleaved complex (re, im pairs, leading dimension ld in complex elements) <-> planes
-void split(vj_fnat m, vj_fnat n, const T *A, vj_fnat ld, T *Ar, T *Ai, vj_fnat ldp)
+// interleaved complex (re, im pairs, leading dimension ld in complex elements) <-> planes,
+// through the library's zsplit_/zmerge_ (csplit_/cmerge_), as the reference's complex
+// drivers call its own (src/tzvjsvd.c:69,137,163)
+vj_fint split(vj_fnat m, vj_fnat n, const T *A, vj_fnat ld, T *Ar, T *Ai, vj_fnat ldp)
 {
-  for (vj_fnat j = 0; j < n; ++j)
-    for (vj_fnat i = 0; i < m; ++i) {
-      Ar[j * ldp + i] = A[2 * (j * ld + i)];
-      Ai[j * ldp + i] = A[2 * (j * ld + i) + 1];
-    }
+#if VJ_CLI_KIND == 'z'
+  return zsplit_(&m, &n, A, &ld, Ar, &ldp, Ai, &ldp);
+#elif VJ_CLI_KIND == 'c'
+  return csplit_(&m, &n, A, &ld, Ar, &ldp, Ai, &ldp);
+#else
+  (void)m, (void)n, (void)A, (void)ld, (void)Ar, (void)Ai, (void)ldp;
+  return -1;
+#endif
 }
 
-void merge(vj_fnat m, vj_fnat n, const T *Ar, const T *Ai, vj_fnat ldp, T *A, vj_fnat ld)
+vj_fint merge(vj_fnat m, vj_fnat n, const T *Ar, const T *Ai, vj_fnat ldp, T *A, vj_fnat ld)
 {
-  for (vj_fnat j = 0; j < n; ++j)
-    for (vj_fnat i = 0; i < m; ++i) {
-      A[2 * (j * ld + i)] = Ar[j * ldp + i];
-      A[2 * (j * ld + i) + 1] = Ai[j * ldp + i];
-    }
+#if VJ_CLI_KIND == 'z'
+  return zmerge_(&m, &n, Ar, &ldp, Ai, &ldp, A, &ld);
+#elif VJ_CLI_KIND == 'c'
+  return cmerge_(&m, &n, Ar, &ldp, Ai, &ldp, A, &ld);
+#else
+  (void)m, (void)n, (void)Ar, (void)Ai, (void)ldp, (void)A, (void)ld;
+  return -1;
+#endif
 }
 
 // the whole file of a real (CPLX false: E = T) or complex (E = 2 T per element) matrix
@@ -294,7 +302,8 @@ int main(int argc, char *argv[])
     if (!Gr || !Gi)
       return 6;
     const auto t0 = std::chrono::steady_clock::now();
-    split(m, n, G, ldG, Gr, Gi, ldG);
+    if (split(m, n, G, ldG, Gr, Gi, ldG) < 0)
+      return 6;
     ts = seconds_since(t0);
   }
   Vr = alloc<T>((size_t)ldV * n);
@@ -362,13 +371,15 @@ int main(int argc, char *argv[])
     if (!V)
       return 11;
     auto t2 = std::chrono::steady_clock::now();
-    merge(n, n, Vr, Vi, ldV, V, ldV);
+    if (merge(n, n, Vr, Vi, ldV, V, ldV) < 0)
+      return 11;
     tv = seconds_since(t2);
     if (!write_matrix(bn, (std::string("V") + tag).c_str(), n, n, V, ldV))
       return 12;
     free(V);
     t2 = std::chrono::steady_clock::now();
-    merge(m, n, Gr, Gi, ldG, G, ldG);
+    if (merge(m, n, Gr, Gi, ldG, G, ldG) < 0)
+      return 13;
     tg = seconds_since(t2);
     if (!write_matrix(bn, (std::string("U") + tag).c_str(), m, n, G, ldG))
       return 14;
