@@ -178,7 +178,7 @@ class Batch:
 BJAC2_INST_PER_ELEM = {"d": 1243.0, "z": 1946.0}
 # thread instructions per element that execute on the FP64 pipe (ncu
 # smsp__inst_executed_pipe_fp64.sum x 32 / elements; profile summary k_bjac2_fp64_pipe_2e24)
-BJAC2_FP64_PIPE_PER_ELEM = {"d": None, "z": None}
+BJAC2_FP64_PIPE_PER_ELEM = {"d": 15728640 * 32 / 2 ** 24, "z": 16515072 * 32 / 2 ** 23}
 # DRAM bytes (read + write) of one 2^24-element real FP64 launch, from the same capture
 BJAC2_D_DRAM_2E24 = 402.791680e6 + 487.371776e6
 # the reference's own AVX-512 dbjac2_/zbjac2_ (src/dbjac2.c, src/zbjac2.c, compiled from its
@@ -465,11 +465,6 @@ def reference_arm(args, dist, rank):
 
 
 # ---------------------------------------------------------------- SVD workloads
-# DRAM bytes (read + write) of one FP32 presweep step of the complex 4096x2048 mixed SVD
-# (ncu dram__bytes_read.sum + dram__bytes_write.sum; the profile summary
-# mixed_zsvd4096x2048_kernels_full)
-MIXED_F32_STEP_DRAM = 100.695296e6 + 39.812864e6
-
 def svd_roofline(flops_per_s, fp64, kernel, dev=None):
     """Roofline object for the Jacobi SVD workloads: algorithmic FLOP rate (12m + 6n real,
     36m + 20n complex per pair and sweep) against the FMA pipe's peak, measured live on this
@@ -558,8 +553,9 @@ def svd_case(args, vj, dist, kind, m, n, lo, mixed_steps, plain_steps, warmup, s
     sig_m, err_m = results()
     out["mixed"] = dict({"ms_per_matrix": round(ms, 2), "matrices_per_s": round(1000.0 / ms, 4),
                          "steps": mixed_steps, "sweeps_fp32": int(sw32), "sweeps_fp64_plain_dot": int(swf),
-                         "sweeps_fp64_reference": int(sw),
-                         "phases_ms": {k: round(v, 1) for k, v in ph.items() if k.endswith("_ms")}}, **err_m)
+                         "sweeps_fp64_reference": int(sw), "fp32_block_sweeps": ph.get("fp32_block_sweeps"),
+                         "phases_ms": {k: round(v, 1) for k, v in ph.items() if k.endswith("_ms")},
+                         "fp32_roofline": mixed_fp32_roofline(ph, kind, m, n, int(sw32))}, **err_m)
     if plain_steps > 0:
         pms, psw = timed(plain, plain_steps)
         sig_p, err_p = results()
@@ -753,22 +749,7 @@ def bench_mixed(args, vj, dist, rank, world, kind, m, n):
                       "max_rel_sigma_err_vs_exact": rel_m, "max_sigma_err_over_sigma_max": nrm_m},
            "phases_ms": {k: round(v, 1) for k, v in phases.items() if k.endswith("_ms")},
            "clocks": clk.summary()}
-    # roofline of the FP32 stage's step kernel: every step reads and writes the columns of
-    # G and of the rotation accumulator W once (FP32, split planes)
-    pk, src = peaks()
-    P = 2 if cx else 1
-    step_bytes = 2.0 * P * 4 * (m * n + n * n)
-    if phases["fp32_ms"] > 0 and phases["fp32_steps"] > 0:
-        ach = step_bytes * phases["fp32_steps"] / (phases["fp32_ms"] * 1e-3) / 1e9
-        # DRAM bytes of one complex 4096x2048 step (ncu), scaled by the size of G and W
-        traffic = MIXED_F32_STEP_DRAM * (m * n + n * n) / (4096 * 2048 + 2048 * 2048) * (P / 2.0)
-        out["roofline"] = {"bound": "hbm", "kernel": "k_presweep_reg<float> (FP32 stages)", "achieved": round(ach, 1),
-                           "peak": pk["hbm_gbs"], "unit": "GB/s", "frac": round(ach / pk["hbm_gbs"], 4),
-                           "traffic": round(traffic), "peak_source": src,
-                           "note": "algorithmic bytes: G and W columns read and written once per step (%d per "
-                                   "step); where the 2 x FP32 copy of G and W fits partly in L2 the DRAM traffic is "
-                                   "lower (traffic, from ncu) and the fraction can exceed 1. The FP64 phases are "
-                                   "FP64-pipe bound." % step_bytes}
+    out["roofline"] = mixed_fp32_roofline(phases, kind, m, n, int(sw32))
     if args.plain_steps > 0:
         pms, psw = timed(plain, args.plain_steps)
         sig_p, rel_p, nrm_p = sigma_err()
@@ -779,6 +760,28 @@ def bench_mixed(args, vj, dist, rank, world, kind, m, n):
         if rank == 0 and args.cpu_baseline:
             out["cpu_baseline"] = cpu_baseline_svd(kind, A, js, stp, int(psw))
     return out
+
+
+def mixed_fp32_roofline(phases, kind, m, n, sweeps32):
+    """Tensor-pipe roofline of the FP32 stages of the mixed SVD when they ran as block sweeps:
+    the split-BF16x3 products of every block step (per block pair: the 128 x 128 Gram matrix
+    over m rows, and the rotation of m + n rows of 128 columns, each 2 x 128 x 128 flops per
+    row and term) over the whole FP32 phase time (which includes the pair eigenproblems on
+    the CUDA cores), against the measured BF16 peak. None for column-pair sweeps (their
+    operands live in L2: no HBM or tensor roofline applies)."""
+    if not (phases.get("fp32_block_sweeps") and phases["fp32_ms"] > 0 and sweeps32 > 0):
+        return None
+    pk, src = peaks()
+    terms = 3 if os.environ.get("VJ_BLOCK_TERMS") == "3" else 6
+    nb = n // (32 if kind == "z" else 64)
+    flops = sweeps32 * (nb - 1) * (nb // 2) * 2.0 * 128 * 128 * (2 * m + n) * terms
+    ach = flops / (phases["fp32_ms"] * 1e-3) / 1e12
+    peak = pk.get("bf16_tflops_sustained") or pk["bf16_tflops"]
+    return {"bound": "tensor", "kernel": "k_gram + k_apply (split-BF16x3 tcgen05, %d terms)" % terms,
+            "achieved": round(ach, 2), "peak": peak, "unit": "TFLOP/s", "frac": round(ach / peak, 4),
+            "traffic": None, "peak_source": src + " (bf16 sustained)",
+            "note": "BF16 tensor flops of the Gram and rotation products over the whole FP32 phase, pair "
+                    "eigenproblems and launch gaps included"}
 
 
 def bench_diff(args, vj, dist, rank, world):

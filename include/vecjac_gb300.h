@@ -142,11 +142,41 @@ vj_fint vj_zvjsvd_mixed_dev(vj_fnat m, vj_fnat n, double *Gr, vj_fnat ldGr, doub
                             vj_fnat ldVr, double *Vi, vj_fnat ldVi, double *eS, double *fS, const unsigned *js,
                             unsigned stp, unsigned swp, unsigned stages, unsigned *presweeps, void *stream);
 
+/* Block one-sided Jacobi in FP32 with split-BF16x3 tensor-core products (tcgen05, FP32
+ * accumulation): the FP32 stages of the mixed-precision SVD, and its building blocks. No
+ * counterpart in the reference (whose FP32 SVDs rotate column pairs, src/svjsvd.c,
+ * src/cvjsvd.c). G (m x n) and W (n x n) are FP32, column-major, split planes for complex
+ * data (cplx != 0; Gi, Wi NULL for real data). The columns are cut into blocks of 64 (real)
+ * or 32 (complex) columns, so a pair of blocks is 128 real columns X = [G_I G_J] (complex:
+ * [Re G_I Re G_J Im G_I Im G_J]); the pairs of block step `step` (0 .. n/b - 2) are those of
+ * the round-robin ordering of the n/b blocks (pair k: blocks (step, n/b - 1) for k = 0, else
+ * ((step + k) mod (n/b - 1), (step - k) mod (n/b - 1)), lower index first). Requirements:
+ * n a multiple of 128 (real) / 64 (complex), m and the leading dimensions multiples of 4,
+ * columns 16-byte aligned; otherwise VJ_ERR_ARG. terms: 6 (products as accurate as FP32)
+ * or 3 (h h + h m + m h, about 16 bits).
+ * vj_block_gram_dev: S (n/b/2 x 128 x 128, row-major per pair) = X^T X for every pair of
+ *   the step. Returns the number of pairs. Synchronous.
+ * vj_block_apply_dev: X := X R for the rows of G and of W, R (n/b/2 x 128 x 128, pair k's
+ *   R[k][i] at R + k 16384 + k + 128 i) the real form of each pair's rotation (complex:
+ *   [[Re R, Im R], [-Im R, Re R]]). Returns the number of pairs. Synchronous.
+ * vj_block_sweep_dev: one block sweep (every block pair once): per pair the Gram matrix,
+ *   `inner` cyclic Jacobi sweeps on its 2b x 2b Hermitian form (rotations where
+ *   |h_pq| >= tol sqrt(h_pp h_qq)), columns ordered by descending norms, and the
+ *   rotation applied to G and W. Returns the number of rotations (0: converged to tol) and
+ *   the largest |h_pq| / sqrt(h_pp h_qq) of a rotated pair in *mu, or a VJ_ERR_* code. */
+vj_fint vj_block_gram_dev(int cplx, vj_fnat m, vj_fnat n, const float *Gr, const float *Gi, vj_fnat ldG, int step,
+                          int terms, float *S, void *stream);
+vj_fint vj_block_apply_dev(int cplx, vj_fnat m, vj_fnat n, float *Gr, float *Gi, vj_fnat ldG, float *Wr, float *Wi,
+                           vj_fnat ldW, int step, int terms, const float *R, void *stream);
+vj_fint vj_block_sweep_dev(int cplx, vj_fnat m, vj_fnat n, float *Gr, float *Gi, vj_fnat ldG, float *Wr, float *Wi,
+                           vj_fnat ldW, float tol, int inner, int terms, float *mu, void *stream);
+
 /* Phase times of the last vj_?vjsvd_mixed_dev call on this process, in milliseconds:
  * out[0] FP32 sweeps, out[1] Newton-Schulz steps and GEMMs, out[2] plain-dot FP64 sweeps
  * and the column sort, out[3] the reference's finishing sweeps; out[4] the number of FP32
- * step launches. */
-vj_fint vj_last_mixed_phases(double out[5]);
+ * kernel launches; out[5] 1 when the FP32 stages ran as block sweeps on the tensor cores,
+ * 0 for column-pair sweeps. */
+vj_fint vj_last_mixed_phases(double out[6]);
 
 /* Adjoint of the thin SVD A = U diag(S) V^T (m >= n, V square), batched over `count`
  * matrices of one shape: given the cotangents dS (n), dU (m x k) and dV (n x k) of S and of

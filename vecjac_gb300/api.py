@@ -251,11 +251,12 @@ PHASES = ("control", "staging", "dots", "2x2", "rotations", "norms")
 
 def last_mixed_phases():
     """Phase times (ms) of the last mixed-precision SVD: FP32 sweeps, Newton-Schulz + GEMMs,
-    plain FP64 sweeps + sort, the reference's finishing sweeps; and the FP32 step launches."""
-    out = (C.c_double * 5)()
+    plain FP64 sweeps + sort, the reference's finishing sweeps; the FP32 kernel launches and
+    whether the FP32 stages ran as block sweeps on the tensor cores."""
+    out = (C.c_double * 6)()
     lib().vj_last_mixed_phases(out)
     return {"fp32_ms": out[0], "gemm_ms": out[1], "fp64_plain_ms": out[2], "finish_ms": out[3],
-            "fp32_steps": int(out[4])}
+            "fp32_launches": int(out[4]), "fp32_block_sweeps": bool(out[5])}
 
 
 def last_trace():

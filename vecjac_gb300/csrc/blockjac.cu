@@ -1,0 +1,838 @@
+// Block one-sided Jacobi sweeps in FP32 with the block rotations on the tensor cores
+// (split-BF16x3 products, FP32 accumulation): the FP32 stages of the mixed-precision SVD.
+//
+// The n columns of the FP32 matrix G (m x n, split real/imaginary planes) and of the
+// rotation accumulator W (n x n) are cut into blocks of b columns (b = 64 real, 32
+// complex, so that a block pair is 128 real columns: [G_I G_J], or [Re G_I Re G_J Im G_I
+// Im G_J]). A block sweep visits every pair of blocks once in the round-robin order, n/b/2
+// independent pairs per block step, and for each pair
+//   1. k_gram:  S = X^T X, the real Gram matrix of the pair's 128 real columns X (128 x 128,
+//      K = m, split over several CTAs), on the tensor cores;
+//   2. k_pair_evd: the Hermitian Gram matrix H = [G_I G_J]^H [G_I G_J] (from S), one cyclic
+//      two-sided Jacobi sweep on H that accumulates the unitary R (2b x 2b) -- in exact
+//      arithmetic the rotations of one-sided Jacobi on the pair's columns, from the same
+//      2x2 Gram blocks, with the same threshold -- and a reordering of R's columns by
+//      descending norms (the block form of the scalar sweep's swap rule);
+//   3. k_apply: [G_I G_J] := [G_I G_J] R and [W_I W_J] := [W_I W_J] R on the tensor cores
+//      (the real 128 x 128 form of R for complex data: [[Re R, Im R], [-Im R, Re R]]).
+// Each FP32 operand x is split into three BF16 terms x = h + m + l (exactly: 8 + 8 + 8
+// significant bits) and a product is formed from the six terms h h, h m, m h, h l, m m,
+// l h (the dropped ones are below 2^-24 relative), accumulated in FP32 in TMEM: the
+// accuracy of an FP32 product at tensor-core speed. Operands are converted from FP32 to
+// the split BF16 tiles by the CTA's threads (the A side) or copied by the bulk-copy TMA
+// engine from the split image that k_pair_evd writes (the R side of k_apply).
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <vector>
+
+#include "svd_core.cuh"
+#include "tc.cuh"
+#include "vj_host.h"
+
+namespace vj {
+namespace bj {
+
+constexpr int TILE = 128;                 // real columns of a block pair = rows of a GEMM tile
+constexpr int KC = 64;                    // K elements of one operand stage
+constexpr int LBO = 128;                  // bytes between core matrices adjacent in K
+constexpr int SBO = (KC / 8) * 128;       // bytes between groups of 8 rows
+constexpr int PLANE = TILE * KC * 2;      // bytes of one BF16 term of a 128 x 64 stage tile
+constexpr uint32_t IDESC = tc::idesc_bf16<TILE, TILE>::value;
+constexpr long long WAIT_CYCLES = 4000000000LL;  // ~2 s at 2 GHz: a wait that long has failed
+
+// terms of the split product, smallest first: (A term, B term), 0 = h, 1 = m, 2 = l
+__constant__ int TA[6] = {2, 1, 0, 1, 0, 0};
+__constant__ int TB[6] = {0, 1, 2, 0, 1, 0};
+
+// byte offset of element (row r, k) in a K-major tile without swizzle
+__device__ __forceinline__ int tile_off(int r, int k)
+{
+  return (r >> 3) * SBO + (k >> 3) * LBO + (r & 7) * 16 + (k & 7) * 2;
+}
+
+// x = h + m + l exactly, each a BF16 (FP32 inputs of normal or zero magnitude)
+__device__ __forceinline__ void split3(float x, __nv_bfloat16 &h, __nv_bfloat16 &m, __nv_bfloat16 &l)
+{
+  h = __float2bfloat16_rn(x);
+  const float r1 = x - __bfloat162float(h);
+  m = __float2bfloat16_rn(r1);
+  const float r2 = r1 - __bfloat162float(m);
+  l = __float2bfloat16_rn(r2);
+}
+
+// the three BF16 terms of 8 values, stored as 16 bytes each at p0, p0 + PLANE, p0 + 2 PLANE
+__device__ __forceinline__ void store_split8(unsigned char *p0, const float (&v)[8])
+{
+  __align__(16) __nv_bfloat16 t[3][8];
+#pragma unroll
+  for (int e = 0; e < 8; ++e)
+    split3(v[e], t[0][e], t[1][e], t[2][e]);
+#pragma unroll
+  for (int s = 0; s < 3; ++s)
+    *reinterpret_cast<uint4 *>(p0 + s * PLANE) = *reinterpret_cast<const uint4 *>(t[s]);
+}
+
+// planar FP32 matrix and the block layout of its columns
+struct Cols {
+  float *re, *im;  // im == nullptr for real data
+  long long ld;
+  int b;  // columns per block: 64 (real) or 32 (complex)
+};
+
+// real column c (0..127) of the block pair (I, J): complex data put the real parts of the
+// pair's 2b columns first, then their imaginary parts
+__device__ __forceinline__ float *pair_col(const Cols &X, int I, int J, int c)
+{
+  const bool cx = X.im != nullptr;
+  const int h = cx ? (c & 63) : c;
+  float *base = (cx && c >= 64) ? X.im : X.re;
+  const int col = (h < X.b) ? (I * X.b + h) : (J * X.b + (h - X.b));
+  return base + (long long)col * X.ld;
+}
+
+// block pair k of block step s of the round-robin ordering of nb blocks (I < J)
+__device__ __forceinline__ void block_pair(int nb, int s, int k, int &I, int &J)
+{
+  const int N = nb - 1;
+  int a, c;
+  if (k == 0) {
+    a = s;
+    c = N;
+  }
+  else {
+    a = (s + k) % N;
+    c = (s + N - k) % N;
+  }
+  I = a < c ? a : c;
+  J = a < c ? c : a;
+}
+
+// ---------------------------------------------------------------- Gram matrices
+// CTA (pair, split): S_part = X[k0:k1]^T X[k0:k1] for the pair's 128 real columns, rows
+// k0..k1 of this split. 128 threads: thread t converts real column t; thread 0 issues the
+// MMAs. Two operand stages (A = B: the Gram tile is its own B operand), 96 KiB.
+template <int NT>
+__global__ void __launch_bounds__(128) k_gram(Cols X, int m, int nb, int step, int ksplit, float *Spart,
+                                               unsigned *err)
+{
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  unsigned char *smem = smem_raw + ((1024u - (tc::saddr(smem_raw) & 1023u)) & 1023u);
+  __shared__ unsigned long long bar[2];
+  __shared__ uint32_t tslot;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const int pair = blockIdx.x / ksplit, ks = blockIdx.x % ksplit;
+  int I, J;
+  block_pair(nb, step, pair, I, J);
+  const int nch_all = (m + KC - 1) / KC;
+  const int per = (nch_all + ksplit - 1) / ksplit;
+  const int c0 = ks * per;
+  const int nch = (nch_all - c0 < per) ? ((nch_all - c0 > 0) ? nch_all - c0 : 0) : per;
+  if (tid == 0) {
+    tc::mbar_init1(&bar[0]);
+    tc::mbar_init1(&bar[1]);
+    tc::mbar_init_fence();
+  }
+  __syncwarp();
+  if (warp == 0)
+    tc::tmem_alloc(&tslot, TILE);
+  tc::fence_before();
+  __syncthreads();
+  tc::fence_after();
+  const uint32_t tmem = tslot;
+  const float *col = pair_col(X, I, J, tid);
+  bool ok = true;
+  int issued = 0;  // chunks whose MMAs were issued
+  for (int it = 0; it < nch; ++it) {
+    const int s = it & 1;
+    unsigned char *st = smem + s * 3 * PLANE;
+    // the MMAs of chunk it - 2 have read stage s; a wait that gives up ends the loop for
+    // the whole CTA (nothing more is issued)
+    const bool w = (it >= 2) ? tc::mbar_wait(&bar[s], (uint32_t)(((it >> 1) - 1) & 1), WAIT_CYCLES) : true;
+    if (!__syncthreads_and(w)) {
+      ok = false;
+      break;
+    }
+    const int k0 = (c0 + it) * KC;
+#pragma unroll 2
+    for (int g = 0; g < KC / 8; ++g) {
+      const int r = k0 + 8 * g;
+      float v[8];
+      if (r + 8 <= m) {
+        const float4 a = *reinterpret_cast<const float4 *>(col + r);
+        const float4 c = *reinterpret_cast<const float4 *>(col + r + 4);
+        v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+        v[4] = c.x; v[5] = c.y; v[6] = c.z; v[7] = c.w;
+      }
+      else {
+#pragma unroll
+        for (int e = 0; e < 8; ++e)
+          v[e] = (r + e < m) ? col[r + e] : 0.f;
+      }
+      store_split8(st + tile_off(tid, 8 * g), v);
+    }
+    tc::fence_proxy_async();
+    __syncthreads();
+    if (tid == 0) {
+      tc::fence_after();
+      const uint32_t a0 = tc::saddr(st);
+#pragma unroll
+      for (int kk = 0; kk < KC / 16; ++kk)
+#pragma unroll
+        for (int t = 6 - NT; t < 6; ++t) {
+          const uint64_t ad = tc::sdesc(a0 + TA[t] * PLANE + kk * 2 * LBO, LBO, SBO);
+          const uint64_t bd = tc::sdesc(a0 + TB[t] * PLANE + kk * 2 * LBO, LBO, SBO);
+          tc::mma_bf16(tmem, ad, bd, IDESC, (it > 0 || kk > 0 || t > 6 - NT) ? 1u : 0u);
+        }
+      tc::commit(&bar[s]);
+    }
+    issued = it + 1;
+  }
+  // every issued chunk complete (commits complete in order; a second bounded wait after a
+  // failed one, so that no MMA is in flight when the TMEM is released)
+  for (int rep = 0; rep < 2 && issued >= 1; ++rep) {
+    bool w = tc::mbar_wait(&bar[(issued - 1) & 1], (uint32_t)(((issued - 1) >> 1) & 1), WAIT_CYCLES);
+    if (issued >= 2)
+      w = tc::mbar_wait(&bar[(issued - 2) & 1], (uint32_t)(((issued - 2) >> 1) & 1), WAIT_CYCLES) && w;
+    if (w)
+      break;
+    ok = false;
+  }
+  tc::fence_after();
+  __syncwarp();
+  float4 *out = reinterpret_cast<float4 *>(Spart + (size_t)blockIdx.x * TILE * TILE + (size_t)tid * TILE);
+  if (nch == 0) {
+    for (int c = 0; c < TILE / 4; ++c)
+      out[c] = make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+  else {
+#pragma unroll 1
+    for (int c = 0; c < TILE; c += 32) {
+      uint32_t r[32];
+      tc::tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c, r);
+#pragma unroll
+      for (int e = 0; e < 8; ++e)
+        out[c / 4 + e] = make_float4(__uint_as_float(r[4 * e]), __uint_as_float(r[4 * e + 1]),
+                                     __uint_as_float(r[4 * e + 2]), __uint_as_float(r[4 * e + 3]));
+    }
+  }
+  if (!ok)
+    atomicOr(err, 1u);
+  tc::fence_before();
+  __syncthreads();
+  tc::fence_after();
+  __syncwarp();
+  if (warp == 0)
+    tc::tmem_dealloc(tmem, TILE);
+}
+
+// ---------------------------------------------------------------- block rotations
+// CTA (pair, row tile): rows r0..r0+127 of the pair's 128 real columns of G (tiles
+// 0..tg-1) or of W (tiles tg..): Y = X R with R's split image (2 K stages x 3 terms of
+// 128 x 64 BF16, 96 KiB per pair) copied in by TMA, X converted by the threads; Y replaces
+// X in place (each CTA reads all of its tile before any of it is written).
+template <int NT>
+__global__ void __launch_bounds__(128) k_apply(Cols G, int m, Cols W, int n, int nb, int step, int tg, int tw,
+                                                const unsigned char *Rimg, unsigned *err)
+{
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  unsigned char *smem = smem_raw + ((1024u - (tc::saddr(smem_raw) & 1023u)) & 1023u);
+  __shared__ unsigned long long bar[2];  // 0: TMA of R, 1: MMA completion
+  __shared__ uint32_t tslot;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const int per_pair = tg + tw;
+  const int pair = blockIdx.x / per_pair, tile = blockIdx.x % per_pair;
+  const bool onG = tile < tg;
+  const Cols &X = onG ? G : W;
+  const int rows = onG ? m : n;
+  const int r0 = (onG ? tile : tile - tg) * TILE;
+  int I, J;
+  block_pair(nb, step, pair, I, J);
+  // smem: stage s at s * 6 PLANE: A terms (3 PLANE), then R terms (3 PLANE)
+  if (tid == 0) {
+    tc::mbar_init1(&bar[0]);
+    tc::mbar_init1(&bar[1]);
+    tc::mbar_init_fence();
+  }
+  __syncwarp();
+  if (warp == 0)
+    tc::tmem_alloc(&tslot, TILE);
+  tc::fence_before();
+  __syncthreads();
+  tc::fence_after();
+  const uint32_t tmem = tslot;
+  if (tid == 0) {
+    mbar_expect_tx(&bar[0], 6u * PLANE);
+    const unsigned char *src = Rimg + (size_t)pair * 6 * PLANE;
+    tma_load_1d(smem + 3 * PLANE, src, 3u * PLANE, &bar[0]);
+    tma_load_1d(smem + 9 * PLANE, src + 3 * PLANE, 3u * PLANE, &bar[0]);
+  }
+  const int row = r0 + tid;
+  const bool live = row < rows;
+#pragma unroll 1
+  for (int s = 0; s < 2; ++s) {
+    unsigned char *st = smem + s * 6 * PLANE;
+#pragma unroll 1
+    for (int g = 0; g < KC / 8; ++g) {
+      float v[8];
+#pragma unroll
+      for (int e = 0; e < 8; ++e)
+        v[e] = live ? pair_col(X, I, J, s * KC + 8 * g + e)[row] : 0.f;
+      store_split8(st + tile_off(tid, 8 * g), v);
+    }
+  }
+  tc::fence_proxy_async();
+  __syncthreads();
+  bool ok = true;
+  if (tid == 0) {
+    ok = tc::mbar_wait(&bar[0], 0u, WAIT_CYCLES);
+    if (!ok)  // the copy did not arrive: wait once more so that it is not in flight at exit
+      tc::mbar_wait(&bar[0], 0u, WAIT_CYCLES);
+    tc::fence_after();
+#pragma unroll 1
+    for (int s = 0; s < 2 && ok; ++s) {
+      const uint32_t a0 = tc::saddr(smem + s * 6 * PLANE), b0 = a0 + 3 * PLANE;
+#pragma unroll
+      for (int kk = 0; kk < KC / 16; ++kk)
+#pragma unroll
+        for (int t = 6 - NT; t < 6; ++t) {
+          const uint64_t ad = tc::sdesc(a0 + TA[t] * PLANE + kk * 2 * LBO, LBO, SBO);
+          const uint64_t bd = tc::sdesc(b0 + TB[t] * PLANE + kk * 2 * LBO, LBO, SBO);
+          tc::mma_bf16(tmem, ad, bd, IDESC, (s > 0 || kk > 0 || t > 6 - NT) ? 1u : 0u);
+        }
+    }
+    tc::commit(&bar[1]);
+  }
+  {
+    bool w = tc::mbar_wait(&bar[1], 0u, WAIT_CYCLES);
+    if (!w)
+      w = tc::mbar_wait(&bar[1], 0u, WAIT_CYCLES);
+    ok = w && ok;
+  }
+  // a CTA whose copy or MMAs failed writes nothing back
+  ok = __syncthreads_and(ok) != 0;
+  tc::fence_after();
+  __syncwarp();
+#pragma unroll 1
+  for (int c = 0; c < TILE && ok; c += 32) {
+    uint32_t r[32];
+    tc::tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c, r);
+    if (live) {
+#pragma unroll
+      for (int e = 0; e < 32; ++e)
+        pair_col(X, I, J, c + e)[row] = __uint_as_float(r[e]);
+    }
+  }
+  if (!ok)
+    atomicOr(err, 1u);
+  tc::fence_before();
+  __syncthreads();
+  tc::fence_after();
+  __syncwarp();
+  if (warp == 0)
+    tc::tmem_dealloc(tmem, TILE);
+}
+
+// the split image of the real 128 x 128 rotation Rb (Rb[k][i], k = input column, i = output
+// column) as k_apply's B operand: B[i][k] = Rb[k][i], stage k / 64, three BF16 terms.
+// Thread layout: each (i, 8 consecutive k) chunk is one 16-byte store per term.
+template <typename F>
+__device__ __forceinline__ void write_rimg(unsigned char *img, F rb)
+{
+  for (int q = threadIdx.x; q < TILE * (TILE / 8); q += blockDim.x) {
+    const int i = q % TILE, k8 = (q / TILE) * 8;
+    float v[8];
+#pragma unroll
+    for (int e = 0; e < 8; ++e)
+      v[e] = rb(k8 + e, i);
+    store_split8(img + (k8 / KC) * 3 * PLANE + tile_off(i, k8 % KC), v);
+  }
+}
+
+// ---------------------------------------------------------------- pair eigenproblems
+// One CTA per block pair: sums the split Gram partials, forms H (complex 64 x 64 from the
+// real Gram of [Re | Im], or real 128 x 128), runs `sweeps` cyclic Jacobi sweeps on H with
+// the rotation accumulated in R (R := I first), orders R's columns by descending diagonal
+// of the final H, and writes R's split image for k_apply. stats[0] += rotations,
+// stats[1] = max over rotated pairs of |h_pq| / sqrt(h_pp h_qq) (as float bits).
+template <bool CPLX>
+__global__ void __launch_bounds__(256) k_pair_evd(const float *Spart, int ksplit, int sweeps, float tol,
+                                                   unsigned char *Rimg, unsigned *stats)
+{
+  constexpr int N = CPLX ? 64 : 128;  // order of H
+  constexpr int P = N / 2;             // pairs per Jacobi step
+  constexpr int LD = N + 1;
+  extern __shared__ __align__(16) float fsm[];
+  float *Hr = fsm, *Hi = Hr + N * LD;
+  float *Rr = Hi + (CPLX ? N * LD : 0), *Ri = Rr + N * LD;
+  float *rot = Ri + (CPLX ? N * LD : 0);  // 5 P: cs, sr, si, dpp, dqq
+  float *cs = rot, *sr = rot + P, *si = rot + 2 * P, *dpp = rot + 3 * P, *dqq = rot + 4 * P;
+  int *pp = reinterpret_cast<int *>(rot + 5 * P), *qq = pp + P, *act = qq + P;
+  int *rank = act + P;
+  __shared__ unsigned nrot_s, mu_s;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const float *S0 = Spart + (size_t)blockIdx.x * ksplit * TILE * TILE;
+  if (tid == 0) {
+    nrot_s = 0u;
+    mu_s = 0u;
+  }
+  // S = sum of the partials; H from S (upper triangle, mirrored: exactly Hermitian)
+  for (int q = tid; q < N * N; q += nt) {
+    const int i = q / N, j = q % N;
+    if (i > j)
+      continue;
+    auto S = [&](int a, int b) {
+      float x = 0.f;
+      for (int k = 0; k < ksplit; ++k)
+        x += S0[(size_t)k * TILE * TILE + (size_t)a * TILE + b];
+      return x;
+    };
+    if (CPLX) {
+      const float hr = S(i, j) + S(64 + i, 64 + j);
+      const float hi = (i == j) ? 0.f : (S(i, 64 + j) - S(64 + i, j));
+      Hr[i * LD + j] = hr;
+      Hi[i * LD + j] = hi;
+      Hr[j * LD + i] = hr;
+      Hi[j * LD + i] = -hi;
+    }
+    else {
+      const float h = S(i, j);
+      Hr[i * LD + j] = h;
+      Hr[j * LD + i] = h;
+    }
+  }
+  for (int q = tid; q < N * N; q += nt) {
+    const int i = q / N, j = q % N;
+    Rr[i * LD + j] = (i == j) ? 1.f : 0.f;
+    if (CPLX)
+      Ri[i * LD + j] = 0.f;
+  }
+  __syncthreads();
+  unsigned nrot = 0u;
+  float mu = 0.f;
+  for (int sw = 0; sw < sweeps; ++sw)
+    for (int stp = 0; stp < N - 1; ++stp) {
+      if (tid < P) {
+        int a, c;
+        if (tid == 0) {
+          a = stp;
+          c = N - 1;
+        }
+        else {
+          a = (stp + tid) % (N - 1);
+          c = (stp + (N - 1) - tid) % (N - 1);
+        }
+        const int p = a < c ? a : c, q = a < c ? c : a;
+        pp[tid] = p;
+        qq[tid] = q;
+        const float ha = fmaxf(Hr[p * LD + p], 0.f), hb = fmaxf(Hr[q * LD + q], 0.f);
+        const float cr = Hr[p * LD + q], ci = CPLX ? Hi[p * LD + q] : 0.f;
+        const float ac = CPLX ? hypotf(cr, ci) : fabsf(cr);
+        const float sc = sqrtf(ha) * sqrtf(hb);
+        float c_ = 1.f, s_r = 0.f, s_i = 0.f, d1 = ha, d2 = hb;
+        int go = 0;
+        if (ac > 0.f && ac >= tol * sc) {
+          const float zeta = (hb - ha) / (2.f * ac);
+          const float az = fabsf(zeta);
+          const float t = (az > 1e18f) ? 0.5f / zeta : copysignf(1.f, zeta) / (az + sqrtf(fmaf(zeta, zeta, 1.f)));
+          c_ = 1.f / sqrtf(fmaf(t, t, 1.f));
+          const float sn = t * c_;
+          s_r = sn * (cr / ac);
+          s_i = CPLX ? sn * (ci / ac) : 0.f;
+          d1 = ha - t * ac;
+          d2 = hb + t * ac;
+          go = 1;
+          ++nrot;
+          mu = fmaxf(mu, (sc > 0.f) ? ac / sc : 1.f);
+        }
+        cs[tid] = c_;
+        sr[tid] = s_r;
+        si[tid] = s_i;
+        dpp[tid] = d1;
+        dqq[tid] = d2;
+        act[tid] = go;
+      }
+      __syncthreads();
+      // H := J^H H J, 2x2 block (u, v) of the step's pairs at a time (u <= v; the (v, u)
+      // block is its conjugate transpose)
+      for (int q = tid; q < P * P; q += nt) {
+        const int u = q / P, v = q % P;
+        if (u > v || !(act[u] | act[v]))
+          continue;
+        const int pu = pp[u], qu = qq[u], pv = pp[v], qv = qq[v];
+        if (u == v) {
+          Hr[pu * LD + pu] = dpp[u];
+          Hr[qu * LD + qu] = dqq[u];
+          Hr[pu * LD + qu] = 0.f;
+          Hr[qu * LD + pu] = 0.f;
+          if (CPLX) {
+            Hi[pu * LD + qu] = 0.f;
+            Hi[qu * LD + pu] = 0.f;
+          }
+          continue;
+        }
+        const float cv = cs[v], svr = sr[v], svi = si[v], cu = cs[u], sur = sr[u], sui = si[u];
+        // B = [[b00, b01], [b10, b11]] = H rows (pu, qu), columns (pv, qv)
+        float b00r = Hr[pu * LD + pv], b01r = Hr[pu * LD + qv], b10r = Hr[qu * LD + pv], b11r = Hr[qu * LD + qv];
+        float b00i = 0.f, b01i = 0.f, b10i = 0.f, b11i = 0.f;
+        if (CPLX) {
+          b00i = Hi[pu * LD + pv];
+          b01i = Hi[pu * LD + qv];
+          b10i = Hi[qu * LD + pv];
+          b11i = Hi[qu * LD + qv];
+        }
+        // C = B J_v: C[:,0] = cv B[:,0] - conj(s_v) B[:,1], C[:,1] = cv B[:,1] + s_v B[:,0]
+        const float c00r = cv * b00r - (svr * b01r + svi * b01i), c00i = cv * b00i - (svr * b01i - svi * b01r);
+        const float c10r = cv * b10r - (svr * b11r + svi * b11i), c10i = cv * b10i - (svr * b11i - svi * b11r);
+        const float c01r = cv * b01r + (svr * b00r - svi * b00i), c01i = cv * b01i + (svr * b00i + svi * b00r);
+        const float c11r = cv * b11r + (svr * b10r - svi * b10i), c11i = cv * b11i + (svr * b10i + svi * b10r);
+        // B' = J_u^H C: row 0 = cu C[0,:] - s_u C[1,:], row 1 = cu C[1,:] + conj(s_u) C[0,:]
+        const float n00r = cu * c00r - (sur * c10r - sui * c10i), n00i = cu * c00i - (sur * c10i + sui * c10r);
+        const float n01r = cu * c01r - (sur * c11r - sui * c11i), n01i = cu * c01i - (sur * c11i + sui * c11r);
+        const float n10r = cu * c10r + (sur * c00r + sui * c00i), n10i = cu * c10i + (sur * c00i - sui * c00r);
+        const float n11r = cu * c11r + (sur * c01r + sui * c01i), n11i = cu * c11i + (sur * c01i - sui * c01r);
+        Hr[pu * LD + pv] = n00r;
+        Hr[pu * LD + qv] = n01r;
+        Hr[qu * LD + pv] = n10r;
+        Hr[qu * LD + qv] = n11r;
+        Hr[pv * LD + pu] = n00r;
+        Hr[qv * LD + pu] = n01r;
+        Hr[pv * LD + qu] = n10r;
+        Hr[qv * LD + qu] = n11r;
+        if (CPLX) {
+          Hi[pu * LD + pv] = n00i;
+          Hi[pu * LD + qv] = n01i;
+          Hi[qu * LD + pv] = n10i;
+          Hi[qu * LD + qv] = n11i;
+          Hi[pv * LD + pu] = -n00i;
+          Hi[qv * LD + pu] = -n01i;
+          Hi[pv * LD + qu] = -n10i;
+          Hi[qv * LD + qu] = -n11i;
+        }
+      }
+      // R := R J: columns (p_v, q_v) of every row
+      for (int q = tid; q < N * P; q += nt) {
+        const int r = q / P, v = q % P;
+        if (!act[v])
+          continue;
+        const int pv = pp[v], qv = qq[v];
+        const float cv = cs[v], svr = sr[v], svi = si[v];
+        const float xr = Rr[r * LD + pv], yr = Rr[r * LD + qv];
+        const float xi = CPLX ? Ri[r * LD + pv] : 0.f, yi = CPLX ? Ri[r * LD + qv] : 0.f;
+        Rr[r * LD + pv] = cv * xr - (svr * yr + svi * yi);
+        Rr[r * LD + qv] = cv * yr + (svr * xr - svi * xi);
+        if (CPLX) {
+          Ri[r * LD + pv] = cv * xi - (svr * yi - svi * yr);
+          Ri[r * LD + qv] = cv * yi + (svr * xi + svi * xr);
+        }
+      }
+      __syncthreads();
+    }
+  // descending order of the diagonal (ties by index): column i of R goes to rank[i]
+  // (a NaN sorts as -inf, so that the ranks stay a permutation)
+  auto key = [&](int i) {
+    const float d = Hr[i * LD + i];
+    return (d == d) ? d : -INFINITY;
+  };
+  for (int i = tid; i < N; i += nt) {
+    const float d = key(i);
+    int r = 0;
+    for (int j = 0; j < N; ++j) {
+      const float e = key(j);
+      r += (e > d || (e == d && j < i)) ? 1 : 0;
+    }
+    rank[r] = i;  // rank[r] = the column of R that goes to position r
+  }
+  if (nrot)
+    atomicAdd(&nrot_s, nrot);
+  if (mu > 0.f)
+    atomicMax(&mu_s, __float_as_uint(mu));
+  __syncthreads();
+  unsigned char *img = Rimg + (size_t)blockIdx.x * 6 * PLANE;
+  if (CPLX)
+    // Rb = [[Re R, Im R], [-Im R, Re R]] with R's columns reordered
+    write_rimg(img, [&](int k, int i) {
+      const int kr = k & 63, ic = rank[i & 63];
+      const float re = Rr[kr * LD + ic], im = Ri[kr * LD + ic];
+      return (k < 64) ? ((i < 64) ? re : im) : ((i < 64) ? -im : re);
+    });
+  else
+    write_rimg(img, [&](int k, int i) { return Rr[k * LD + rank[i]]; });
+  if (tid == 0) {
+    if (nrot_s)
+      atomicAdd(stats, nrot_s);
+    if (mu_s)
+      atomicMax(stats + 1, mu_s);
+  }
+}
+
+// the split image of caller-given real 128 x 128 rotations (pair k: R + k 128 128,
+// column-major: R[k][i] at k + 128 i), for vj_block_apply_dev
+__global__ void __launch_bounds__(256) k_rimg(const float *R, unsigned char *Rimg)
+{
+  const float *Rk = R + (size_t)blockIdx.x * TILE * TILE;
+  write_rimg(Rimg + (size_t)blockIdx.x * 6 * PLANE, [&](int k, int i) { return Rk[k + TILE * i]; });
+}
+
+static size_t evd_smem(bool cplx)
+{
+  const int N = cplx ? 64 : 128, P = N / 2, LD = N + 1;
+  return (size_t)(cplx ? 4 : 2) * N * LD * 4 + (size_t)5 * P * 4 + (size_t)3 * P * 4 + (size_t)N * 4;
+}
+
+constexpr size_t GRAM_SMEM = 2 * 3 * PLANE + 1024;
+constexpr size_t APPLY_SMEM = 2 * 6 * PLANE + 1024;
+
+// ---------------------------------------------------------------- host side
+struct Plan {
+  int nb, npairs, ksplit, tg, tw, b;
+  bool cplx;
+};
+
+static bool attrs_set(bool cplx)
+{
+  static int done[2] = {0, 0};
+  int &d = done[cplx ? 1 : 0];
+  if (!d) {
+    bool ok = cudaFuncSetAttribute(k_gram<6>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)GRAM_SMEM) ==
+                  cudaSuccess &&
+              cudaFuncSetAttribute(k_gram<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)GRAM_SMEM) ==
+                  cudaSuccess &&
+              cudaFuncSetAttribute(k_apply<6>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)APPLY_SMEM) ==
+                  cudaSuccess &&
+              cudaFuncSetAttribute(k_apply<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)APPLY_SMEM) ==
+                  cudaSuccess;
+    ok = ok && (cplx ? cudaFuncSetAttribute(k_pair_evd<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            (int)evd_smem(true))
+                     : cudaFuncSetAttribute(k_pair_evd<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                            (int)evd_smem(false))) == cudaSuccess;
+    if (!ok) {
+      cudaGetLastError();
+      return false;
+    }
+    d = 1;
+  }
+  return true;
+}
+
+static Plan plan(bool cplx, long long m, long long n)
+{
+  Plan p;
+  p.cplx = cplx;
+  p.b = cplx ? 32 : 64;
+  p.nb = (int)(n / p.b);
+  p.npairs = p.nb / 2;
+  // split K so that the Gram grid covers the GPU about once
+  const int sms = host::sm_count();
+  const int nch = (int)((m + KC - 1) / KC);
+  int ks = (sms + p.npairs - 1) / p.npairs;
+  if (ks > nch)
+    ks = nch;
+  if (ks < 1)
+    ks = 1;
+  p.ksplit = ks;
+  p.tg = (int)((m + TILE - 1) / TILE);
+  p.tw = (int)((n + TILE - 1) / TILE);
+  return p;
+}
+
+}  // namespace bj
+
+// whether the block sweeps apply to an m x n FP32 problem: whole blocks in an even number
+// (n a multiple of 128 real / 64 complex columns), 16-byte aligned columns
+bool block_sweeps_apply(bool cplx, long long m, long long n, long long ld)
+{
+  const long long bw = cplx ? 64 : 128;
+  return n >= bw && (n % bw) == 0 && (m % 4) == 0 && (ld % 4) == 0 && m <= (1LL << 30);
+}
+
+// Scratch bytes of block_sweep for an m x n problem.
+size_t block_sweep_scratch(bool cplx, long long m, long long n)
+{
+  const bj::Plan p = bj::plan(cplx, m, n);
+  return (size_t)p.npairs * p.ksplit * bj::TILE * bj::TILE * 4 + (size_t)p.npairs * 6 * bj::PLANE + 256;
+}
+
+// One block sweep (nb - 1 block steps) on planar FP32 G (m x n) and W (n x n), both with
+// the given leading dimensions. scratch: block_sweep_scratch bytes; stats: 4 device words
+// (zeroed here; [0] rotations, [1] max scaled |h_pq| of a rotated pair as float bits, [2]
+// error flag). terms: 6 (FP32-accurate products) or 3. Returns rotations, or -1 (launch
+// failure or a kernel whose wait gave up).
+long long block_sweep(bool cplx, int m, int n, float *Gr, float *Gi, long long ldg, float *Wr, float *Wi,
+                      long long ldw, unsigned char *scratch, unsigned *stats, float tol, int inner, int terms,
+                      cudaStream_t s, float *mu)
+{
+  using namespace bj;
+  if (!attrs_set(cplx))
+    return -1;
+  const Plan p = plan(cplx, m, n);
+  float *Spart = reinterpret_cast<float *>(scratch);
+  unsigned char *Rimg = scratch + (size_t)p.npairs * p.ksplit * TILE * TILE * 4;
+  const Cols G{Gr, cplx ? Gi : nullptr, ldg, p.b}, W{Wr, cplx ? Wi : nullptr, ldw, p.b};
+  if (cudaMemsetAsync(stats, 0, 16, s) != cudaSuccess)
+    return -1;
+  for (int step = 0; step < p.nb - 1; ++step) {
+    if (terms == 3)
+      k_gram<3><<<p.npairs * p.ksplit, 128, GRAM_SMEM, s>>>(G, m, p.nb, step, p.ksplit, Spart, stats + 2);
+    else
+      k_gram<6><<<p.npairs * p.ksplit, 128, GRAM_SMEM, s>>>(G, m, p.nb, step, p.ksplit, Spart, stats + 2);
+    if (cplx)
+      k_pair_evd<true><<<p.npairs, 256, evd_smem(true), s>>>(Spart, p.ksplit, inner, tol, Rimg, stats);
+    else
+      k_pair_evd<false><<<p.npairs, 256, evd_smem(false), s>>>(Spart, p.ksplit, inner, tol, Rimg, stats);
+    if (terms == 3)
+      k_apply<3><<<p.npairs * (p.tg + p.tw), 128, APPLY_SMEM, s>>>(G, m, W, n, p.nb, step, p.tg, p.tw, Rimg,
+                                                                    stats + 2);
+    else
+      k_apply<6><<<p.npairs * (p.tg + p.tw), 128, APPLY_SMEM, s>>>(G, m, W, n, p.nb, step, p.tg, p.tw, Rimg,
+                                                                    stats + 2);
+  }
+  unsigned hs[4] = {0u, 0u, 0u, 0u};
+  if (cudaGetLastError() != cudaSuccess || cudaMemcpyAsync(hs, stats, 16, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+      cudaStreamSynchronize(s) != cudaSuccess)
+    return -1;
+  if (hs[2])
+    return -1;
+  std::memcpy(mu, &hs[1], 4);
+  return (long long)hs[0];
+}
+
+}  // namespace vj
+
+using namespace vj;
+
+// ---------------------------------------------------------------- C ABI
+// The block-sweep building blocks on their own (tests, and callers that drive their own
+// block orderings). Real data: Gi, Wi NULL; complex: split planes.
+static bool block_args(int cplx, vj_fnat m, vj_fnat n, vj_fnat ld)
+{
+  return block_sweeps_apply(cplx != 0, (long long)m, (long long)n, (long long)ld) && ld >= m;
+}
+
+extern "C" vj_fint vj_block_gram_dev(int cplx, vj_fnat m, vj_fnat n, const float *Gr, const float *Gi, vj_fnat ldG,
+                                     int step, int terms, float *S, void *stream)
+{
+  using namespace vj::bj;
+  if (!block_args(cplx, m, n, ldG) || (terms != 3 && terms != 6) || (cplx && !Gi))
+    return VJ_ERR_ARG;
+  if (!host::gpu_ready())
+    return VJ_ERR_NO_GPU;
+  const Plan p = plan(cplx != 0, (long long)m, (long long)n);
+  if (step < 0 || step >= p.nb - 1)
+    return VJ_ERR_ARG;
+  if (!attrs_set(cplx != 0))
+    return VJ_ERR_CUDA;
+  cudaStream_t s = (cudaStream_t)stream;
+  float *Spart = nullptr;
+  unsigned *err = nullptr;
+  if (cudaMalloc(&Spart, (size_t)p.npairs * p.ksplit * TILE * TILE * 4) != cudaSuccess)
+    return VJ_ERR_NOMEM;
+  if (cudaMalloc(&err, 16) != cudaSuccess) {
+    cudaFree(Spart);
+    return VJ_ERR_NOMEM;
+  }
+  const Cols G{const_cast<float *>(Gr), cplx ? const_cast<float *>(Gi) : nullptr, (long long)ldG, p.b};
+  vj_fint r = 0;
+  bool ok = cudaMemsetAsync(err, 0, 16, s) == cudaSuccess;
+  if (ok) {
+    if (terms == 3)
+      k_gram<3><<<p.npairs * p.ksplit, 128, GRAM_SMEM, s>>>(G, (int)m, p.nb, step, p.ksplit, Spart, err);
+    else
+      k_gram<6><<<p.npairs * p.ksplit, 128, GRAM_SMEM, s>>>(G, (int)m, p.nb, step, p.ksplit, Spart, err);
+    ok = cudaGetLastError() == cudaSuccess;
+  }
+  // S = the sum of the K splits, pair by pair
+  std::vector<float> h((size_t)p.npairs * p.ksplit * TILE * TILE);
+  unsigned he = 0;
+  ok = ok && cudaMemcpyAsync(h.data(), Spart, h.size() * 4, cudaMemcpyDeviceToHost, s) == cudaSuccess &&
+       cudaMemcpyAsync(&he, err, 4, cudaMemcpyDeviceToHost, s) == cudaSuccess && cudaStreamSynchronize(s) == cudaSuccess;
+  if (ok && !he) {
+    std::vector<float> o((size_t)p.npairs * TILE * TILE, 0.f);
+    for (int k = 0; k < p.npairs; ++k)
+      for (int q = 0; q < p.ksplit; ++q)
+        for (int e = 0; e < TILE * TILE; ++e)
+          o[(size_t)k * TILE * TILE + e] += h[((size_t)k * p.ksplit + q) * TILE * TILE + e];
+    ok = cudaMemcpyAsync(S, o.data(), o.size() * 4, cudaMemcpyHostToDevice, s) == cudaSuccess &&
+         cudaStreamSynchronize(s) == cudaSuccess;
+  }
+  else
+    ok = false;
+  cudaFree(Spart);
+  cudaFree(err);
+  if (!ok)
+    r = VJ_ERR_CUDA;
+  return r ? r : (vj_fint)p.npairs;
+}
+
+extern "C" vj_fint vj_block_apply_dev(int cplx, vj_fnat m, vj_fnat n, float *Gr, float *Gi, vj_fnat ldG, float *Wr,
+                                      float *Wi, vj_fnat ldW, int step, int terms, const float *R, void *stream)
+{
+  using namespace vj::bj;
+  if (!block_args(cplx, m, n, ldG) || !block_args(cplx, n, n, ldW) || (terms != 3 && terms != 6) ||
+      (cplx && (!Gi || !Wi)))
+    return VJ_ERR_ARG;
+  if (!host::gpu_ready())
+    return VJ_ERR_NO_GPU;
+  const Plan p = plan(cplx != 0, (long long)m, (long long)n);
+  if (step < 0 || step >= p.nb - 1)
+    return VJ_ERR_ARG;
+  if (!attrs_set(cplx != 0))
+    return VJ_ERR_CUDA;
+  cudaStream_t s = (cudaStream_t)stream;
+  unsigned char *img = nullptr;
+  unsigned *err = nullptr;
+  if (cudaMalloc(&img, (size_t)p.npairs * 6 * PLANE) != cudaSuccess)
+    return VJ_ERR_NOMEM;
+  if (cudaMalloc(&err, 16) != cudaSuccess) {
+    cudaFree(img);
+    return VJ_ERR_NOMEM;
+  }
+  const Cols G{Gr, cplx ? Gi : nullptr, (long long)ldG, p.b}, W{Wr, cplx ? Wi : nullptr, (long long)ldW, p.b};
+  bool ok = cudaMemsetAsync(err, 0, 16, s) == cudaSuccess;
+  if (ok) {
+    k_rimg<<<p.npairs, 256, 0, s>>>(R, img);
+    if (terms == 3)
+      k_apply<3><<<p.npairs * (p.tg + p.tw), 128, APPLY_SMEM, s>>>(G, (int)m, W, (int)n, p.nb, step, p.tg, p.tw, img,
+                                                                    err);
+    else
+      k_apply<6><<<p.npairs * (p.tg + p.tw), 128, APPLY_SMEM, s>>>(G, (int)m, W, (int)n, p.nb, step, p.tg, p.tw, img,
+                                                                    err);
+    ok = cudaGetLastError() == cudaSuccess;
+  }
+  unsigned he = 0;
+  ok = ok && cudaMemcpyAsync(&he, err, 4, cudaMemcpyDeviceToHost, s) == cudaSuccess &&
+       cudaStreamSynchronize(s) == cudaSuccess && !he;
+  cudaFree(img);
+  cudaFree(err);
+  return ok ? (vj_fint)p.npairs : VJ_ERR_CUDA;
+}
+
+extern "C" vj_fint vj_block_sweep_dev(int cplx, vj_fnat m, vj_fnat n, float *Gr, float *Gi, vj_fnat ldG, float *Wr,
+                                      float *Wi, vj_fnat ldW, float tol, int inner, int terms, float *mu,
+                                      void *stream)
+{
+  if (!block_args(cplx, m, n, ldG) || !block_args(cplx, n, n, ldW) || (terms != 3 && terms != 6) || inner < 1 ||
+      (cplx && (!Gi || !Wi)))
+    return VJ_ERR_ARG;
+  if (!host::gpu_ready())
+    return VJ_ERR_NO_GPU;
+  unsigned char *scr = nullptr;
+  unsigned *stats = nullptr;
+  if (cudaMalloc(&scr, block_sweep_scratch(cplx != 0, (long long)m, (long long)n)) != cudaSuccess)
+    return VJ_ERR_NOMEM;
+  if (cudaMalloc(&stats, 16) != cudaSuccess) {
+    cudaFree(scr);
+    return VJ_ERR_NOMEM;
+  }
+  float mu_ = 0.f;
+  const long long r = block_sweep(cplx != 0, (int)m, (int)n, Gr, Gi, (long long)ldG, Wr, Wi, (long long)ldW, scr,
+                                  stats, tol, inner, terms, (cudaStream_t)stream, &mu_);
+  cudaFree(scr);
+  cudaFree(stats);
+  if (mu)
+    *mu = mu_;
+  return r < 0 ? VJ_ERR_CUDA : (vj_fint)r;
+}

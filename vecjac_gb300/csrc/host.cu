@@ -147,25 +147,26 @@ void trace_sweep(unsigned sweep, unsigned long long rotations)
   g_trace.sweeps = sweep + 1;
 }
 
-static double g_mixed[5];
+static double g_mixed[6];
 
-void mixed_phases_set(double fp32, double gemm, double fp64, double fin, double fp32_steps)
+void mixed_phases_set(double fp32, double gemm, double fp64, double fin, double fp32_steps, double block)
 {
   g_mixed[0] = fp32;
   g_mixed[1] = gemm;
   g_mixed[2] = fp64;
   g_mixed[3] = fin;
   g_mixed[4] = fp32_steps;
+  g_mixed[5] = block;
 }
 
 }  // namespace host
 }  // namespace vj
 
-extern "C" vj_fint vj_last_mixed_phases(double out[5])
+extern "C" vj_fint vj_last_mixed_phases(double out[6])
 {
   if (!out)
     return VJ_ERR_ARG;
-  for (int i = 0; i < 5; ++i)
+  for (int i = 0; i < 6; ++i)
     out[i] = vj::host::g_mixed[i];
   return 0;
 }

@@ -23,6 +23,7 @@
 // real products per complex one on the split planes).
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <chrono>
 #include <cstring>
 #include <algorithm>
@@ -36,6 +37,13 @@
 #include "vj_host.h"
 
 namespace vj {
+
+// defined in blockjac.cu: block sweeps with split-BF16x3 tensor-core products
+bool block_sweeps_apply(bool cplx, long long m, long long n, long long ld);
+size_t block_sweep_scratch(bool cplx, long long m, long long n);
+long long block_sweep(bool cplx, int m, int n, float *Gr, float *Gi, long long ldg, float *Wr, float *Wi,
+                      long long ldw, unsigned char *scratch, unsigned *stats, float tol, int inner, int terms,
+                      cudaStream_t s, float *mu);
 
 // defined in jsvd.cu
 template <typename T, bool CPLX>
@@ -556,9 +564,21 @@ static vj_fint mixed_dev(vj_fnat m_, vj_fnat n_, double *G, vj_fnat ldG, double 
   // (3 n n doubles)
   const size_t gpn = ((size_t)P * mn > 3 * nn) ? (size_t)P * mn : 3 * nn;
   const size_t f64b = (gpn + P * 3 * nn) * 8;
+  // FP32 stages: block sweeps on the tensor cores where the shape has whole blocks
+  // (VJ_BLOCK=0 in the environment selects the column-pair sweeps), with the terms of the
+  // split products (VJ_BLOCK_TERMS, 6 or 3) and inner Jacobi sweeps per block pair
+  // (VJ_BLOCK_INNER)
+  const char *eb = getenv("VJ_BLOCK");
+  const bool blk = !(eb && *eb == '0') && block_sweeps_apply(CPLX, m, n, m);
+  const char *et = getenv("VJ_BLOCK_TERMS");
+  const int terms = (et && atoi(et) == 3) ? 3 : 6;
+  const char *ei = getenv("VJ_BLOCK_INNER");
+  const int inner = (ei && atoi(ei) >= 1 && atoi(ei) <= 8) ? atoi(ei) : 1;
+  const size_t blkb = blk ? ((block_sweep_scratch(CPLX, m, n) + 255) & ~(size_t)255) : 0;
   host::Staging &stg = host::staging3();
-  if (!stg.reserve(f32b + f64b + 256))
+  if (!stg.reserve(f32b + f64b + 256 + blkb))
     return VJ_ERR_NOMEM;
+  unsigned char *bscr = reinterpret_cast<unsigned char *>(stg.ptr) + f32b + f64b + 256;
   float *G32 = reinterpret_cast<float *>(stg.ptr);
   float *W32 = G32 + P * mn;
   double *Gp = reinterpret_cast<double *>(stg.ptr + f32b);
@@ -615,8 +635,11 @@ static vj_fint mixed_dev(vj_fnat m_, vj_fnat n_, double *G, vj_fnat ldG, double 
     const float stop = 4.f * tol;
     for (; sw < maxsw; ++sw) {
       float mu = 0.f;
-      const long long hc = presweep<float, CPLX>(mi, ni, G32, m, CPLX ? G32 + mn : nullptr, m, W32, n,
-                                                 CPLX ? W32 + nn : nullptr, n, js, stp, tol, cnt, s, &mu);
+      const long long hc =
+          blk ? block_sweep(CPLX, mi, ni, G32, CPLX ? G32 + mn : nullptr, m, W32, CPLX ? W32 + nn : nullptr, n, bscr,
+                            cnt, tol, inner, terms, s, &mu)
+              : presweep<float, CPLX>(mi, ni, G32, m, CPLX ? G32 + mn : nullptr, m, W32, n, CPLX ? W32 + nn : nullptr,
+                                      n, js, stp, tol, cnt, s, &mu);
       if (hc < 0)
         return VJ_ERR_CUDA;
       if (!hc)
@@ -753,7 +776,9 @@ static vj_fint mixed_dev(vj_fnat m_, vj_fnat n_, double *G, vj_fnat ldG, double 
   // 6. FP64 finishing sweeps (the reference's algorithm) with V preset
   const vj_fint r = svd_dev_entry<double, CPLX>(m_, n_, G, ldG, Gi, ldGi, V, ldV, Vi, ldVi, eS, fS, js, stp, swp, 1, s);
   const double msfin = std::chrono::duration<double, std::milli>(now() - t0).count();
-  host::mixed_phases_set(ms32, msgemm, ms64, msfin, (double)total32 * stp);
+  // FP32 launches: 3 per block step (n/b - 1 steps per block sweep), else 1 per pivot step
+  const double steps32 = blk ? (double)total32 * (double)(n / (CPLX ? 32 : 64) - 1) * 3.0 : (double)total32 * stp;
+  host::mixed_phases_set(ms32, msgemm, ms64, msfin, steps32, blk ? 1.0 : 0.0);
   if (trace)
     std::fprintf(stderr, "mixed SVD phases (ms): FP32 sweeps %.1f, Newton-Schulz + GEMMs %.1f, plain FP64 sweeps + sort %.1f, "
                  "finishing %.1f\n", ms32, msgemm, ms64, msfin);

@@ -75,8 +75,9 @@ void trace_sweep(unsigned sweep, unsigned long long rotations);
 bool trace_enabled();
 void trace_phases(const unsigned long long *cycles, int count);
 
-// phase times (ms) of the last mixed-precision SVD and its number of FP32 step launches
-void mixed_phases_set(double fp32, double gemm, double fp64, double fin, double fp32_steps);
+// phase times (ms) of the last mixed-precision SVD, its number of FP32 launches and whether
+// its FP32 stages ran as block sweeps on the tensor cores (1) or column-pair sweeps (0)
+void mixed_phases_set(double fp32, double gemm, double fp64, double fin, double fp32_steps, double block);
 
 // elements per chunk of a host-pointer 2x2 call (a multiple of `lanes`)
 long long bjac2_chunk(long long n, size_t elem, bool cplx, int lanes);
