@@ -16,6 +16,7 @@
 #define __host__
 #define __device__
 #define __forceinline__ inline
+#define __noinline__ __attribute__((noinline))
 
 static long long g_host_ddiv_calls = 0;
 

@@ -4,9 +4,12 @@
 //            (FP32: S8JAC*_LOOP, src/sbjac2.c, constants src/scjac2.h)
 //   complex: Z8JAC2_LOOP / Z8JACL_LOOP / Z8JACI_LOOP   src/zbjac2.c:18-62, :65-106, :179-219
 // KIND 0: cosine + tangent(s), KIND 1: cosine + sine(s), KIND 2: secant + tangent(s).
-// Finite inputs take a path whose exponent logic (getexp, min, scalef by an integer)
-// runs on the integer pipes; inputs with an inf or NaN take the literal transcription.
+// Nonzero normal inputs of moderate spread take a fast path whose scalings are exponent
+// adds; other finite inputs take a path whose exponent logic (getexp, min, scalef by an
+// integer) runs on the integer pipes; inputs with an inf or NaN take the literal
+// transcription.
 #pragma once
+#include "dsqrt.cuh"
 #include "idiv.cuh"
 #include "vj_fp.cuh"
 
@@ -41,21 +44,76 @@ template <typename T> __device__ __forceinline__ T clamp_t2(T q)
   return (u < lim) ? q : F::sqrt_huge();
 }
 
+// ---- the all-normal fast path ----
+// When every input is a nonzero normal number and their exponents span less than the
+// scaling headroom (BE + BIAS - 1 binades), the prescale exponent is es = BE + BIAS - (the
+// largest biased exponent), every scaled value stays normal, and each scaling by a power of
+// two is an add to the exponent field: the general path's getexp/min/scale2 sequences,
+// whose rare branches the compiler would otherwise predicate into every lane, reduce to a
+// few integer operations. The results are those of the general path bit for bit (the
+// general path takes the same normal-range branch of every escale and scale2 then).
+template <typename T> __device__ __forceinline__ int bexp(T x)
+{
+  return (int)((fp<T>::bits(x) & ~fp<T>::SIGN) >> fp<T>::MB);
+}
+// x * 2^n for a normal x whose product is normal: an integer add to the exponent field
+template <typename T> __device__ __forceinline__ T addexp(T x, int n)
+{
+  return fp<T>::val(fp<T>::bits(x) + ((typename fp<T>::U)(long long)n << fp<T>::MB));
+}
+// the general scale2, kept out of line
+template <typename T> __device__ __noinline__ T scale2_rare(T x, int n) { return scale2(x, n); }
+// x * 2^n for a finite x: the exponent add when x and the product are normal
+template <typename T> __device__ __forceinline__ T scale2_nr(T x, int n)
+{
+  const int be = bexp(x), bn = be + n;
+  if (be > 0 && bn > 0 && bn <= fp<T>::EMAXB)
+    return addexp(x, n);
+  return scale2_rare(x, n);
+}
+// a < b for finite a, b on the integer pipes (two's-complement order of the bit patterns,
+// with -0 == +0), max / min of non-negative finite values likewise
+__device__ __forceinline__ long long okey(double x)
+{
+  const long long u = (long long)fp<double>::bits(x);
+  return (u < 0) ? -(u & 0x7fffffffffffffffLL) : u;
+}
+__device__ __forceinline__ int okey(float x)
+{
+  const int u = (int)fp<float>::bits(x);
+  return (u < 0) ? -(u & 0x7fffffff) : u;
+}
+template <typename T> __device__ __forceinline__ bool lt_fin(T a, T b) { return okey(a) < okey(b); }
+template <typename T> __device__ __forceinline__ T nnmin(T a, T b) { return (fp<T>::bits(a) < fp<T>::bits(b)) ? a : b; }
+template <typename T> __device__ __forceinline__ T nnmax(T a, T b) { return (fp<T>::bits(a) > fp<T>::bits(b)) ? a : b; }
+// square root of 1 <= x < 2^EMAX: FP64 with the few-FP64-operation routine of dsqrt.cuh,
+// FP32 with the FP32 unit's correctly rounded root
+__device__ __forceinline__ double sqrt_ge1(double x) { return dsqrt_pos(x); }
+__device__ __forceinline__ float sqrt_ge1(float x) { return fp<float>::sqrt_(x); }
+
+template <typename T> struct fastc {
+  static constexpr int BE = (sizeof(T) == 8) ? 1020 : 124;  // src/dzjac2.h:10, src/scjac2.h:10
+  static constexpr int TOP = BE + fp<T>::BIAS;               // biased exponent of the largest scaled input
+};
+
 // shared tail of the real and complex lanes: angle from the prescaled (a1, a2, ab)
 template <typename T> struct angle {
   T t1, s2, s1;
 };
 
-template <typename T> __device__ __forceinline__ angle<T> jac_angle(T a1, T a2, T ab, T &ad_out)
+// (FAST: the square roots' arguments, 1 + t2^2 and 1 + t1^2, are at least 1 and finite --
+// t2 is clamped to sqrt(huge) -- so the fast path takes sqrt_ge1)
+template <typename T, bool FAST = false>
+__device__ __forceinline__ angle<T> jac_angle(T a1, T a2, T ab, T &ad_out)
 {
   using F = fp<T>;
   const T one = (T)1;
   const T ad = a1 - a2;
   ad_out = ad;
   const T t2 = vor(clamp_t2(qdiv(ab, vabs(ad))), vsgn(ad));
-  const T t1 = qdiv(t2, one + F::sqrt_(F::fma_(t2, t2, one)));
+  const T t1 = qdiv(t2, one + (FAST ? sqrt_ge1(F::fma_(t2, t2, one)) : F::sqrt_(F::fma_(t2, t2, one))));
   const T s2 = F::fma_(t1, t1, one);
-  return angle<T>{t1, s2, F::sqrt_(s2)};
+  return angle<T>{t1, s2, FAST ? sqrt_ge1(s2) : F::sqrt_(s2)};
 }
 
 template <typename T, int KIND>
@@ -64,7 +122,27 @@ __device__ __forceinline__ unsigned rjac2(T a1, T a2, T ar, T &c, T &at, T &l1, 
   using F = fp<T>;
   const T one = (T)1;
   T L1, L2, t1, s1, s2, as;
-  if (all_finite3(a1, a2, ar)) {
+  bool fin = false;  // L1, L2 finite: compared on the integer pipes
+  const int b1 = bexp(a1), b2 = bexp(a2), br = bexp(ar);
+  const int bmax = max(max(b1, b2), br), bmin = min(min(b1, b2), br);
+  if (bmin > 0 && bmax <= F::EMAXB && bmax - bmin < fastc<T>::TOP) {
+    const int es = fastc<T>::TOP - bmax;
+    ar = addexp(ar, es);
+    a1 = addexp(a1, es);
+    a2 = addexp(a2, es);
+    const T aa = vabs(ar);
+    as = vsgn(ar);
+    const T ab = addexp(aa, 1);
+    T ad;
+    const angle<T> g = jac_angle<T, true>(a1, a2, ab, ad);
+    t1 = g.t1; s2 = g.s2; s1 = g.s1;
+    L1 = qdiv(F::fma_(t1, F::fma_(a2, t1, ab), a1), s2);
+    L2 = qdiv(F::fma_(t1, F::fma_(a1, t1, -ab), a2), s2);
+    l1 = scale2_nr(L1, -es);
+    l2 = scale2_nr(L2, -es);
+    fin = true;
+  }
+  else if (all_finite3(a1, a2, ar)) {
     const int es = min(min(escale(a1), escale(a2)), min(escale(ar), 1 << 20));
     ar = scale2(ar, es);
     a1 = scale2(a1, es);
@@ -109,7 +187,7 @@ __device__ __forceinline__ unsigned rjac2(T a1, T a2, T ar, T &c, T &at, T &l1, 
     c = qdiv(one, s1);
     at = ((KIND == 1) ? qdiv(vxor(t1, as), s1) : vxor(t1, as));
   }
-  return (L1 < L2) ? 1u : 0u;
+  return (fin ? lt_fin(L1, L2) : (L1 < L2)) ? 1u : 0u;
 }
 
 template <typename T, int KIND>
@@ -118,7 +196,38 @@ __device__ __forceinline__ unsigned cjac2(T a1, T a2, T ar, T ai, T &c, T &cat, 
   using F = fp<T>;
   const T one = (T)1, zero = (T)0;
   T L1, L2, t1, s1, s2, ar_, ai_;
-  if (all_finite3(a1, a2, ar) && visfinite(ai)) {
+  bool fin = false;
+  const int b1 = bexp(a1), b2 = bexp(a2), br = bexp(ar), bi = bexp(ai);
+  const int bmax = max(max(b1, b2), max(br, bi)), bmin = min(min(b1, b2), min(br, bi));
+  if (bmin > 0 && bmax <= F::EMAXB && bmax - bmin < fastc<T>::TOP) {
+    const int es = fastc<T>::TOP - bmax;
+    ar = addexp(ar, es);
+    ai = addexp(ai, es);
+    a1 = addexp(a1, es);
+    a2 = addexp(a2, es);
+    ar_ = vabs(ar);
+    ai_ = vabs(ai);
+    const T as = vsgn(ar);
+    // the min / max below compare non-negative finite values: integer comparisons; the
+    // quotient am / aM is >= 0 and aa >= aM > 0, so the reference's max with 0 and with
+    // the smallest subnormal return their first operand
+    const T am = nnmin(ar_, ai_);
+    const T aM = nnmax(ar_, ai_);
+    T aa = qdiv(am, aM);
+    aa = sqrt_ge1(F::fma_(aa, aa, one)) * aM;
+    ar_ = vor(nnmin(qdiv(ar_, aa), one), as);
+    ai_ = qdiv(ai, aa);
+    const T ab = addexp(aa, 1);
+    T ad;
+    const angle<T> g = jac_angle<T, true>(a1, a2, ab, ad);
+    t1 = g.t1; s2 = g.s2; s1 = g.s1;
+    L1 = qdiv(F::fma_(t1, F::fma_(a2, t1, ab), a1), s2);
+    L2 = qdiv(F::fma_(t1, F::fma_(a1, t1, -ab), a2), s2);
+    l1 = scale2_nr(L1, -es);
+    l2 = scale2_nr(L2, -es);
+    fin = true;
+  }
+  else if (all_finite3(a1, a2, ar) && visfinite(ai)) {
     const int es = min(min(1 << 20, min(escale(a1), escale(a2))), min(escale(ar), escale(ai)));
     ar = scale2(ar, es);
     ai = scale2(ai, es);
@@ -189,7 +298,7 @@ __device__ __forceinline__ unsigned cjac2(T a1, T a2, T ar, T ai, T &c, T &cat, 
   }
   cat = ar_;
   sat = ai_;
-  return (L1 < L2) ? 1u : 0u;
+  return (fin ? lt_fin(L1, L2) : (L1 < L2)) ? 1u : 0u;
 }
 
 }  // namespace vj
