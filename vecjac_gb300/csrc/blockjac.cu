@@ -113,8 +113,9 @@ __device__ __forceinline__ void block_pair(int nb, int s, int k, int &I, int &J)
 
 // ---------------------------------------------------------------- Gram matrices
 // CTA (pair, split): S_part = X[k0:k1]^T X[k0:k1] for the pair's 128 real columns, rows
-// k0..k1 of this split. 128 threads: thread t converts real column t; thread 0 issues the
-// MMAs. Two operand stages (A = B: the Gram tile is its own B operand), 96 KiB.
+// k0..k1 of this split. 128 threads: thread t converts real column t (the next chunk's 64
+// values are loaded into registers while the current one is split and stored); thread 0
+// issues the MMAs. Two operand stages (A = B: the Gram tile is its own B operand), 96 KiB.
 template <int NT>
 __global__ void __launch_bounds__(128) k_gram(Cols X, int m, int nb, int step, int ksplit, float *Spart,
                                                unsigned *err)
@@ -144,11 +145,35 @@ __global__ void __launch_bounds__(128) k_gram(Cols X, int m, int nb, int step, i
   tc::fence_after();
   const uint32_t tmem = tslot;
   const float *col = pair_col(X, I, J, tid);
+  // rows k0 .. k0 + 63 of this thread's column (zeros past m)
+  auto load = [&](int it, float (&v)[KC]) {
+    const int k0 = (c0 + it) * KC;
+    if (k0 + KC <= m) {
+#pragma unroll
+      for (int g = 0; g < KC / 4; ++g) {
+        const float4 a = *reinterpret_cast<const float4 *>(col + k0 + 4 * g);
+        v[4 * g] = a.x;
+        v[4 * g + 1] = a.y;
+        v[4 * g + 2] = a.z;
+        v[4 * g + 3] = a.w;
+      }
+    }
+    else {
+#pragma unroll
+      for (int e = 0; e < KC; ++e)
+        v[e] = (k0 + e < m) ? col[k0 + e] : 0.f;
+    }
+  };
+  float cur[KC], nxt[KC];
+  if (nch > 0)
+    load(0, cur);
   bool ok = true;
   int issued = 0;  // chunks whose MMAs were issued
   for (int it = 0; it < nch; ++it) {
     const int s = it & 1;
     unsigned char *st = smem + s * 3 * PLANE;
+    if (it + 1 < nch)
+      load(it + 1, nxt);
     // the MMAs of chunk it - 2 have read stage s; a wait that gives up ends the loop for
     // the whole CTA (nothing more is issued)
     const bool w = (it >= 2) ? tc::mbar_wait(&bar[s], (uint32_t)(((it >> 1) - 1) & 1), WAIT_CYCLES) : true;
@@ -156,23 +181,10 @@ __global__ void __launch_bounds__(128) k_gram(Cols X, int m, int nb, int step, i
       ok = false;
       break;
     }
-    const int k0 = (c0 + it) * KC;
-#pragma unroll 2
-    for (int g = 0; g < KC / 8; ++g) {
-      const int r = k0 + 8 * g;
-      float v[8];
-      if (r + 8 <= m) {
-        const float4 a = *reinterpret_cast<const float4 *>(col + r);
-        const float4 c = *reinterpret_cast<const float4 *>(col + r + 4);
-        v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
-        v[4] = c.x; v[5] = c.y; v[6] = c.z; v[7] = c.w;
-      }
-      else {
 #pragma unroll
-        for (int e = 0; e < 8; ++e)
-          v[e] = (r + e < m) ? col[r + e] : 0.f;
-      }
-      store_split8(st + tile_off(tid, 8 * g), v);
+    for (int g = 0; g < KC / 8; ++g) {
+      const float(&v8)[8] = *reinterpret_cast<const float(*)[8]>(cur + 8 * g);
+      store_split8(st + tile_off(tid, 8 * g), v8);
     }
     tc::fence_proxy_async();
     __syncthreads();
@@ -190,6 +202,9 @@ __global__ void __launch_bounds__(128) k_gram(Cols X, int m, int nb, int step, i
       tc::commit(&bar[s]);
     }
     issued = it + 1;
+#pragma unroll
+    for (int e = 0; e < KC; ++e)
+      cur[e] = nxt[e];
   }
   // every issued chunk complete (commits complete in order; a second bounded wait after a
   // failed one, so that no MMA is in flight when the TMEM is released)
@@ -230,28 +245,28 @@ __global__ void __launch_bounds__(128) k_gram(Cols X, int m, int nb, int step, i
 }
 
 // ---------------------------------------------------------------- block rotations
-// CTA (pair, row tile): rows r0..r0+127 of the pair's 128 real columns of G (tiles
-// 0..tg-1) or of W (tiles tg..): Y = X R with R's split image (2 K stages x 3 terms of
-// 128 x 64 BF16, 96 KiB per pair) copied in by TMA, X converted by the threads; Y replaces
-// X in place (each CTA reads all of its tile before any of it is written).
+// CTA (pair, q): the row tiles q, q + Q, q + 2Q, ... of the pair's 128 real columns of G
+// (tiles 0..tg-1, 128 rows each) and of W (tiles tg..tg+tw-1): Y = X R, Y replacing X in
+// place. R's split image (2 K stages x 3 terms of 128 x 64 BF16, 96 KiB) is copied in once
+// by TMA; each tile of X is converted by the 256 threads (thread t: row t % 128, K half
+// t / 128), multiplied into one of two TMEM accumulators, and written back while the next
+// tile's product runs. Each CTA reads all of a tile before any of it is written, and the
+// tiles of a pair are disjoint rows.
+constexpr int APPLY_THREADS = 256;
 template <int NT>
-__global__ void __launch_bounds__(128) k_apply(Cols G, int m, Cols W, int n, int nb, int step, int tg, int tw,
-                                                const unsigned char *Rimg, unsigned *err)
+__global__ void __launch_bounds__(APPLY_THREADS) k_apply(Cols G, int m, Cols W, int n, int nb, int step, int tg,
+                                                         int tw, int Q, const unsigned char *Rimg, unsigned *err)
 {
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char *smem = smem_raw + ((1024u - (tc::saddr(smem_raw) & 1023u)) & 1023u);
-  __shared__ unsigned long long bar[2];  // 0: TMA of R, 1: MMA completion
+  unsigned char *Rs = smem, *As = smem + 6 * PLANE;  // R: [stage][term]; A: [stage][term]
+  __shared__ unsigned long long bar[2];  // 0: TMA of R, 1: MMA completion (one phase per tile)
   __shared__ uint32_t tslot;
   const int tid = threadIdx.x, warp = tid >> 5;
-  const int per_pair = tg + tw;
-  const int pair = blockIdx.x / per_pair, tile = blockIdx.x % per_pair;
-  const bool onG = tile < tg;
-  const Cols &X = onG ? G : W;
-  const int rows = onG ? m : n;
-  const int r0 = (onG ? tile : tile - tg) * TILE;
+  const int pair = blockIdx.x / Q, q0 = blockIdx.x % Q;
+  const int ntile = tg + tw;
   int I, J;
   block_pair(nb, step, pair, I, J);
-  // smem: stage s at s * 6 PLANE: A terms (3 PLANE), then R terms (3 PLANE)
   if (tid == 0) {
     tc::mbar_init1(&bar[0]);
     tc::mbar_init1(&bar[1]);
@@ -259,7 +274,7 @@ __global__ void __launch_bounds__(128) k_apply(Cols G, int m, Cols W, int n, int
   }
   __syncwarp();
   if (warp == 0)
-    tc::tmem_alloc(&tslot, TILE);
+    tc::tmem_alloc(&tslot, 2 * TILE);
   tc::fence_before();
   __syncthreads();
   tc::fence_after();
@@ -267,64 +282,113 @@ __global__ void __launch_bounds__(128) k_apply(Cols G, int m, Cols W, int n, int
   if (tid == 0) {
     mbar_expect_tx(&bar[0], 6u * PLANE);
     const unsigned char *src = Rimg + (size_t)pair * 6 * PLANE;
-    tma_load_1d(smem + 3 * PLANE, src, 3u * PLANE, &bar[0]);
-    tma_load_1d(smem + 9 * PLANE, src + 3 * PLANE, 3u * PLANE, &bar[0]);
+    tma_load_1d(Rs, src, 3u * PLANE, &bar[0]);
+    tma_load_1d(Rs + 3 * PLANE, src + 3 * PLANE, 3u * PLANE, &bar[0]);
   }
-  const int row = r0 + tid;
-  const bool live = row < rows;
+  const int row = tid & (TILE - 1), half = tid >> 7;
+  bool ok = true, rready = false;
+  auto tile_of = [&](int t, const Cols *&X, int &rows, int &r0) {
+    const bool onG = t < tg;
+    X = onG ? &G : &W;
+    rows = onG ? m : n;
+    r0 = (onG ? t : t - tg) * TILE;
+  };
+  // write back tile t from TMEM buffer b: warp w reads lanes 32 (w % 4) .. + 31 (rows),
+  // columns 64 (w / 4) .. + 63
+  auto epilogue = [&](int t, int b) {
+    const Cols *X;
+    int rows, r0;
+    tile_of(t, X, rows, r0);
+    const int r = r0 + 32 * (warp & 3) + (tid & 31);
 #pragma unroll 1
-  for (int s = 0; s < 2; ++s) {
-    unsigned char *st = smem + s * 6 * PLANE;
-#pragma unroll 1
-    for (int g = 0; g < KC / 8; ++g) {
-      float v[8];
+    for (int c = 64 * (warp >> 2); c < 64 * (warp >> 2) + 64; c += 32) {
+      uint32_t v[32];
+      tc::tmem_ld32(tmem + (uint32_t)(b * TILE) + ((uint32_t)(32 * (warp & 3)) << 16) + (uint32_t)c, v);
+      if (r < rows) {
 #pragma unroll
-      for (int e = 0; e < 8; ++e)
-        v[e] = live ? pair_col(X, I, J, s * KC + 8 * g + e)[row] : 0.f;
-      store_split8(st + tile_off(tid, 8 * g), v);
+        for (int e = 0; e < 32; ++e)
+          pair_col(*X, I, J, c + e)[r] = __uint_as_float(v[e]);
+      }
     }
-  }
-  tc::fence_proxy_async();
-  __syncthreads();
-  bool ok = true;
-  if (tid == 0) {
-    ok = tc::mbar_wait(&bar[0], 0u, WAIT_CYCLES);
-    if (!ok)  // the copy did not arrive: wait once more so that it is not in flight at exit
-      tc::mbar_wait(&bar[0], 0u, WAIT_CYCLES);
-    tc::fence_after();
+  };
+  int done = 0;  // tiles whose MMAs were committed
+  for (int t = q0, k = 0; t < ntile; t += Q, ++k) {
+    // the previous tile's MMAs have read the A buffer
+    if (k > 0) {
+      const bool w = tc::mbar_wait(&bar[1], (uint32_t)((k - 1) & 1), WAIT_CYCLES);
+      if (!__syncthreads_and(w)) {
+        ok = false;
+        break;
+      }
+      tc::fence_after();
+    }
+    {
+      const Cols *X;
+      int rows, r0;
+      tile_of(t, X, rows, r0);
+      const int gr = r0 + row;
+      const bool live = gr < rows;
+      float v[KC];
+#pragma unroll
+      for (int e = 0; e < KC; ++e)
+        v[e] = live ? pair_col(*X, I, J, half * KC + e)[gr] : 0.f;
+      unsigned char *st = As + half * 3 * PLANE;
+#pragma unroll
+      for (int g = 0; g < KC / 8; ++g) {
+        const float(&v8)[8] = *reinterpret_cast<const float(*)[8]>(v + 8 * g);
+        store_split8(st + tile_off(row, 8 * g), v8);
+      }
+    }
+    tc::fence_proxy_async();
+    tc::fence_before();
+    __syncthreads();
+    if (tid == 0) {
+      if (!rready) {
+        rready = tc::mbar_wait(&bar[0], 0u, WAIT_CYCLES);
+        if (!rready)  // the copy did not arrive: wait once more so that it is not in flight at exit
+          tc::mbar_wait(&bar[0], 0u, WAIT_CYCLES);
+      }
+      tc::fence_after();
+      if (rready) {
+        const uint32_t d = tmem + (uint32_t)((k & 1) * TILE);
 #pragma unroll 1
-    for (int s = 0; s < 2 && ok; ++s) {
-      const uint32_t a0 = tc::saddr(smem + s * 6 * PLANE), b0 = a0 + 3 * PLANE;
+        for (int s2 = 0; s2 < 2; ++s2) {
+          const uint32_t a0 = tc::saddr(As + s2 * 3 * PLANE), b0 = tc::saddr(Rs + s2 * 3 * PLANE);
 #pragma unroll
-      for (int kk = 0; kk < KC / 16; ++kk)
+          for (int kk = 0; kk < KC / 16; ++kk)
 #pragma unroll
-        for (int t = 6 - NT; t < 6; ++t) {
-          const uint64_t ad = tc::sdesc(a0 + TA[t] * PLANE + kk * 2 * LBO, LBO, SBO);
-          const uint64_t bd = tc::sdesc(b0 + TB[t] * PLANE + kk * 2 * LBO, LBO, SBO);
-          tc::mma_bf16(tmem, ad, bd, IDESC, (s > 0 || kk > 0 || t > 6 - NT) ? 1u : 0u);
+            for (int tt = 6 - NT; tt < 6; ++tt) {
+              const uint64_t ad = tc::sdesc(a0 + TA[tt] * PLANE + kk * 2 * LBO, LBO, SBO);
+              const uint64_t bd = tc::sdesc(b0 + TB[tt] * PLANE + kk * 2 * LBO, LBO, SBO);
+              tc::mma_bf16(d, ad, bd, IDESC, (s2 > 0 || kk > 0 || tt > 6 - NT) ? 1u : 0u);
+            }
         }
+      }
+      tc::commit(&bar[1]);
     }
-    tc::commit(&bar[1]);
+    done = k + 1;
+    if (!__syncthreads_or(tid == 0 && !rready)) {
+      // write back the previous tile while this one's product runs
+      if (k > 0) {
+        __syncwarp();
+        epilogue(t - Q, (k - 1) & 1);
+      }
+    }
+    else {
+      ok = false;
+      break;
+    }
   }
-  {
-    bool w = tc::mbar_wait(&bar[1], 0u, WAIT_CYCLES);
+  // the last tile: its product complete, then written back
+  if (done > 0) {
+    bool w = tc::mbar_wait(&bar[1], (uint32_t)((done - 1) & 1), WAIT_CYCLES);
     if (!w)
-      w = tc::mbar_wait(&bar[1], 0u, WAIT_CYCLES);
-    ok = w && ok;
-  }
-  // a CTA whose copy or MMAs failed writes nothing back
-  ok = __syncthreads_and(ok) != 0;
-  tc::fence_after();
-  __syncwarp();
-#pragma unroll 1
-  for (int c = 0; c < TILE && ok; c += 32) {
-    uint32_t r[32];
-    tc::tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c, r);
-    if (live) {
-#pragma unroll
-      for (int e = 0; e < 32; ++e)
-        pair_col(X, I, J, c + e)[row] = __uint_as_float(r[e]);
-    }
+      w = tc::mbar_wait(&bar[1], (uint32_t)((done - 1) & 1), WAIT_CYCLES);
+    ok = __syncthreads_and(w && ok) != 0;
+    tc::fence_after();
+    __syncwarp();
+    if (ok)
+      epilogue(q0 + (done - 1) * Q, (done - 1) & 1);
   }
   if (!ok)
     atomicOr(err, 1u);
@@ -333,7 +397,7 @@ __global__ void __launch_bounds__(128) k_apply(Cols G, int m, Cols W, int n, int
   tc::fence_after();
   __syncwarp();
   if (warp == 0)
-    tc::tmem_dealloc(tmem, TILE);
+    tc::tmem_dealloc(tmem, 2 * TILE);
 }
 
 // the split image of the real 128 x 128 rotation Rb (Rb[k][i], k = input column, i = output
@@ -353,34 +417,90 @@ __device__ __forceinline__ void write_rimg(unsigned char *img, F rb)
 }
 
 // ---------------------------------------------------------------- pair eigenproblems
-// One CTA per block pair: sums the split Gram partials, forms H (complex 64 x 64 from the
-// real Gram of [Re | Im], or real 128 x 128), runs `sweeps` cyclic Jacobi sweeps on H with
-// the rotation accumulated in R (R := I first), orders R's columns by descending diagonal
-// of the final H, and writes R's split image for k_apply. stats[0] += rotations,
-// stats[1] = max over rotated pairs of |h_pq| / sqrt(h_pp h_qq) (as float bits).
+// Rotation of one pair (p, q) of the Hermitian H from h_pp = a, h_qq = b, h_pq = c (the
+// scalar sweep's formulas: zeta = (b - a) / (2|c|), t the smaller root of t^2 + 2 zeta t = 1,
+// cs = 1 / sqrt(1 + t^2), s = t cs c / |c|), with fast approximate division and reciprocal
+// square roots refined by one Newton step: these sweeps are a preconditioner, and the same
+// rotation is applied to G and W, so a rotation a few ulps from unitary changes nothing
+// but the accumulated W's orthogonality, which the FP64 Newton-Schulz steps restore.
+struct Rot {
+  float c, sr, si, d1, d2;
+  int go;
+};
+__device__ __forceinline__ float rsqrt_nr(float x)
+{
+  const float y = rsqrtf(x);
+  return y * fmaf(-0.5f * x, y * y, 1.5f);
+}
+__device__ __forceinline__ Rot pair_rot(float ha, float hb, float cr, float ci, float tol)
+{
+  Rot r{1.f, 0.f, 0.f, ha, hb, 0};
+  const float ar = fabsf(cr), ai = fabsf(ci);
+  const float am = fmaxf(ar, ai), an = fminf(ar, ai);
+  if (!(am > 0.f))
+    return r;
+  const float qn = __fdividef(an, am);
+  const float ac = am * (fmaf(qn, qn, 1.f) * rsqrt_nr(fmaf(qn, qn, 1.f)));  // |c|
+  const float sc = sqrtf(ha) * sqrtf(hb);
+  if (!(ac >= tol * sc))
+    return r;
+  const float zeta = __fdividef(hb - ha, 2.f * ac);
+  const float az = fabsf(zeta);
+  const float t = (az > 1e18f) ? __fdividef(0.5f, zeta)
+                               : copysignf(1.f, zeta) / (az + fmaf(az, az, 1.f) * rsqrt_nr(fmaf(az, az, 1.f)));
+  const float cs = rsqrt_nr(fmaf(t, t, 1.f));
+  const float sn = t * cs, ia = __fdividef(1.f, ac);
+  r.c = cs;
+  r.sr = sn * (cr * ia);
+  r.si = sn * (ci * ia);
+  r.d1 = ha - t * ac;
+  r.d2 = hb + t * ac;
+  r.go = 1;
+  return r;
+}
+
+// One CTA (512 threads) per block pair: sums the split Gram partials, forms H (complex
+// 64 x 64 from the real Gram of [Re | Im], or real 128 x 128), runs `sweeps` cyclic
+// Jacobi sweeps on H with the rotation accumulated in R (R := I first), orders R's columns
+// by descending diagonal of the final H, and writes R's split image for k_apply.
+// stats[0] += rotations, stats[1] = max over rotated pairs of |h_pq| / sqrt(h_pp h_qq)
+// (as float bits).
+// Per Jacobi step: every warp reads the step's pairs (lane u: pair u, and u + 32 for real
+// data) and, after a barrier (no H entry is written before all are read), computes their
+// rotations into its own slice of shared memory; then the threads update the 2x2 blocks
+// (u <= v) of H := J^H H J from a precomputed triangular list and the columns of R := R J;
+// a second barrier ends the step.
+constexpr int EVD_THREADS = 512;
 template <bool CPLX>
-__global__ void __launch_bounds__(256) k_pair_evd(const float *Spart, int ksplit, int sweeps, float tol,
-                                                   unsigned char *Rimg, unsigned *stats)
+__global__ void __launch_bounds__(EVD_THREADS) k_pair_evd(const float *Spart, int ksplit, int sweeps, float tol,
+                                                          unsigned char *Rimg, unsigned *stats)
 {
   constexpr int N = CPLX ? 64 : 128;  // order of H
   constexpr int P = N / 2;             // pairs per Jacobi step
+  constexpr int PL = P / 32;           // pairs per lane
   constexpr int LD = N + 1;
+  constexpr int NB = P * (P + 1) / 2;  // blocks u <= v
+  constexpr int NW = EVD_THREADS / 32;
   extern __shared__ __align__(16) float fsm[];
   float *Hr = fsm, *Hi = Hr + N * LD;
   float *Rr = Hi + (CPLX ? N * LD : 0), *Ri = Rr + N * LD;
-  float *rot = Ri + (CPLX ? N * LD : 0);  // 5 P: cs, sr, si, dpp, dqq
-  float *cs = rot, *sr = rot + P, *si = rot + 2 * P, *dpp = rot + 3 * P, *dqq = rot + 4 * P;
-  int *pp = reinterpret_cast<int *>(rot + 5 * P), *qq = pp + P, *act = qq + P;
-  int *rank = act + P;
+  float *wrot = Ri + (CPLX ? N * LD : 0);  // per warp: 3 P (c, sr, si) + 2 P (d1, d2)
+  unsigned short *tri = reinterpret_cast<unsigned short *>(wrot + NW * 5 * P);  // NB entries: u << 8 | v
+  int *rank = reinterpret_cast<int *>(tri + ((NB + 1) & ~1));
   __shared__ unsigned nrot_s, mu_s;
-  const int tid = threadIdx.x, nt = blockDim.x;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const float *S0 = Spart + (size_t)blockIdx.x * ksplit * TILE * TILE;
   if (tid == 0) {
     nrot_s = 0u;
     mu_s = 0u;
   }
+  for (int q = tid; q < P * P; q += EVD_THREADS) {
+    const int u = q / P, v = q % P;
+    if (u <= v)
+      tri[u * P - u * (u - 1) / 2 + (v - u)] = (unsigned short)((u << 8) | v);
+  }
   // S = sum of the partials; H from S (upper triangle, mirrored: exactly Hermitian)
-  for (int q = tid; q < N * N; q += nt) {
+  for (int q = tid; q < N * N; q += EVD_THREADS) {
     const int i = q / N, j = q % N;
     if (i > j)
       continue;
@@ -404,7 +524,7 @@ __global__ void __launch_bounds__(256) k_pair_evd(const float *Spart, int ksplit
       Hr[j * LD + i] = h;
     }
   }
-  for (int q = tid; q < N * N; q += nt) {
+  for (int q = tid; q < N * N; q += EVD_THREADS) {
     const int i = q / N, j = q % N;
     Rr[i * LD + j] = (i == j) ? 1.f : 0.f;
     if (CPLX)
@@ -413,59 +533,84 @@ __global__ void __launch_bounds__(256) k_pair_evd(const float *Spart, int ksplit
   __syncthreads();
   unsigned nrot = 0u;
   float mu = 0.f;
+  float *wr = wrot + warp * 5 * P;
   for (int sw = 0; sw < sweeps; ++sw)
     for (int stp = 0; stp < N - 1; ++stp) {
-      if (tid < P) {
+      // the step's pairs and their entries (lane u: pairs u, u + 32)
+      float va[PL], vb[PL], vr[PL], vi[PL];
+      int vp[PL], vq[PL];
+#pragma unroll
+      for (int h = 0; h < PL; ++h) {
+        const int u = lane + 32 * h;
         int a, c;
-        if (tid == 0) {
+        if (u == 0) {
           a = stp;
           c = N - 1;
         }
         else {
-          a = (stp + tid) % (N - 1);
-          c = (stp + (N - 1) - tid) % (N - 1);
+          a = stp + u;
+          a -= (a >= N - 1) ? (N - 1) : 0;
+          c = stp + (N - 1) - u;
+          c -= (c >= N - 1) ? (N - 1) : 0;
         }
-        const int p = a < c ? a : c, q = a < c ? c : a;
-        pp[tid] = p;
-        qq[tid] = q;
-        const float ha = fmaxf(Hr[p * LD + p], 0.f), hb = fmaxf(Hr[q * LD + q], 0.f);
-        const float cr = Hr[p * LD + q], ci = CPLX ? Hi[p * LD + q] : 0.f;
-        const float ac = CPLX ? hypotf(cr, ci) : fabsf(cr);
-        const float sc = sqrtf(ha) * sqrtf(hb);
-        float c_ = 1.f, s_r = 0.f, s_i = 0.f, d1 = ha, d2 = hb;
-        int go = 0;
-        if (ac > 0.f && ac >= tol * sc) {
-          const float zeta = (hb - ha) / (2.f * ac);
-          const float az = fabsf(zeta);
-          const float t = (az > 1e18f) ? 0.5f / zeta : copysignf(1.f, zeta) / (az + sqrtf(fmaf(zeta, zeta, 1.f)));
-          c_ = 1.f / sqrtf(fmaf(t, t, 1.f));
-          const float sn = t * c_;
-          s_r = sn * (cr / ac);
-          s_i = CPLX ? sn * (ci / ac) : 0.f;
-          d1 = ha - t * ac;
-          d2 = hb + t * ac;
-          go = 1;
-          ++nrot;
-          mu = fmaxf(mu, (sc > 0.f) ? ac / sc : 1.f);
-        }
-        cs[tid] = c_;
-        sr[tid] = s_r;
-        si[tid] = s_i;
-        dpp[tid] = d1;
-        dqq[tid] = d2;
-        act[tid] = go;
+        vp[h] = a < c ? a : c;
+        vq[h] = a < c ? c : a;
+        va[h] = fmaxf(Hr[vp[h] * LD + vp[h]], 0.f);
+        vb[h] = fmaxf(Hr[vq[h] * LD + vq[h]], 0.f);
+        vr[h] = Hr[vp[h] * LD + vq[h]];
+        vi[h] = CPLX ? Hi[vp[h] * LD + vq[h]] : 0.f;
       }
       __syncthreads();
-      // H := J^H H J, 2x2 block (u, v) of the step's pairs at a time (u <= v; the (v, u)
-      // block is its conjugate transpose)
-      for (int q = tid; q < P * P; q += nt) {
-        const int u = q / P, v = q % P;
-        if (u > v || !(act[u] | act[v]))
+#pragma unroll
+      for (int h = 0; h < PL; ++h) {
+        const int u = lane + 32 * h;
+        const Rot r = pair_rot(va[h], vb[h], vr[h], vi[h], tol);
+        wr[u] = r.c;
+        wr[P + u] = r.sr;
+        wr[2 * P + u] = r.si;
+        wr[3 * P + u] = r.d1;
+        wr[4 * P + u] = r.d2;
+        if (warp == 0) {
+          if (r.go) {
+            ++nrot;
+            const float sc = sqrtf(va[h]) * sqrtf(vb[h]);
+            mu = fmaxf(mu, (sc > 0.f) ? hypotf(vr[h], vi[h]) / sc : 1.f);
+          }
+        }
+      }
+      __syncwarp();
+      // the pairs and activity of this step as this warp computed them (all warps compute
+      // the same values): index u of the slice; p, q recomputed from the closed form
+      auto pidx = [&](int u, int &p, int &q) {
+        int a, c;
+        if (u == 0) {
+          a = stp;
+          c = N - 1;
+        }
+        else {
+          a = stp + u;
+          a -= (a >= N - 1) ? (N - 1) : 0;
+          c = stp + (N - 1) - u;
+          c -= (c >= N - 1) ? (N - 1) : 0;
+        }
+        p = a < c ? a : c;
+        q = a < c ? c : a;
+      };
+      // H := J^H H J, 2x2 block (u, v), u <= v, at a time; the (v, u) block is its
+      // conjugate transpose
+      for (int q = tid; q < NB; q += EVD_THREADS) {
+        const int u = tri[q] >> 8, v = tri[q] & 255;
+        const float cu = wr[u], sur = wr[P + u], sui = wr[2 * P + u];
+        const float cv = wr[v], svr = wr[P + v], svi = wr[2 * P + v];
+        const bool au = (sur != 0.f) || (sui != 0.f) || (cu != 1.f), av = (svr != 0.f) || (svi != 0.f) || (cv != 1.f);
+        if (!(au || av))
           continue;
-        const int pu = pp[u], qu = qq[u], pv = pp[v], qv = qq[v];
+        int pu, qu, pv, qv;
+        pidx(u, pu, qu);
+        pidx(v, pv, qv);
         if (u == v) {
-          Hr[pu * LD + pu] = dpp[u];
-          Hr[qu * LD + qu] = dqq[u];
+          Hr[pu * LD + pu] = wr[3 * P + u];
+          Hr[qu * LD + qu] = wr[4 * P + u];
           Hr[pu * LD + qu] = 0.f;
           Hr[qu * LD + pu] = 0.f;
           if (CPLX) {
@@ -474,8 +619,6 @@ __global__ void __launch_bounds__(256) k_pair_evd(const float *Spart, int ksplit
           }
           continue;
         }
-        const float cv = cs[v], svr = sr[v], svi = si[v], cu = cs[u], sur = sr[u], sui = si[u];
-        // B = [[b00, b01], [b10, b11]] = H rows (pu, qu), columns (pv, qv)
         float b00r = Hr[pu * LD + pv], b01r = Hr[pu * LD + qv], b10r = Hr[qu * LD + pv], b11r = Hr[qu * LD + qv];
         float b00i = 0.f, b01i = 0.f, b10i = 0.f, b11i = 0.f;
         if (CPLX) {
@@ -514,12 +657,13 @@ __global__ void __launch_bounds__(256) k_pair_evd(const float *Spart, int ksplit
         }
       }
       // R := R J: columns (p_v, q_v) of every row
-      for (int q = tid; q < N * P; q += nt) {
+      for (int q = tid; q < N * P; q += EVD_THREADS) {
         const int r = q / P, v = q % P;
-        if (!act[v])
+        const float cv = wr[v], svr = wr[P + v], svi = wr[2 * P + v];
+        if (svr == 0.f && svi == 0.f && cv == 1.f)
           continue;
-        const int pv = pp[v], qv = qq[v];
-        const float cv = cs[v], svr = sr[v], svi = si[v];
+        int pv, qv;
+        pidx(v, pv, qv);
         const float xr = Rr[r * LD + pv], yr = Rr[r * LD + qv];
         const float xi = CPLX ? Ri[r * LD + pv] : 0.f, yi = CPLX ? Ri[r * LD + qv] : 0.f;
         Rr[r * LD + pv] = cv * xr - (svr * yr + svi * yi);
@@ -531,25 +675,27 @@ __global__ void __launch_bounds__(256) k_pair_evd(const float *Spart, int ksplit
       }
       __syncthreads();
     }
-  // descending order of the diagonal (ties by index): column i of R goes to rank[i]
+  // descending order of the diagonal (ties by index): column rank[r] of R goes to place r
   // (a NaN sorts as -inf, so that the ranks stay a permutation)
   auto key = [&](int i) {
     const float d = Hr[i * LD + i];
     return (d == d) ? d : -INFINITY;
   };
-  for (int i = tid; i < N; i += nt) {
+  for (int i = tid; i < N; i += EVD_THREADS) {
     const float d = key(i);
     int r = 0;
     for (int j = 0; j < N; ++j) {
       const float e = key(j);
       r += (e > d || (e == d && j < i)) ? 1 : 0;
     }
-    rank[r] = i;  // rank[r] = the column of R that goes to position r
+    rank[r] = i;
   }
-  if (nrot)
-    atomicAdd(&nrot_s, nrot);
-  if (mu > 0.f)
-    atomicMax(&mu_s, __float_as_uint(mu));
+  if (warp == 0) {
+    if (nrot)
+      atomicAdd(&nrot_s, nrot);
+    if (mu > 0.f)
+      atomicMax(&mu_s, __float_as_uint(mu));
+  }
   __syncthreads();
   unsigned char *img = Rimg + (size_t)blockIdx.x * 6 * PLANE;
   if (CPLX)
@@ -579,16 +725,17 @@ __global__ void __launch_bounds__(256) k_rimg(const float *R, unsigned char *Rim
 
 static size_t evd_smem(bool cplx)
 {
-  const int N = cplx ? 64 : 128, P = N / 2, LD = N + 1;
-  return (size_t)(cplx ? 4 : 2) * N * LD * 4 + (size_t)5 * P * 4 + (size_t)3 * P * 4 + (size_t)N * 4;
+  const int N = cplx ? 64 : 128, P = N / 2, LD = N + 1, NB = P * (P + 1) / 2;
+  return (size_t)(cplx ? 4 : 2) * N * LD * 4 + (size_t)(EVD_THREADS / 32) * 5 * P * 4 + (size_t)((NB + 1) & ~1) * 2 +
+         (size_t)N * 4;
 }
 
 constexpr size_t GRAM_SMEM = 2 * 3 * PLANE + 1024;
-constexpr size_t APPLY_SMEM = 2 * 6 * PLANE + 1024;
+constexpr size_t APPLY_SMEM = 2 * 6 * PLANE + 1024;  // R image + one A tile (both K stages)
 
 // ---------------------------------------------------------------- host side
 struct Plan {
-  int nb, npairs, ksplit, tg, tw, b;
+  int nb, npairs, ksplit, tg, tw, b, q;  // q: CTAs per pair of k_apply
   bool cplx;
 };
 
@@ -636,6 +783,11 @@ static Plan plan(bool cplx, long long m, long long n)
   p.ksplit = ks;
   p.tg = (int)((m + TILE - 1) / TILE);
   p.tw = (int)((n + TILE - 1) / TILE);
+  // k_apply: one CTA per SM (its shared memory), the pair's row tiles spread over q CTAs
+  int q = sms / p.npairs;
+  if (q > p.tg + p.tw)
+    q = p.tg + p.tw;
+  p.q = (q < 1) ? 1 : q;
   return p;
 }
 
@@ -680,14 +832,14 @@ long long block_sweep(bool cplx, int m, int n, float *Gr, float *Gi, long long l
     else
       k_gram<6><<<p.npairs * p.ksplit, 128, GRAM_SMEM, s>>>(G, m, p.nb, step, p.ksplit, Spart, stats + 2);
     if (cplx)
-      k_pair_evd<true><<<p.npairs, 256, evd_smem(true), s>>>(Spart, p.ksplit, inner, tol, Rimg, stats);
+      k_pair_evd<true><<<p.npairs, EVD_THREADS, evd_smem(true), s>>>(Spart, p.ksplit, inner, tol, Rimg, stats);
     else
-      k_pair_evd<false><<<p.npairs, 256, evd_smem(false), s>>>(Spart, p.ksplit, inner, tol, Rimg, stats);
+      k_pair_evd<false><<<p.npairs, EVD_THREADS, evd_smem(false), s>>>(Spart, p.ksplit, inner, tol, Rimg, stats);
     if (terms == 3)
-      k_apply<3><<<p.npairs * (p.tg + p.tw), 128, APPLY_SMEM, s>>>(G, m, W, n, p.nb, step, p.tg, p.tw, Rimg,
+      k_apply<3><<<p.npairs * p.q, APPLY_THREADS, APPLY_SMEM, s>>>(G, m, W, n, p.nb, step, p.tg, p.tw, p.q, Rimg,
                                                                     stats + 2);
     else
-      k_apply<6><<<p.npairs * (p.tg + p.tw), 128, APPLY_SMEM, s>>>(G, m, W, n, p.nb, step, p.tg, p.tw, Rimg,
+      k_apply<6><<<p.npairs * p.q, APPLY_THREADS, APPLY_SMEM, s>>>(G, m, W, n, p.nb, step, p.tg, p.tw, p.q, Rimg,
                                                                     stats + 2);
   }
   unsigned hs[4] = {0u, 0u, 0u, 0u};
@@ -795,10 +947,12 @@ extern "C" vj_fint vj_block_apply_dev(int cplx, vj_fnat m, vj_fnat n, float *Gr,
   if (ok) {
     k_rimg<<<p.npairs, 256, 0, s>>>(R, img);
     if (terms == 3)
-      k_apply<3><<<p.npairs * (p.tg + p.tw), 128, APPLY_SMEM, s>>>(G, (int)m, W, (int)n, p.nb, step, p.tg, p.tw, img,
+      k_apply<3><<<p.npairs * p.q, APPLY_THREADS, APPLY_SMEM, s>>>(G, (int)m, W, (int)n, p.nb, step, p.tg, p.tw, p.q,
+                                                                      img,
                                                                     err);
     else
-      k_apply<6><<<p.npairs * (p.tg + p.tw), 128, APPLY_SMEM, s>>>(G, (int)m, W, (int)n, p.nb, step, p.tg, p.tw, img,
+      k_apply<6><<<p.npairs * p.q, APPLY_THREADS, APPLY_SMEM, s>>>(G, (int)m, W, (int)n, p.nb, step, p.tg, p.tw, p.q,
+                                                                      img,
                                                                     err);
     ok = cudaGetLastError() == cudaSuccess;
   }
