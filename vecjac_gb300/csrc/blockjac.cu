@@ -54,26 +54,35 @@ __device__ __forceinline__ int tile_off(int r, int k)
   return (r >> 3) * SBO + (k >> 3) * LBO + (r & 7) * 16 + (k & 7) * 2;
 }
 
-// x = h + m + l exactly, each a BF16 (FP32 inputs of normal or zero magnitude)
-__device__ __forceinline__ void split3(float x, __nv_bfloat16 &h, __nv_bfloat16 &m, __nv_bfloat16 &l)
+// x = h + m + l exactly, each a BF16 (for FP32 inputs of normal or zero magnitude), two
+// values at a time: cvt.rn.bf16x2.f32 rounds a pair into one 32-bit word, and a BF16 back to
+// FP32 is its bits shifted up by 16
+__device__ __forceinline__ uint32_t pack_bf16x2(float lo, float hi)
 {
-  h = __float2bfloat16_rn(x);
-  const float r1 = x - __bfloat162float(h);
-  m = __float2bfloat16_rn(r1);
-  const float r2 = r1 - __bfloat162float(m);
-  l = __float2bfloat16_rn(r2);
+  uint32_t r;
+  asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(r) : "f"(hi), "f"(lo));
+  return r;
+}
+__device__ __forceinline__ void split3x2(float x0, float x1, uint32_t &h, uint32_t &m, uint32_t &l)
+{
+  h = pack_bf16x2(x0, x1);
+  const float r0 = x0 - __uint_as_float(h << 16), r1 = x1 - __uint_as_float(h & 0xFFFF0000u);
+  m = pack_bf16x2(r0, r1);
+  const float s0 = r0 - __uint_as_float(m << 16), s1 = r1 - __uint_as_float(m & 0xFFFF0000u);
+  l = pack_bf16x2(s0, s1);
 }
 
 // the three BF16 terms of 8 values, stored as 16 bytes each at p0, p0 + PLANE, p0 + 2 PLANE
 __device__ __forceinline__ void store_split8(unsigned char *p0, const float (&v)[8])
 {
-  __align__(16) __nv_bfloat16 t[3][8];
-#pragma unroll
-  for (int e = 0; e < 8; ++e)
-    split3(v[e], t[0][e], t[1][e], t[2][e]);
-#pragma unroll
-  for (int s = 0; s < 3; ++s)
-    *reinterpret_cast<uint4 *>(p0 + s * PLANE) = *reinterpret_cast<const uint4 *>(t[s]);
+  uint4 h, m, l;
+  split3x2(v[0], v[1], h.x, m.x, l.x);
+  split3x2(v[2], v[3], h.y, m.y, l.y);
+  split3x2(v[4], v[5], h.z, m.z, l.z);
+  split3x2(v[6], v[7], h.w, m.w, l.w);
+  *reinterpret_cast<uint4 *>(p0) = h;
+  *reinterpret_cast<uint4 *>(p0 + PLANE) = m;
+  *reinterpret_cast<uint4 *>(p0 + 2 * PLANE) = l;
 }
 
 // planar FP32 matrix and the block layout of its columns
@@ -439,20 +448,22 @@ __device__ __forceinline__ Rot pair_rot(float ha, float hb, float cr, float ci, 
   const float am = fmaxf(ar, ai), an = fminf(ar, ai);
   if (!(am > 0.f))
     return r;
-  const float qn = __fdividef(an, am);
+  // (IEEE quotients: the entries of small columns' Gram blocks can be subnormal, where the
+  // approximate division flushes to zero)
+  const float qn = an / am;
   const float ac = am * (fmaf(qn, qn, 1.f) * rsqrt_nr(fmaf(qn, qn, 1.f)));  // |c|
   const float sc = sqrtf(ha) * sqrtf(hb);
   if (!(ac >= tol * sc))
     return r;
-  const float zeta = __fdividef(hb - ha, 2.f * ac);
+  const float zeta = (hb - ha) / (2.f * ac);
   const float az = fabsf(zeta);
-  const float t = (az > 1e18f) ? __fdividef(0.5f, zeta)
+  const float t = (az > 1e18f) ? 0.5f / zeta
                                : copysignf(1.f, zeta) / (az + fmaf(az, az, 1.f) * rsqrt_nr(fmaf(az, az, 1.f)));
   const float cs = rsqrt_nr(fmaf(t, t, 1.f));
-  const float sn = t * cs, ia = __fdividef(1.f, ac);
+  const float sn = t * cs;
   r.c = cs;
-  r.sr = sn * (cr * ia);
-  r.si = sn * (ci * ia);
+  r.sr = sn * (cr / ac);
+  r.si = sn * (ci / ac);
   r.d1 = ha - t * ac;
   r.d2 = hb + t * ac;
   r.go = 1;

@@ -83,9 +83,13 @@ __device__ __forceinline__ int okey(float x)
   const int u = (int)fp<float>::bits(x);
   return (u < 0) ? -(u & 0x7fffffff) : u;
 }
-template <typename T> __device__ __forceinline__ bool lt_fin(T a, T b) { return okey(a) < okey(b); }
-template <typename T> __device__ __forceinline__ T nnmin(T a, T b) { return (fp<T>::bits(a) < fp<T>::bits(b)) ? a : b; }
-template <typename T> __device__ __forceinline__ T nnmax(T a, T b) { return (fp<T>::bits(a) > fp<T>::bits(b)) ? a : b; }
+// (FP32 compares on the wide FP32 pipe: the plain comparison, identical for finite values)
+__device__ __forceinline__ bool lt_fin(double a, double b) { return okey(a) < okey(b); }
+__device__ __forceinline__ bool lt_fin(float a, float b) { return a < b; }
+__device__ __forceinline__ double nnmin(double a, double b) { return (fp<double>::bits(a) < fp<double>::bits(b)) ? a : b; }
+__device__ __forceinline__ double nnmax(double a, double b) { return (fp<double>::bits(a) > fp<double>::bits(b)) ? a : b; }
+__device__ __forceinline__ float nnmin(float a, float b) { return fminf(a, b); }
+__device__ __forceinline__ float nnmax(float a, float b) { return fmaxf(a, b); }
 // square root of 1 <= x < 2^EMAX: FP64 with the few-FP64-operation routine of dsqrt.cuh,
 // FP32 with the FP32 unit's correctly rounded root
 __device__ __forceinline__ double sqrt_ge1(double x) { return dsqrt_pos(x); }
