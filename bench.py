@@ -741,7 +741,7 @@ def bench_mixed(args, vj, dist, rank, world, kind, m, n):
            "value": round(world * 1000.0 / ms, 5), "unit": "matrices/s", "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic (Haar factors, log-uniform sigma in [%g, 1])" % (1e-8 if cx else 1e-6),
-           "config": {"workload": "%svjsvd_ %dx%d mixed precision (FP32 presweep rounds, each with 2 Newton-Schulz "
+           "config": {"workload": "%svjsvd_ %dx%d mixed precision (FP32 block-sweep rounds, each with Newton-Schulz "
                                   "steps, then FP64 finishing sweeps), pivot strategy id %d" % (kind, m, n, args.pivot),
                       "stages": args.stages or 2,
                       "sweeps_fp32": int(sw32), "sweeps_fp64_plain_dot": int(swf), "sweeps_fp64": int(sw64),

@@ -126,7 +126,8 @@ vj_fint vj_cvjsvd_dev(vj_fnat m, vj_fnat n, float *Gr, vj_fnat ldGr, float *Gi, 
 
 /* Mixed-precision SVD (FP64 data, result to FP64 accuracy): `stages` rounds (0: 2) of FP32
  * one-sided Jacobi sweeps on the current G rounded to FP32, each followed by FP64
- * re-orthogonalisation of the accumulated rotation W (two Newton-Schulz steps) and the
+ * re-orthogonalisation of the accumulated rotation W (2 to 5 Newton-Schulz steps, as its
+ * distance from unitarity needs) and the
  * FP64 products G := G W, V := V W; FP64 sweeps with plain dot products on G and V to
  * twice the reference's tolerance; then FP64 finishing sweeps of dvjsvd_/zvjsvd_ with V
  * preset (the reference's iwork[0] != 0 mode, src/dvjsvd.c:88-96, src/zvjsvd.c:100-110).

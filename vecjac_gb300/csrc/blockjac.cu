@@ -173,23 +173,18 @@ __global__ void __launch_bounds__(128) k_gram(Cols X, int m, int nb, int step, i
         v[e] = (k0 + e < m) ? col[k0 + e] : 0.f;
     }
   };
-  float cur[KC], nxt[KC];
-  if (nch > 0)
-    load(0, cur);
-  bool ok = true;
   int issued = 0;  // chunks whose MMAs were issued
-  for (int it = 0; it < nch; ++it) {
+  // chunk it from the registers cur while chunk it + 1 loads into nxt; false (for the whole
+  // CTA) when the wait for a stage gave up
+  auto one = [&](int it, float (&cur)[KC], float (&nxt)[KC]) -> bool {
     const int s = it & 1;
     unsigned char *st = smem + s * 3 * PLANE;
     if (it + 1 < nch)
       load(it + 1, nxt);
-    // the MMAs of chunk it - 2 have read stage s; a wait that gives up ends the loop for
-    // the whole CTA (nothing more is issued)
+    // the MMAs of chunk it - 2 have read stage s
     const bool w = (it >= 2) ? tc::mbar_wait(&bar[s], (uint32_t)(((it >> 1) - 1) & 1), WAIT_CYCLES) : true;
-    if (!__syncthreads_and(w)) {
-      ok = false;
-      break;
-    }
+    if (!__syncthreads_and(w))
+      return false;
 #pragma unroll
     for (int g = 0; g < KC / 8; ++g) {
       const float(&v8)[8] = *reinterpret_cast<const float(*)[8]>(cur + 8 * g);
@@ -211,9 +206,25 @@ __global__ void __launch_bounds__(128) k_gram(Cols X, int m, int nb, int step, i
       tc::commit(&bar[s]);
     }
     issued = it + 1;
-#pragma unroll
-    for (int e = 0; e < KC; ++e)
-      cur[e] = nxt[e];
+    return true;
+  };
+  bool ok = true;
+  {
+    float va[KC], vb[KC];
+    if (nch > 0)
+      load(0, va);
+    for (int it = 0; it < nch; it += 2) {
+      if (!one(it, va, vb)) {
+        ok = false;
+        break;
+      }
+      if (it + 1 >= nch)
+        break;
+      if (!one(it + 1, vb, va)) {
+        ok = false;
+        break;
+      }
+    }
   }
   // every issued chunk complete (commits complete in order; a second bounded wait after a
   // failed one, so that no MMA is in flight when the TMEM is released)
@@ -320,34 +331,35 @@ __global__ void __launch_bounds__(APPLY_THREADS) k_apply(Cols G, int m, Cols W, 
       }
     }
   };
+  auto load_tile = [&](int t, float (&v)[KC]) {
+    const Cols *X;
+    int rows, r0;
+    tile_of(t, X, rows, r0);
+    const int gr = r0 + row;
+    const bool live = gr < rows;
+#pragma unroll
+    for (int e = 0; e < KC; ++e)
+      v[e] = live ? pair_col(*X, I, J, half * KC + e)[gr] : 0.f;
+  };
   int done = 0;  // tiles whose MMAs were committed
-  for (int t = q0, k = 0; t < ntile; t += Q, ++k) {
+  // tile t (the k-th of this CTA) from the registers cur, while the next tile's values load
+  // into nxt; false (for the whole CTA) when a wait gave up
+  auto one = [&](int t, int k, float (&cur)[KC], float (&nxt)[KC]) -> bool {
     // the previous tile's MMAs have read the A buffer
     if (k > 0) {
       const bool w = tc::mbar_wait(&bar[1], (uint32_t)((k - 1) & 1), WAIT_CYCLES);
-      if (!__syncthreads_and(w)) {
-        ok = false;
-        break;
-      }
+      if (!__syncthreads_and(w))
+        return false;
       tc::fence_after();
     }
-    {
-      const Cols *X;
-      int rows, r0;
-      tile_of(t, X, rows, r0);
-      const int gr = r0 + row;
-      const bool live = gr < rows;
-      float v[KC];
+    unsigned char *st = As + half * 3 * PLANE;
 #pragma unroll
-      for (int e = 0; e < KC; ++e)
-        v[e] = live ? pair_col(*X, I, J, half * KC + e)[gr] : 0.f;
-      unsigned char *st = As + half * 3 * PLANE;
-#pragma unroll
-      for (int g = 0; g < KC / 8; ++g) {
-        const float(&v8)[8] = *reinterpret_cast<const float(*)[8]>(v + 8 * g);
-        store_split8(st + tile_off(row, 8 * g), v8);
-      }
+    for (int g = 0; g < KC / 8; ++g) {
+      const float(&v8)[8] = *reinterpret_cast<const float(*)[8]>(cur + 8 * g);
+      store_split8(st + tile_off(row, 8 * g), v8);
     }
+    if (t + Q < ntile)
+      load_tile(t + Q, nxt);  // in flight during this tile's product and the write-back below
     tc::fence_proxy_async();
     tc::fence_before();
     __syncthreads();
@@ -376,16 +388,30 @@ __global__ void __launch_bounds__(APPLY_THREADS) k_apply(Cols G, int m, Cols W, 
       tc::commit(&bar[1]);
     }
     done = k + 1;
-    if (!__syncthreads_or(tid == 0 && !rready)) {
-      // write back the previous tile while this one's product runs
-      if (k > 0) {
-        __syncwarp();
-        epilogue(t - Q, (k - 1) & 1);
-      }
+    if (__syncthreads_or(tid == 0 && !rready))
+      return false;
+    // write back the previous tile while this one's product runs
+    if (k > 0) {
+      __syncwarp();
+      epilogue(t - Q, (k - 1) & 1);
     }
-    else {
-      ok = false;
-      break;
+    return true;
+  };
+  {
+    float va[KC], vb[KC];
+    if (q0 < ntile)
+      load_tile(q0, va);
+    for (int t = q0, k = 0; t < ntile; t += 2 * Q, k += 2) {
+      if (!one(t, k, va, vb)) {
+        ok = false;
+        break;
+      }
+      if (t + Q >= ntile)
+        break;
+      if (!one(t + Q, k + 1, vb, va)) {
+        ok = false;
+        break;
+      }
     }
   }
   // the last tile: its product complete, then written back
@@ -433,7 +459,7 @@ __device__ __forceinline__ void write_rimg(unsigned char *img, F rb)
 // rotation is applied to G and W, so a rotation a few ulps from unitary changes nothing
 // but the accumulated W's orthogonality, which the FP64 Newton-Schulz steps restore.
 struct Rot {
-  float c, sr, si, d1, d2;
+  float c, sr, si, d1, d2, ac, sc;
   int go;
 };
 __device__ __forceinline__ float rsqrt_nr(float x)
@@ -443,7 +469,7 @@ __device__ __forceinline__ float rsqrt_nr(float x)
 }
 __device__ __forceinline__ Rot pair_rot(float ha, float hb, float cr, float ci, float tol)
 {
-  Rot r{1.f, 0.f, 0.f, ha, hb, 0};
+  Rot r{1.f, 0.f, 0.f, ha, hb, 0.f, 0.f, 0};
   const float ar = fabsf(cr), ai = fabsf(ci);
   const float am = fmaxf(ar, ai), an = fminf(ar, ai);
   if (!(am > 0.f))
@@ -453,6 +479,8 @@ __device__ __forceinline__ Rot pair_rot(float ha, float hb, float cr, float ci, 
   const float qn = an / am;
   const float ac = am * (fmaf(qn, qn, 1.f) * rsqrt_nr(fmaf(qn, qn, 1.f)));  // |c|
   const float sc = sqrtf(ha) * sqrtf(hb);
+  r.ac = ac;
+  r.sc = sc;
   if (!(ac >= tol * sc))
     return r;
   const float zeta = (hb - ha) / (2.f * ac);
@@ -464,8 +492,8 @@ __device__ __forceinline__ Rot pair_rot(float ha, float hb, float cr, float ci, 
   r.c = cs;
   r.sr = sn * (cr / ac);
   r.si = sn * (ci / ac);
-  r.d1 = ha - t * ac;
-  r.d2 = hb + t * ac;
+  r.d1 = fmaf(-t, ac, ha);
+  r.d2 = fmaf(t, ac, hb);
   r.go = 1;
   return r;
 }
@@ -478,9 +506,10 @@ __device__ __forceinline__ Rot pair_rot(float ha, float hb, float cr, float ci, 
 // (as float bits).
 // Per Jacobi step: every warp reads the step's pairs (lane u: pair u, and u + 32 for real
 // data) and, after a barrier (no H entry is written before all are read), computes their
-// rotations into its own slice of shared memory; then the threads update the 2x2 blocks
-// (u <= v) of H := J^H H J from a precomputed triangular list and the columns of R := R J;
-// a second barrier ends the step.
+// rotations into its own slice of shared memory (all warps compute the same values); then
+// the threads update the 2x2 blocks of H := J^H H J from a list (the off-diagonal blocks
+// u < v first, then the diagonal ones) and the columns of R := R J (lane v: pair v, each
+// warp a share of the rows); a second barrier ends the step.
 constexpr int EVD_THREADS = 512;
 template <bool CPLX>
 __global__ void __launch_bounds__(EVD_THREADS) k_pair_evd(const float *Spart, int ksplit, int sweeps, float tol,
@@ -490,13 +519,15 @@ __global__ void __launch_bounds__(EVD_THREADS) k_pair_evd(const float *Spart, in
   constexpr int P = N / 2;             // pairs per Jacobi step
   constexpr int PL = P / 32;           // pairs per lane
   constexpr int LD = N + 1;
-  constexpr int NB = P * (P + 1) / 2;  // blocks u <= v
+  constexpr int NO = P * (P - 1) / 2;  // off-diagonal blocks u < v
+  constexpr int NB = NO + P;           // and the diagonal ones
   constexpr int NW = EVD_THREADS / 32;
+  constexpr int SL = 7 * P;            // per-warp slice: c, sr, si, d1, d2, p, q
   extern __shared__ __align__(16) float fsm[];
   float *Hr = fsm, *Hi = Hr + N * LD;
   float *Rr = Hi + (CPLX ? N * LD : 0), *Ri = Rr + N * LD;
-  float *wrot = Ri + (CPLX ? N * LD : 0);  // per warp: 3 P (c, sr, si) + 2 P (d1, d2)
-  unsigned short *tri = reinterpret_cast<unsigned short *>(wrot + NW * 5 * P);  // NB entries: u << 8 | v
+  float *wrot = Ri + (CPLX ? N * LD : 0);
+  unsigned short *tri = reinterpret_cast<unsigned short *>(wrot + NW * SL);  // NB entries: u << 8 | v
   int *rank = reinterpret_cast<int *>(tri + ((NB + 1) & ~1));
   __shared__ unsigned nrot_s, mu_s;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -507,8 +538,10 @@ __global__ void __launch_bounds__(EVD_THREADS) k_pair_evd(const float *Spart, in
   }
   for (int q = tid; q < P * P; q += EVD_THREADS) {
     const int u = q / P, v = q % P;
-    if (u <= v)
-      tri[u * P - u * (u - 1) / 2 + (v - u)] = (unsigned short)((u << 8) | v);
+    if (u < v)
+      tri[u * P - u * (u + 1) / 2 + (v - u - 1)] = (unsigned short)((u << 8) | v);
+    else if (u == v)
+      tri[NO + u] = (unsigned short)((u << 8) | u);
   }
   // S = sum of the partials; H from S (upper triangle, mirrored: exactly Hermitian)
   for (int q = tid; q < N * N; q += EVD_THREADS) {
@@ -544,7 +577,8 @@ __global__ void __launch_bounds__(EVD_THREADS) k_pair_evd(const float *Spart, in
   __syncthreads();
   unsigned nrot = 0u;
   float mu = 0.f;
-  float *wr = wrot + warp * 5 * P;
+  float *wr = wrot + warp * SL;
+  int *wpq = reinterpret_cast<int *>(wr + 5 * P);
   for (int sw = 0; sw < sweeps; ++sw)
     for (int stp = 0; stp < N - 1; ++stp) {
       // the step's pairs and their entries (lane u: pairs u, u + 32)
@@ -581,34 +615,15 @@ __global__ void __launch_bounds__(EVD_THREADS) k_pair_evd(const float *Spart, in
         wr[2 * P + u] = r.si;
         wr[3 * P + u] = r.d1;
         wr[4 * P + u] = r.d2;
-        if (warp == 0) {
-          if (r.go) {
-            ++nrot;
-            const float sc = sqrtf(va[h]) * sqrtf(vb[h]);
-            mu = fmaxf(mu, (sc > 0.f) ? hypotf(vr[h], vi[h]) / sc : 1.f);
-          }
+        wpq[u] = vp[h];
+        wpq[P + u] = vq[h];
+        if (warp == 0 && r.go) {
+          ++nrot;
+          mu = fmaxf(mu, (r.sc > 0.f) ? r.ac / r.sc : 1.f);
         }
       }
       __syncwarp();
-      // the pairs and activity of this step as this warp computed them (all warps compute
-      // the same values): index u of the slice; p, q recomputed from the closed form
-      auto pidx = [&](int u, int &p, int &q) {
-        int a, c;
-        if (u == 0) {
-          a = stp;
-          c = N - 1;
-        }
-        else {
-          a = stp + u;
-          a -= (a >= N - 1) ? (N - 1) : 0;
-          c = stp + (N - 1) - u;
-          c -= (c >= N - 1) ? (N - 1) : 0;
-        }
-        p = a < c ? a : c;
-        q = a < c ? c : a;
-      };
-      // H := J^H H J, 2x2 block (u, v), u <= v, at a time; the (v, u) block is its
-      // conjugate transpose
+      // H := J^H H J, one 2x2 block (u, v) per item, the (v, u) block its conjugate transpose
       for (int q = tid; q < NB; q += EVD_THREADS) {
         const int u = tri[q] >> 8, v = tri[q] & 255;
         const float cu = wr[u], sur = wr[P + u], sui = wr[2 * P + u];
@@ -616,9 +631,7 @@ __global__ void __launch_bounds__(EVD_THREADS) k_pair_evd(const float *Spart, in
         const bool au = (sur != 0.f) || (sui != 0.f) || (cu != 1.f), av = (svr != 0.f) || (svi != 0.f) || (cv != 1.f);
         if (!(au || av))
           continue;
-        int pu, qu, pv, qv;
-        pidx(u, pu, qu);
-        pidx(v, pv, qv);
+        const int pu = wpq[u], qu = wpq[P + u], pv = wpq[v], qv = wpq[P + v];
         if (u == v) {
           Hr[pu * LD + pu] = wr[3 * P + u];
           Hr[qu * LD + qu] = wr[4 * P + u];
@@ -630,7 +643,7 @@ __global__ void __launch_bounds__(EVD_THREADS) k_pair_evd(const float *Spart, in
           }
           continue;
         }
-        float b00r = Hr[pu * LD + pv], b01r = Hr[pu * LD + qv], b10r = Hr[qu * LD + pv], b11r = Hr[qu * LD + qv];
+        const float b00r = Hr[pu * LD + pv], b01r = Hr[pu * LD + qv], b10r = Hr[qu * LD + pv], b11r = Hr[qu * LD + qv];
         float b00i = 0.f, b01i = 0.f, b10i = 0.f, b11i = 0.f;
         if (CPLX) {
           b00i = Hi[pu * LD + pv];
@@ -639,15 +652,23 @@ __global__ void __launch_bounds__(EVD_THREADS) k_pair_evd(const float *Spart, in
           b11i = Hi[qu * LD + qv];
         }
         // C = B J_v: C[:,0] = cv B[:,0] - conj(s_v) B[:,1], C[:,1] = cv B[:,1] + s_v B[:,0]
-        const float c00r = cv * b00r - (svr * b01r + svi * b01i), c00i = cv * b00i - (svr * b01i - svi * b01r);
-        const float c10r = cv * b10r - (svr * b11r + svi * b11i), c10i = cv * b10i - (svr * b11i - svi * b11r);
-        const float c01r = cv * b01r + (svr * b00r - svi * b00i), c01i = cv * b01i + (svr * b00i + svi * b00r);
-        const float c11r = cv * b11r + (svr * b10r - svi * b10i), c11i = cv * b11i + (svr * b10i + svi * b10r);
+        const float c00r = fmaf(cv, b00r, -fmaf(svr, b01r, svi * b01i));
+        const float c00i = fmaf(cv, b00i, -fmaf(svr, b01i, -(svi * b01r)));
+        const float c10r = fmaf(cv, b10r, -fmaf(svr, b11r, svi * b11i));
+        const float c10i = fmaf(cv, b10i, -fmaf(svr, b11i, -(svi * b11r)));
+        const float c01r = fmaf(cv, b01r, fmaf(svr, b00r, -(svi * b00i)));
+        const float c01i = fmaf(cv, b01i, fmaf(svr, b00i, svi * b00r));
+        const float c11r = fmaf(cv, b11r, fmaf(svr, b10r, -(svi * b10i)));
+        const float c11i = fmaf(cv, b11i, fmaf(svr, b10i, svi * b10r));
         // B' = J_u^H C: row 0 = cu C[0,:] - s_u C[1,:], row 1 = cu C[1,:] + conj(s_u) C[0,:]
-        const float n00r = cu * c00r - (sur * c10r - sui * c10i), n00i = cu * c00i - (sur * c10i + sui * c10r);
-        const float n01r = cu * c01r - (sur * c11r - sui * c11i), n01i = cu * c01i - (sur * c11i + sui * c11r);
-        const float n10r = cu * c10r + (sur * c00r + sui * c00i), n10i = cu * c10i + (sur * c00i - sui * c00r);
-        const float n11r = cu * c11r + (sur * c01r + sui * c01i), n11i = cu * c11i + (sur * c01i - sui * c01r);
+        const float n00r = fmaf(cu, c00r, -fmaf(sur, c10r, -(sui * c10i)));
+        const float n00i = fmaf(cu, c00i, -fmaf(sur, c10i, sui * c10r));
+        const float n01r = fmaf(cu, c01r, -fmaf(sur, c11r, -(sui * c11i)));
+        const float n01i = fmaf(cu, c01i, -fmaf(sur, c11i, sui * c11r));
+        const float n10r = fmaf(cu, c10r, fmaf(sur, c00r, sui * c00i));
+        const float n10i = fmaf(cu, c10i, fmaf(sur, c00i, -(sui * c00r)));
+        const float n11r = fmaf(cu, c11r, fmaf(sur, c01r, sui * c01i));
+        const float n11i = fmaf(cu, c11i, fmaf(sur, c01i, -(sui * c01r)));
         Hr[pu * LD + pv] = n00r;
         Hr[pu * LD + qv] = n01r;
         Hr[qu * LD + pv] = n10r;
@@ -667,21 +688,27 @@ __global__ void __launch_bounds__(EVD_THREADS) k_pair_evd(const float *Spart, in
           Hi[qv * LD + qu] = -n11i;
         }
       }
-      // R := R J: columns (p_v, q_v) of every row
-      for (int q = tid; q < N * P; q += EVD_THREADS) {
-        const int r = q / P, v = q % P;
+      // R := R J: lane v takes pair v (and v + 32), warp w the rows w, w + NW, ...
+#pragma unroll
+      for (int h = 0; h < PL; ++h) {
+        const int v = lane + 32 * h;
         const float cv = wr[v], svr = wr[P + v], svi = wr[2 * P + v];
         if (svr == 0.f && svi == 0.f && cv == 1.f)
           continue;
-        int pv, qv;
-        pidx(v, pv, qv);
-        const float xr = Rr[r * LD + pv], yr = Rr[r * LD + qv];
-        const float xi = CPLX ? Ri[r * LD + pv] : 0.f, yi = CPLX ? Ri[r * LD + qv] : 0.f;
-        Rr[r * LD + pv] = cv * xr - (svr * yr + svi * yi);
-        Rr[r * LD + qv] = cv * yr + (svr * xr - svi * xi);
-        if (CPLX) {
-          Ri[r * LD + pv] = cv * xi - (svr * yi - svi * yr);
-          Ri[r * LD + qv] = cv * yi + (svr * xi + svi * xr);
+        const int pv = wpq[v], qv = wpq[P + v];
+        for (int r = warp; r < N; r += NW) {
+          const float xr = Rr[r * LD + pv], yr = Rr[r * LD + qv];
+          if (CPLX) {
+            const float xi = Ri[r * LD + pv], yi = Ri[r * LD + qv];
+            Rr[r * LD + pv] = fmaf(cv, xr, -fmaf(svr, yr, svi * yi));
+            Rr[r * LD + qv] = fmaf(cv, yr, fmaf(svr, xr, -(svi * xi)));
+            Ri[r * LD + pv] = fmaf(cv, xi, -fmaf(svr, yi, -(svi * yr)));
+            Ri[r * LD + qv] = fmaf(cv, yi, fmaf(svr, xi, svi * xr));
+          }
+          else {
+            Rr[r * LD + pv] = fmaf(cv, xr, -(svr * yr));
+            Rr[r * LD + qv] = fmaf(cv, yr, svr * xr);
+          }
         }
       }
       __syncthreads();
@@ -737,7 +764,7 @@ __global__ void __launch_bounds__(256) k_rimg(const float *R, unsigned char *Rim
 static size_t evd_smem(bool cplx)
 {
   const int N = cplx ? 64 : 128, P = N / 2, LD = N + 1, NB = P * (P + 1) / 2;
-  return (size_t)(cplx ? 4 : 2) * N * LD * 4 + (size_t)(EVD_THREADS / 32) * 5 * P * 4 + (size_t)((NB + 1) & ~1) * 2 +
+  return (size_t)(cplx ? 4 : 2) * N * LD * 4 + (size_t)(EVD_THREADS / 32) * 7 * P * 4 + (size_t)((NB + 1) & ~1) * 2 +
          (size_t)N * 4;
 }
 

@@ -7,9 +7,9 @@
 //   2. runs FP32 one-sided Jacobi sweeps on it (k_presweep_reg / k_presweep, Hestenes
 //      rotations from plain FP32 dot products) from W := I until no pair exceeds the FP32
 //      tolerance;
-//   3. widens W to FP64 and makes it orthonormal to FP64 accuracy with two Newton-Schulz
-//      polar steps, W <- W (3I - W^H W) / 2 (W is orthonormal to ~1e-5, and each step
-//      squares the error);
+//   3. widens W to FP64 and makes it orthonormal to FP64 accuracy with Newton-Schulz polar
+//      steps, W <- W (3I - W^H W) / 2 (each step maps an error e of W^H W - I to about
+//      3e^2/4; the number of steps, 2 to 5, follows from the error measured first);
 //   4. forms G_s = G_{s-1} W and V_s = V_{s-1} W (FP64 GEMMs).
 // FP32 rounding is relative to each element, so from the second stage on the FP32 sweeps
 // see the columns of G_{s-1} to their own relative accuracy and resolve the directions of
@@ -444,6 +444,25 @@ static bool zgemm(cublasHandle_t h, bool cplx, bool conjA, int m, int n, int k, 
   return ok;
 }
 
+// max |Y(r, c) - I(r, c)| of one plane of an n x n matrix (diag: the real plane, which holds
+// the identity's ones) into *out, as the bits of a non-negative double
+__global__ void k_dev_identity(const double *Y, long long n, int diag, unsigned long long *out)
+{
+  unsigned long long mx = 0ull;
+  for (long long c = blockIdx.y; c < n; c += gridDim.y)
+    for (long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (long long)gridDim.x * blockDim.x) {
+      const double d = fabs(Y[c * n + r] - ((diag && r == c) ? 1.0 : 0.0));
+      const unsigned long long b = (d == d) ? (unsigned long long)__double_as_longlong(d) : 0x7ff0000000000000ull;
+      mx = (b > mx) ? b : mx;
+    }
+  for (int o = 16; o >= 1; o >>= 1) {
+    const unsigned long long w = __shfl_xor_sync(0xffffffffu, mx, o);
+    mx = (w > mx) ? w : mx;
+  }
+  if ((threadIdx.x & 31) == 0 && mx)
+    atomicMax(out, mx);
+}
+
 // T(r, c) = T(c, r) for r < c (fill the upper triangle of an n x n matrix from the lower)
 __global__ void k_sym_lower(double *Tm, int n)
 {
@@ -665,8 +684,30 @@ static vj_fint mixed_dev(vj_fnat m_, vj_fnat n_, double *G, vj_fnat ldG, double 
           W32 + pl * nn, (long long)nn, X + pl * nn);
     // (the Gram product by symmetric rank-k updates, the products of near-unitary
     // matrices by 3M; the Gp scratch, free until step 4, holds their temporaries)
-    for (int it = 0; it < 2; ++it) {
-      if (!gram(h, CPLX, ni, Xp, Yp, Gp, s) || !zgemm3m(h, CPLX, ni, ni, ni, Xp, Yp, Tp, Gp, s))
+    // (as many steps as W's distance from unitarity needs: each step maps an error e of
+    // W^H W - I to about 3e^2/4, and the FP32 stage leaves e between 1e-6 and 1e-3)
+    int nsteps = 2;
+    for (int it = 0; it < nsteps; ++it) {
+      if (!gram(h, CPLX, ni, Xp, Yp, Gp, s))
+        return VJ_ERR_CUDA;
+      if (it == 0) {
+        if (cudaMemsetAsync(cell, 0, 8, s) != cudaSuccess)
+          return VJ_ERR_CUDA;
+        for (int pl = 0; pl < P; ++pl)
+          k_dev_identity<<<grid2(n, n), 256, 0, s>>>(Y + pl * nn, n, pl == 0, cell);
+        unsigned long long eb = 0;
+        if (cudaMemcpyAsync(&eb, cell, 8, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+            cudaStreamSynchronize(s) != cudaSuccess)
+          return VJ_ERR_CUDA;
+        double e0;
+        memcpy(&e0, &eb, 8);
+        nsteps = 1;
+        for (double e = e0; e > 1e-17 && nsteps < 5; e = 0.75 * e * e + 1e-17)
+          ++nsteps;
+        if (!(e0 < 0.5))
+          nsteps = 5;
+      }
+      if (!zgemm3m(h, CPLX, ni, ni, ni, Xp, Yp, Tp, Gp, s))
         return VJ_ERR_CUDA;
       const double a15 = 1.5, am05 = -0.5;
       for (int pl = 0; pl < P; ++pl)
