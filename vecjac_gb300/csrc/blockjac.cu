@@ -280,6 +280,7 @@ __global__ void __launch_bounds__(APPLY_THREADS) k_apply(Cols G, int m, Cols W, 
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char *smem = smem_raw + ((1024u - (tc::saddr(smem_raw) & 1023u)) & 1023u);
   unsigned char *Rs = smem, *As = smem + 6 * PLANE;  // R: [stage][term]; A: [stage][term]
+  float **colG = reinterpret_cast<float **>(smem + 12 * PLANE), **colW = colG + TILE;  // the pair's columns
   __shared__ unsigned long long bar[2];  // 0: TMA of R, 1: MMA completion (one phase per tile)
   __shared__ uint32_t tslot;
   const int tid = threadIdx.x, warp = tid >> 5;
@@ -307,16 +308,21 @@ __global__ void __launch_bounds__(APPLY_THREADS) k_apply(Cols G, int m, Cols W, 
   }
   const int row = tid & (TILE - 1), half = tid >> 7;
   bool ok = true, rready = false;
-  auto tile_of = [&](int t, const Cols *&X, int &rows, int &r0) {
+  if (tid < TILE)
+    colG[tid] = pair_col(G, I, J, tid);
+  else
+    colW[tid - TILE] = pair_col(W, I, J, tid - TILE);
+  __syncthreads();
+  auto tile_of = [&](int t, float **&X, int &rows, int &r0) {
     const bool onG = t < tg;
-    X = onG ? &G : &W;
+    X = onG ? colG : colW;
     rows = onG ? m : n;
     r0 = (onG ? t : t - tg) * TILE;
   };
   // write back tile t from TMEM buffer b: warp w reads lanes 32 (w % 4) .. + 31 (rows),
   // columns 64 (w / 4) .. + 63
   auto epilogue = [&](int t, int b) {
-    const Cols *X;
+    float **X;
     int rows, r0;
     tile_of(t, X, rows, r0);
     const int r = r0 + 32 * (warp & 3) + (tid & 31);
@@ -327,19 +333,19 @@ __global__ void __launch_bounds__(APPLY_THREADS) k_apply(Cols G, int m, Cols W, 
       if (r < rows) {
 #pragma unroll
         for (int e = 0; e < 32; ++e)
-          pair_col(*X, I, J, c + e)[r] = __uint_as_float(v[e]);
+          X[c + e][r] = __uint_as_float(v[e]);
       }
     }
   };
   auto load_tile = [&](int t, float (&v)[KC]) {
-    const Cols *X;
+    float **X;
     int rows, r0;
     tile_of(t, X, rows, r0);
     const int gr = r0 + row;
     const bool live = gr < rows;
 #pragma unroll
     for (int e = 0; e < KC; ++e)
-      v[e] = live ? pair_col(*X, I, J, half * KC + e)[gr] : 0.f;
+      v[e] = live ? X[half * KC + e][gr] : 0.f;
   };
   int done = 0;  // tiles whose MMAs were committed
   // tile t (the k-th of this CTA) from the registers cur, while the next tile's values load
@@ -498,19 +504,18 @@ __device__ __forceinline__ Rot pair_rot(float ha, float hb, float cr, float ci, 
   return r;
 }
 
-// One CTA (512 threads) per block pair: sums the split Gram partials, forms H (complex
+// One CTA (256 threads) per block pair: sums the split Gram partials, forms H (complex
 // 64 x 64 from the real Gram of [Re | Im], or real 128 x 128), runs `sweeps` cyclic
 // Jacobi sweeps on H with the rotation accumulated in R (R := I first), orders R's columns
 // by descending diagonal of the final H, and writes R's split image for k_apply.
 // stats[0] += rotations, stats[1] = max over rotated pairs of |h_pq| / sqrt(h_pp h_qq)
 // (as float bits).
-// Per Jacobi step: every warp reads the step's pairs (lane u: pair u, and u + 32 for real
-// data) and, after a barrier (no H entry is written before all are read), computes their
-// rotations into its own slice of shared memory (all warps compute the same values); then
-// the threads update the 2x2 blocks of H := J^H H J from a list (the off-diagonal blocks
-// u < v first, then the diagonal ones) and the columns of R := R J (lane v: pair v, each
-// warp a share of the rows); a second barrier ends the step.
-constexpr int EVD_THREADS = 512;
+// Per Jacobi step: warp 0 (lane u: pair u, and u + 32 for real data) reads the step's
+// pairs from H and writes their rotations to shared memory; after a barrier every thread
+// updates 2x2 blocks of H := J^H H J from a list (the off-diagonal blocks u < v first, then
+// the diagonal ones) and columns of R := R J (lane v: pair v, each warp a share of the
+// rows); a second barrier ends the step.
+constexpr int EVD_THREADS = 256;
 template <bool CPLX>
 __global__ void __launch_bounds__(EVD_THREADS) k_pair_evd(const float *Spart, int ksplit, int sweeps, float tol,
                                                           unsigned char *Rimg, unsigned *stats)
@@ -522,12 +527,12 @@ __global__ void __launch_bounds__(EVD_THREADS) k_pair_evd(const float *Spart, in
   constexpr int NO = P * (P - 1) / 2;  // off-diagonal blocks u < v
   constexpr int NB = NO + P;           // and the diagonal ones
   constexpr int NW = EVD_THREADS / 32;
-  constexpr int SL = 7 * P;            // per-warp slice: c, sr, si, d1, d2, p, q
   extern __shared__ __align__(16) float fsm[];
   float *Hr = fsm, *Hi = Hr + N * LD;
   float *Rr = Hi + (CPLX ? N * LD : 0), *Ri = Rr + N * LD;
-  float *wrot = Ri + (CPLX ? N * LD : 0);
-  unsigned short *tri = reinterpret_cast<unsigned short *>(wrot + NW * SL);  // NB entries: u << 8 | v
+  float *rc = Ri + (CPLX ? N * LD : 0), *rsr = rc + P, *rsi = rsr + P, *rd1 = rsi + P, *rd2 = rd1 + P;
+  int *rp = reinterpret_cast<int *>(rd2 + P), *rq = rp + P, *ract = rq + P;
+  unsigned short *tri = reinterpret_cast<unsigned short *>(ract + P);  // NB entries: u << 8 | v
   int *rank = reinterpret_cast<int *>(tri + ((NB + 1) & ~1));
   __shared__ unsigned nrot_s, mu_s;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -577,64 +582,55 @@ __global__ void __launch_bounds__(EVD_THREADS) k_pair_evd(const float *Spart, in
   __syncthreads();
   unsigned nrot = 0u;
   float mu = 0.f;
-  float *wr = wrot + warp * SL;
-  int *wpq = reinterpret_cast<int *>(wr + 5 * P);
   for (int sw = 0; sw < sweeps; ++sw)
     for (int stp = 0; stp < N - 1; ++stp) {
-      // the step's pairs and their entries (lane u: pairs u, u + 32)
-      float va[PL], vb[PL], vr[PL], vi[PL];
-      int vp[PL], vq[PL];
+      // the step's pairs and their rotations (warp 0; lane u: pairs u, u + 32)
+      if (warp == 0) {
 #pragma unroll
-      for (int h = 0; h < PL; ++h) {
-        const int u = lane + 32 * h;
-        int a, c;
-        if (u == 0) {
-          a = stp;
-          c = N - 1;
+        for (int h = 0; h < PL; ++h) {
+          const int u = lane + 32 * h;
+          int a, c;
+          if (u == 0) {
+            a = stp;
+            c = N - 1;
+          }
+          else {
+            a = stp + u;
+            a -= (a >= N - 1) ? (N - 1) : 0;
+            c = stp + (N - 1) - u;
+            c -= (c >= N - 1) ? (N - 1) : 0;
+          }
+          // (the circle order's own orientation: the first indices of a step are consecutive
+          // modulo N - 1, and so are the second ones, so that the row and column accesses of
+          // the updates fall into distinct shared-memory banks)
+          const int p = a, q = c;
+          const Rot r = pair_rot(fmaxf(Hr[p * LD + p], 0.f), fmaxf(Hr[q * LD + q], 0.f), Hr[p * LD + q],
+                                 CPLX ? Hi[p * LD + q] : 0.f, tol);
+          rc[u] = r.c;
+          rsr[u] = r.sr;
+          rsi[u] = r.si;
+          rd1[u] = r.d1;
+          rd2[u] = r.d2;
+          rp[u] = p;
+          rq[u] = q;
+          ract[u] = r.go && ((r.sr != 0.f) || (r.si != 0.f));
+          if (r.go) {
+            ++nrot;
+            mu = fmaxf(mu, (r.sc > 0.f) ? r.ac / r.sc : 1.f);
+          }
         }
-        else {
-          a = stp + u;
-          a -= (a >= N - 1) ? (N - 1) : 0;
-          c = stp + (N - 1) - u;
-          c -= (c >= N - 1) ? (N - 1) : 0;
-        }
-        vp[h] = a < c ? a : c;
-        vq[h] = a < c ? c : a;
-        va[h] = fmaxf(Hr[vp[h] * LD + vp[h]], 0.f);
-        vb[h] = fmaxf(Hr[vq[h] * LD + vq[h]], 0.f);
-        vr[h] = Hr[vp[h] * LD + vq[h]];
-        vi[h] = CPLX ? Hi[vp[h] * LD + vq[h]] : 0.f;
       }
       __syncthreads();
-#pragma unroll
-      for (int h = 0; h < PL; ++h) {
-        const int u = lane + 32 * h;
-        const Rot r = pair_rot(va[h], vb[h], vr[h], vi[h], tol);
-        wr[u] = r.c;
-        wr[P + u] = r.sr;
-        wr[2 * P + u] = r.si;
-        wr[3 * P + u] = r.d1;
-        wr[4 * P + u] = r.d2;
-        wpq[u] = vp[h];
-        wpq[P + u] = vq[h];
-        if (warp == 0 && r.go) {
-          ++nrot;
-          mu = fmaxf(mu, (r.sc > 0.f) ? r.ac / r.sc : 1.f);
-        }
-      }
-      __syncwarp();
       // H := J^H H J, one 2x2 block (u, v) per item, the (v, u) block its conjugate transpose
       for (int q = tid; q < NB; q += EVD_THREADS) {
         const int u = tri[q] >> 8, v = tri[q] & 255;
-        const float cu = wr[u], sur = wr[P + u], sui = wr[2 * P + u];
-        const float cv = wr[v], svr = wr[P + v], svi = wr[2 * P + v];
-        const bool au = (sur != 0.f) || (sui != 0.f) || (cu != 1.f), av = (svr != 0.f) || (svi != 0.f) || (cv != 1.f);
-        if (!(au || av))
+        const int au = ract[u], av = ract[v];
+        if (!(au | av))
           continue;
-        const int pu = wpq[u], qu = wpq[P + u], pv = wpq[v], qv = wpq[P + v];
+        const int pu = rp[u], qu = rq[u];
         if (u == v) {
-          Hr[pu * LD + pu] = wr[3 * P + u];
-          Hr[qu * LD + qu] = wr[4 * P + u];
+          Hr[pu * LD + pu] = rd1[u];
+          Hr[qu * LD + qu] = rd2[u];
           Hr[pu * LD + qu] = 0.f;
           Hr[qu * LD + pu] = 0.f;
           if (CPLX) {
@@ -643,6 +639,9 @@ __global__ void __launch_bounds__(EVD_THREADS) k_pair_evd(const float *Spart, in
           }
           continue;
         }
+        const int pv = rp[v], qv = rq[v];
+        const float cu = rc[u], sur = rsr[u], sui = rsi[u];
+        const float cv = rc[v], svr = rsr[v], svi = rsi[v];
         const float b00r = Hr[pu * LD + pv], b01r = Hr[pu * LD + qv], b10r = Hr[qu * LD + pv], b11r = Hr[qu * LD + qv];
         float b00i = 0.f, b01i = 0.f, b10i = 0.f, b11i = 0.f;
         if (CPLX) {
@@ -692,10 +691,11 @@ __global__ void __launch_bounds__(EVD_THREADS) k_pair_evd(const float *Spart, in
 #pragma unroll
       for (int h = 0; h < PL; ++h) {
         const int v = lane + 32 * h;
-        const float cv = wr[v], svr = wr[P + v], svi = wr[2 * P + v];
-        if (svr == 0.f && svi == 0.f && cv == 1.f)
+        if (!ract[v])
           continue;
-        const int pv = wpq[v], qv = wpq[P + v];
+        const int pv = rp[v], qv = rq[v];
+        const float cv = rc[v], svr = rsr[v], svi = rsi[v];
+#pragma unroll 4
         for (int r = warp; r < N; r += NW) {
           const float xr = Rr[r * LD + pv], yr = Rr[r * LD + qv];
           if (CPLX) {
@@ -764,12 +764,11 @@ __global__ void __launch_bounds__(256) k_rimg(const float *R, unsigned char *Rim
 static size_t evd_smem(bool cplx)
 {
   const int N = cplx ? 64 : 128, P = N / 2, LD = N + 1, NB = P * (P + 1) / 2;
-  return (size_t)(cplx ? 4 : 2) * N * LD * 4 + (size_t)(EVD_THREADS / 32) * 7 * P * 4 + (size_t)((NB + 1) & ~1) * 2 +
-         (size_t)N * 4;
+  return (size_t)(cplx ? 4 : 2) * N * LD * 4 + (size_t)8 * P * 4 + (size_t)((NB + 1) & ~1) * 2 + (size_t)N * 4;
 }
 
 constexpr size_t GRAM_SMEM = 2 * 3 * PLANE + 1024;
-constexpr size_t APPLY_SMEM = 2 * 6 * PLANE + 1024;  // R image + one A tile (both K stages)
+constexpr size_t APPLY_SMEM = 2 * 6 * PLANE + 2 * TILE * sizeof(float *) + 1024;  // R image, one A tile, columns
 
 // ---------------------------------------------------------------- host side
 struct Plan {
@@ -810,10 +809,10 @@ static Plan plan(bool cplx, long long m, long long n)
   p.b = cplx ? 32 : 64;
   p.nb = (int)(n / p.b);
   p.npairs = p.nb / 2;
-  // split K so that the Gram grid covers the GPU about once
+  // split K so that the Gram grid covers every SM with its two resident CTAs
   const int sms = host::sm_count();
   const int nch = (int)((m + KC - 1) / KC);
-  int ks = (sms + p.npairs - 1) / p.npairs;
+  int ks = (2 * sms) / p.npairs;
   if (ks > nch)
     ks = nch;
   if (ks < 1)
