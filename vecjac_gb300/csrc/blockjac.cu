@@ -7,7 +7,8 @@
 // Im G_J]). A block sweep visits every pair of blocks once in the round-robin order, n/b/2
 // independent pairs per block step, and for each pair
 //   1. k_gram:  S = X^T X, the real Gram matrix of the pair's 128 real columns X (128 x 128,
-//      K = m, split over several CTAs), on the tensor cores;
+//      K = m, split over several CTAs), on the tensor cores (its symmetry halves the cross
+//      terms of the split products);
 //   2. k_pair_evd: the Hermitian Gram matrix H = [G_I G_J]^H [G_I G_J] (from S), one cyclic
 //      two-sided Jacobi sweep on H that accumulates the unitary R (2b x 2b) -- in exact
 //      arithmetic the rotations of one-sided Jacobi on the pair's columns, from the same
@@ -148,7 +149,7 @@ __global__ void __launch_bounds__(128) k_gram(Cols X, int m, int nb, int step, i
   }
   __syncwarp();
   if (warp == 0)
-    tc::tmem_alloc(&tslot, TILE);
+    tc::tmem_alloc(&tslot, 2 * TILE);
   tc::fence_before();
   __syncthreads();
   tc::fence_after();
@@ -195,14 +196,24 @@ __global__ void __launch_bounds__(128) k_gram(Cols X, int m, int nb, int step, i
     if (tid == 0) {
       tc::fence_after();
       const uint32_t a0 = tc::saddr(st);
+      // X^T X is symmetric and D_ts = D_st^T for D_st = X_s^T X_t: F = D_hh + D_mm and
+      // E = D_hm + D_hl (six-term split) or F = D_hh, E = D_hm (three-term), so that
+      // S = F + E + E^T with four (two) products instead of six (three)
 #pragma unroll
-      for (int kk = 0; kk < KC / 16; ++kk)
-#pragma unroll
-        for (int t = 6 - NT; t < 6; ++t) {
-          const uint64_t ad = tc::sdesc(a0 + TA[t] * PLANE + kk * 2 * LBO, LBO, SBO);
-          const uint64_t bd = tc::sdesc(a0 + TB[t] * PLANE + kk * 2 * LBO, LBO, SBO);
-          tc::mma_bf16(tmem, ad, bd, IDESC, (it > 0 || kk > 0 || t > 6 - NT) ? 1u : 0u);
+      for (int kk = 0; kk < KC / 16; ++kk) {
+        auto d = [&](int term) { return tc::sdesc(a0 + term * PLANE + kk * 2 * LBO, LBO, SBO); };
+        const uint32_t first = (it > 0 || kk > 0) ? 1u : 0u;
+        if (NT == 6) {
+          tc::mma_bf16(tmem, d(1), d(1), IDESC, first);
+          tc::mma_bf16(tmem, d(0), d(0), IDESC, 1u);
+          tc::mma_bf16(tmem + TILE, d(0), d(2), IDESC, first);
+          tc::mma_bf16(tmem + TILE, d(0), d(1), IDESC, 1u);
         }
+        else {
+          tc::mma_bf16(tmem, d(0), d(0), IDESC, first);
+          tc::mma_bf16(tmem + TILE, d(0), d(1), IDESC, first);
+        }
+      }
       tc::commit(&bar[s]);
     }
     issued = it + 1;
@@ -238,20 +249,24 @@ __global__ void __launch_bounds__(128) k_gram(Cols X, int m, int nb, int step, i
   }
   tc::fence_after();
   __syncwarp();
-  float4 *out = reinterpret_cast<float4 *>(Spart + (size_t)blockIdx.x * TILE * TILE + (size_t)tid * TILE);
-  if (nch == 0) {
-    for (int c = 0; c < TILE / 4; ++c)
-      out[c] = make_float4(0.f, 0.f, 0.f, 0.f);
-  }
-  else {
+  // F then E, row tid of each (TMEM lane tid)
+  for (int mat = 0; mat < 2; ++mat) {
+    float4 *out = reinterpret_cast<float4 *>(Spart + ((size_t)blockIdx.x * 2 + mat) * TILE * TILE +
+                                             (size_t)tid * TILE);
+    if (nch == 0) {
+      for (int c = 0; c < TILE / 4; ++c)
+        out[c] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    else {
 #pragma unroll 1
-    for (int c = 0; c < TILE; c += 32) {
-      uint32_t r[32];
-      tc::tmem_ld32(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)c, r);
+      for (int c = 0; c < TILE; c += 32) {
+        uint32_t r[32];
+        tc::tmem_ld32(tmem + (uint32_t)(mat * TILE) + ((uint32_t)(warp * 32) << 16) + (uint32_t)c, r);
 #pragma unroll
-      for (int e = 0; e < 8; ++e)
-        out[c / 4 + e] = make_float4(__uint_as_float(r[4 * e]), __uint_as_float(r[4 * e + 1]),
-                                     __uint_as_float(r[4 * e + 2]), __uint_as_float(r[4 * e + 3]));
+        for (int e = 0; e < 8; ++e)
+          out[c / 4 + e] = make_float4(__uint_as_float(r[4 * e]), __uint_as_float(r[4 * e + 1]),
+                                       __uint_as_float(r[4 * e + 2]), __uint_as_float(r[4 * e + 3]));
+      }
     }
   }
   if (!ok)
@@ -261,7 +276,7 @@ __global__ void __launch_bounds__(128) k_gram(Cols X, int m, int nb, int step, i
   tc::fence_after();
   __syncwarp();
   if (warp == 0)
-    tc::tmem_dealloc(tmem, TILE);
+    tc::tmem_dealloc(tmem, 2 * TILE);
 }
 
 // ---------------------------------------------------------------- block rotations
@@ -457,6 +472,36 @@ __device__ __forceinline__ void write_rimg(unsigned char *img, F rb)
   }
 }
 
+// ---------------------------------------------------------------- Gram reduction
+// S = sum over the K splits of F + E + E^T, tile by tile: CTA (pair, 32 x 32 tile (ti, tj))
+// reads the tile (ti, tj) of every split's F and E and the tile (tj, ti) of its E through
+// shared memory (coalesced rows; the transpose in shared memory), and writes S's tile.
+__global__ void __launch_bounds__(256) k_gram_reduce(const float *Spart, int ksplit, float *S)
+{
+  __shared__ float et[32][33];
+  const int pair = blockIdx.x >> 4, tile = blockIdx.x & 15, ti = tile >> 2, tj = tile & 3;
+  const int x = threadIdx.x & 31, y0 = threadIdx.x >> 5;  // 8 rows of the tile per pass
+  float acc[4] = {0.f, 0.f, 0.f, 0.f};
+  for (int k = 0; k < ksplit; ++k) {
+    const float *F = Spart + ((size_t)pair * ksplit + k) * 2 * TILE * TILE, *E = F + TILE * TILE;
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      const int y = y0 + 8 * r;
+      et[y][x] = E[(tj * 32 + y) * TILE + ti * 32 + x];  // row tj*32+y of E, columns of tile ti
+    }
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      const int y = y0 + 8 * r, i = ti * 32 + y, j = tj * 32 + x;
+      acc[r] += F[i * TILE + j] + (E[i * TILE + j] + et[x][y]);
+    }
+  }
+#pragma unroll
+  for (int r = 0; r < 4; ++r)
+    S[(size_t)pair * TILE * TILE + (ti * 32 + y0 + 8 * r) * TILE + tj * 32 + x] = acc[r];
+}
+
 // ---------------------------------------------------------------- pair eigenproblems
 // Rotation of one pair (p, q) of the Hermitian H from h_pp = a, h_qq = b, h_pq = c (the
 // scalar sweep's formulas: zeta = (b - a) / (2|c|), t the smaller root of t^2 + 2 zeta t = 1,
@@ -504,7 +549,7 @@ __device__ __forceinline__ Rot pair_rot(float ha, float hb, float cr, float ci, 
   return r;
 }
 
-// One CTA (256 threads) per block pair: sums the split Gram partials, forms H (complex
+// One CTA (256 threads) per block pair: from the pair's Gram matrix S forms H (complex
 // 64 x 64 from the real Gram of [Re | Im], or real 128 x 128), runs `sweeps` cyclic
 // Jacobi sweeps on H with the rotation accumulated in R (R := I first), orders R's columns
 // by descending diagonal of the final H, and writes R's split image for k_apply.
@@ -517,7 +562,7 @@ __device__ __forceinline__ Rot pair_rot(float ha, float hb, float cr, float ci, 
 // rows); a second barrier ends the step.
 constexpr int EVD_THREADS = 256;
 template <bool CPLX>
-__global__ void __launch_bounds__(EVD_THREADS) k_pair_evd(const float *Spart, int ksplit, int sweeps, float tol,
+__global__ void __launch_bounds__(EVD_THREADS) k_pair_evd(const float *Sred, int sweeps, float tol,
                                                           unsigned char *Rimg, unsigned *stats)
 {
   constexpr int N = CPLX ? 64 : 128;  // order of H
@@ -536,7 +581,7 @@ __global__ void __launch_bounds__(EVD_THREADS) k_pair_evd(const float *Spart, in
   int *rank = reinterpret_cast<int *>(tri + ((NB + 1) & ~1));
   __shared__ unsigned nrot_s, mu_s;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const float *S0 = Spart + (size_t)blockIdx.x * ksplit * TILE * TILE;
+  const float *S0 = Sred + (size_t)blockIdx.x * TILE * TILE;
   if (tid == 0) {
     nrot_s = 0u;
     mu_s = 0u;
@@ -553,12 +598,7 @@ __global__ void __launch_bounds__(EVD_THREADS) k_pair_evd(const float *Spart, in
     const int i = q / N, j = q % N;
     if (i > j)
       continue;
-    auto S = [&](int a, int b) {
-      float x = 0.f;
-      for (int k = 0; k < ksplit; ++k)
-        x += S0[(size_t)k * TILE * TILE + (size_t)a * TILE + b];
-      return x;
-    };
+    auto S = [&](int a, int b) { return S0[a * TILE + b]; };
     if (CPLX) {
       const float hr = S(i, j) + S(64 + i, 64 + j);
       const float hi = (i == j) ? 0.f : (S(i, 64 + j) - S(64 + i, j));
@@ -842,7 +882,7 @@ bool block_sweeps_apply(bool cplx, long long m, long long n, long long ld)
 size_t block_sweep_scratch(bool cplx, long long m, long long n)
 {
   const bj::Plan p = bj::plan(cplx, m, n);
-  return (size_t)p.npairs * p.ksplit * bj::TILE * bj::TILE * 4 + (size_t)p.npairs * 6 * bj::PLANE + 256;
+  return (size_t)p.npairs * (p.ksplit * 2 + 1) * bj::TILE * bj::TILE * 4 + (size_t)p.npairs * 6 * bj::PLANE + 256;
 }
 
 // One block sweep (nb - 1 block steps) on planar FP32 G (m x n) and W (n x n), both with
@@ -859,7 +899,8 @@ long long block_sweep(bool cplx, int m, int n, float *Gr, float *Gi, long long l
     return -1;
   const Plan p = plan(cplx, m, n);
   float *Spart = reinterpret_cast<float *>(scratch);
-  unsigned char *Rimg = scratch + (size_t)p.npairs * p.ksplit * TILE * TILE * 4;
+  float *Sred = Spart + (size_t)p.npairs * p.ksplit * 2 * TILE * TILE;
+  unsigned char *Rimg = scratch + (size_t)p.npairs * (p.ksplit * 2 + 1) * TILE * TILE * 4;
   const Cols G{Gr, cplx ? Gi : nullptr, ldg, p.b}, W{Wr, cplx ? Wi : nullptr, ldw, p.b};
   if (cudaMemsetAsync(stats, 0, 16, s) != cudaSuccess)
     return -1;
@@ -868,10 +909,11 @@ long long block_sweep(bool cplx, int m, int n, float *Gr, float *Gi, long long l
       k_gram<3><<<p.npairs * p.ksplit, 128, GRAM_SMEM, s>>>(G, m, p.nb, step, p.ksplit, Spart, stats + 2);
     else
       k_gram<6><<<p.npairs * p.ksplit, 128, GRAM_SMEM, s>>>(G, m, p.nb, step, p.ksplit, Spart, stats + 2);
+    k_gram_reduce<<<p.npairs * 16, 256, 0, s>>>(Spart, p.ksplit, Sred);
     if (cplx)
-      k_pair_evd<true><<<p.npairs, EVD_THREADS, evd_smem(true), s>>>(Spart, p.ksplit, inner, tol, Rimg, stats);
+      k_pair_evd<true><<<p.npairs, EVD_THREADS, evd_smem(true), s>>>(Sred, inner, tol, Rimg, stats);
     else
-      k_pair_evd<false><<<p.npairs, EVD_THREADS, evd_smem(false), s>>>(Spart, p.ksplit, inner, tol, Rimg, stats);
+      k_pair_evd<false><<<p.npairs, EVD_THREADS, evd_smem(false), s>>>(Sred, inner, tol, Rimg, stats);
     if (terms == 3)
       k_apply<3><<<p.npairs * p.q, APPLY_THREADS, APPLY_SMEM, s>>>(G, m, W, n, p.nb, step, p.tg, p.tw, p.q, Rimg,
                                                                     stats + 2);
@@ -917,43 +959,29 @@ extern "C" vj_fint vj_block_gram_dev(int cplx, vj_fnat m, vj_fnat n, const float
   cudaStream_t s = (cudaStream_t)stream;
   float *Spart = nullptr;
   unsigned *err = nullptr;
-  if (cudaMalloc(&Spart, (size_t)p.npairs * p.ksplit * TILE * TILE * 4) != cudaSuccess)
+  if (cudaMalloc(&Spart, (size_t)p.npairs * p.ksplit * 2 * TILE * TILE * 4) != cudaSuccess)
     return VJ_ERR_NOMEM;
   if (cudaMalloc(&err, 16) != cudaSuccess) {
     cudaFree(Spart);
     return VJ_ERR_NOMEM;
   }
   const Cols G{const_cast<float *>(Gr), cplx ? const_cast<float *>(Gi) : nullptr, (long long)ldG, p.b};
-  vj_fint r = 0;
   bool ok = cudaMemsetAsync(err, 0, 16, s) == cudaSuccess;
   if (ok) {
+    // the split partials, then S = their sum of F + E + E^T, pair by pair
     if (terms == 3)
       k_gram<3><<<p.npairs * p.ksplit, 128, GRAM_SMEM, s>>>(G, (int)m, p.nb, step, p.ksplit, Spart, err);
     else
       k_gram<6><<<p.npairs * p.ksplit, 128, GRAM_SMEM, s>>>(G, (int)m, p.nb, step, p.ksplit, Spart, err);
+    k_gram_reduce<<<p.npairs * 16, 256, 0, s>>>(Spart, p.ksplit, S);
     ok = cudaGetLastError() == cudaSuccess;
   }
-  // S = the sum of the K splits, pair by pair
-  std::vector<float> h((size_t)p.npairs * p.ksplit * TILE * TILE);
   unsigned he = 0;
-  ok = ok && cudaMemcpyAsync(h.data(), Spart, h.size() * 4, cudaMemcpyDeviceToHost, s) == cudaSuccess &&
-       cudaMemcpyAsync(&he, err, 4, cudaMemcpyDeviceToHost, s) == cudaSuccess && cudaStreamSynchronize(s) == cudaSuccess;
-  if (ok && !he) {
-    std::vector<float> o((size_t)p.npairs * TILE * TILE, 0.f);
-    for (int k = 0; k < p.npairs; ++k)
-      for (int q = 0; q < p.ksplit; ++q)
-        for (int e = 0; e < TILE * TILE; ++e)
-          o[(size_t)k * TILE * TILE + e] += h[((size_t)k * p.ksplit + q) * TILE * TILE + e];
-    ok = cudaMemcpyAsync(S, o.data(), o.size() * 4, cudaMemcpyHostToDevice, s) == cudaSuccess &&
-         cudaStreamSynchronize(s) == cudaSuccess;
-  }
-  else
-    ok = false;
+  ok = ok && cudaMemcpyAsync(&he, err, 4, cudaMemcpyDeviceToHost, s) == cudaSuccess &&
+       cudaStreamSynchronize(s) == cudaSuccess && !he;
   cudaFree(Spart);
   cudaFree(err);
-  if (!ok)
-    r = VJ_ERR_CUDA;
-  return r ? r : (vj_fint)p.npairs;
+  return ok ? (vj_fint)p.npairs : VJ_ERR_CUDA;
 }
 
 extern "C" vj_fint vj_block_apply_dev(int cplx, vj_fnat m, vj_fnat n, float *Gr, float *Gi, vj_fnat ldG, float *Wr,

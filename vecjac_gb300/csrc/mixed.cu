@@ -706,6 +706,9 @@ static vj_fint mixed_dev(vj_fnat m_, vj_fnat n_, double *G, vj_fnat ldG, double 
           ++nsteps;
         if (!(e0 < 0.5))
           nsteps = 5;
+        if (trace)
+          std::fprintf(stderr, "mixed SVD stage %u: max |W^H W - I| = %.3g, %d Newton-Schulz steps\n", stage, e0,
+                       nsteps);
       }
       if (!zgemm3m(h, CPLX, ni, ni, ni, Xp, Yp, Tp, Gp, s))
         return VJ_ERR_CUDA;
