@@ -444,6 +444,23 @@ static bool zgemm(cublasHandle_t h, bool cplx, bool conjA, int m, int n, int k, 
   return ok;
 }
 
+// d_c = Y(c, c)^-1/2 from the real plane of Y = X^H X (the squared column norms of X)
+__global__ void k_diag_rsqrt(const double *Y, long long n, double *d)
+{
+  for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x)
+    d[c] = 1.0 / sqrt(Y[c * n + c]);
+}
+
+// X(r, c) *= d_c and Y(r, c) *= d_r d_c for one plane of the n x n matrices X and Y
+__global__ void k_unit_cols(double *X, double *Y, const double *d, long long n)
+{
+  for (long long c = blockIdx.y; c < n; c += gridDim.y)
+    for (long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (long long)gridDim.x * blockDim.x) {
+      X[c * n + r] *= d[c];
+      Y[c * n + r] *= d[r] * d[c];
+    }
+}
+
 // max |Y(r, c) - I(r, c)| of one plane of an n x n matrix (diag: the real plane, which holds
 // the identity's ones) into *out, as the bits of a non-negative double
 __global__ void k_dev_identity(const double *Y, long long n, int diag, unsigned long long *out)
@@ -691,6 +708,13 @@ static vj_fint mixed_dev(vj_fnat m_, vj_fnat n_, double *G, vj_fnat ldG, double 
       if (!gram(h, CPLX, ni, Xp, Yp, Gp, s))
         return VJ_ERR_CUDA;
       if (it == 0) {
+        // columns of W to unit length first (X := X D, Y := D Y D with D = diag(Y)^-1/2):
+        // the FP32 stage's rounding shrinks or stretches W's columns slowly, and scaling is
+        // free of the Newton-Schulz steps that the off-diagonal error alone would need
+        double *dsc = T;  // n entries of scratch, free until the product below
+        k_diag_rsqrt<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(Y, n, dsc);
+        for (int pl = 0; pl < P; ++pl)
+          k_unit_cols<<<grid2(n, n), 256, 0, s>>>(X + pl * nn, Y + pl * nn, dsc, n);
         if (cudaMemsetAsync(cell, 0, 8, s) != cudaSuccess)
           return VJ_ERR_CUDA;
         for (int pl = 0; pl < P; ++pl)
@@ -701,9 +725,12 @@ static vj_fint mixed_dev(vj_fnat m_, vj_fnat n_, double *G, vj_fnat ldG, double 
           return VJ_ERR_CUDA;
         double e0;
         memcpy(&e0, &eb, 8);
-        nsteps = 1;
-        for (double e = e0; e > 1e-17 && nsteps < 5; e = 0.75 * e * e + 1e-17)
+        // steps until the predicted error is below 1e-16 (at least 2, at most 5)
+        nsteps = 0;
+        for (double e = e0; e > 1e-16 && nsteps < 5; e = 0.75 * e * e)
           ++nsteps;
+        if (nsteps < 2)
+          nsteps = 2;
         if (!(e0 < 0.5))
           nsteps = 5;
         if (trace)
