@@ -125,17 +125,18 @@ vj_fint vj_cvjsvd_dev(vj_fnat m, vj_fnat n, float *Gr, vj_fnat ldGr, float *Gi, 
                       unsigned stp, unsigned swp, int preset, void *stream);
 
 /* Mixed-precision SVD (FP64 data, result to FP64 accuracy): `stages` rounds (0: 2) of FP32
- * one-sided Jacobi sweeps on the current G rounded to FP32, each followed by FP64
- * re-orthogonalisation of the accumulated rotation W (2 to 5 Newton-Schulz steps, as its
- * distance from unitarity needs) and the
- * FP64 products G := G W, V := V W; FP64 sweeps with plain dot products on G and V to
- * twice the reference's tolerance; then FP64 finishing sweeps of dvjsvd_/zvjsvd_ with V
- * preset (the reference's iwork[0] != 0 mode, src/dvjsvd.c:88-96, src/zvjsvd.c:100-110).
- * Shape rules and return values are dvjsvd_'s/zvjsvd_'s (the finishing phase's sweep
- * count or its error); presweeps (optional, 2 entries) receives the number of FP32 sweeps
- * and of plain-dot FP64 sweeps. js/stp is the pivot table of every phase; swp caps each
- * phase (presweep phases at most 60). All arrays on the device. Links cuBLAS for the FP64
- * GEMMs. */
+ * one-sided Jacobi sweeps on the current G rounded to FP32 (block sweeps on the tensor
+ * cores where n allows, vj_block_sweep_dev), each followed by an FP64 Cholesky QR of the
+ * accumulated rotation W (columns in ascending order of norm) and the FP64 products
+ * G := G Q, V := V Q; FP64 sweeps with plain dot products on G and V to half the
+ * reference's tolerance; then the FP64 finishing sweeps of dvjsvd_/zvjsvd_ with V preset
+ * (the reference's iwork[0] != 0 mode, src/dvjsvd.c:88-96, src/zvjsvd.c:100-110), whose
+ * first sweep is checked for every pair at once first and skipped when it would change
+ * nothing. Shape rules and return values are dvjsvd_'s/zvjsvd_'s (the finishing phase's
+ * sweep count or its error); presweeps (optional, 2 entries) receives the number of FP32
+ * sweeps and of plain-dot FP64 sweeps. js/stp is the pivot table of every phase; swp caps
+ * each phase (presweep phases at most 60). All arrays on the device. Links cuBLAS and
+ * cuSOLVER for the FP64 GEMMs and the Cholesky factorisation. */
 vj_fint vj_dvjsvd_mixed_dev(vj_fnat m, vj_fnat n, double *G, vj_fnat ldG, double *V, vj_fnat ldV, double *eS,
                             double *fS, const unsigned *js, unsigned stp, unsigned swp, unsigned stages,
                             unsigned *presweeps, void *stream);
@@ -173,7 +174,7 @@ vj_fint vj_block_sweep_dev(int cplx, vj_fnat m, vj_fnat n, float *Gr, float *Gi,
                            vj_fnat ldW, float tol, int inner, int terms, float *mu, void *stream);
 
 /* Phase times of the last vj_?vjsvd_mixed_dev call on this process, in milliseconds:
- * out[0] FP32 sweeps, out[1] Newton-Schulz steps and GEMMs, out[2] plain-dot FP64 sweeps
+ * out[0] FP32 sweeps, out[1] orthonormalisation of W and the GEMMs, out[2] plain-dot FP64 sweeps
  * and the column sort, out[3] the reference's finishing sweeps; out[4] the number of FP32
  * kernel launches; out[5] 1 when the FP32 stages ran as block sweeps on the tensor cores,
  * 0 for column-pair sweeps. */

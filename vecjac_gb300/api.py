@@ -250,7 +250,7 @@ PHASES = ("control", "staging", "dots", "2x2", "rotations", "norms")
 
 
 def last_mixed_phases():
-    """Phase times (ms) of the last mixed-precision SVD: FP32 sweeps, Newton-Schulz + GEMMs,
+    """Phase times (ms) of the last mixed-precision SVD: FP32 sweeps, orthonormalisation + GEMMs,
     plain FP64 sweeps + sort, the reference's finishing sweeps; the FP32 kernel launches and
     whether the FP32 stages ran as block sweeps on the tensor cores."""
     out = (C.c_double * 6)()

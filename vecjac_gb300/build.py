@@ -67,7 +67,7 @@ def build(verbose=False, extra=(), lp64=False, out_dir=None):
         objs = list(ex.map(lambda s: _compile(s, extra, out), srcs))
     if os.path.exists(lib) and os.path.getmtime(lib) >= max(os.path.getmtime(o) for o in objs):
         return lib
-    cmd = [nvcc()] + ARCH + ["-shared", "-o", lib] + objs + ["-lcudart", "-lcublas"]
+    cmd = [nvcc()] + ARCH + ["-shared", "-o", lib] + objs + ["-lcudart", "-lcublas", "-lcusolver"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError("link failed:\n%s\n%s" % (" ".join(cmd), r.stderr))

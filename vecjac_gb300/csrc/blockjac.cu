@@ -23,6 +23,7 @@
 // the split BF16 tiles by the CTA's threads (the A side) or copied by the bulk-copy TMA
 // engine from the split image that k_pair_evd writes (the R side of k_apply).
 #include <cuda_bf16.h>
+#include <type_traits>
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -508,7 +509,7 @@ __global__ void __launch_bounds__(256) k_gram_reduce(const float *Spart, int ksp
 // cs = 1 / sqrt(1 + t^2), s = t cs c / |c|), with fast approximate division and reciprocal
 // square roots refined by one Newton step: these sweeps are a preconditioner, and the same
 // rotation is applied to G and W, so a rotation a few ulps from unitary changes nothing
-// but the accumulated W's orthogonality, which the FP64 Newton-Schulz steps restore.
+// but the accumulated W's orthogonality, which the FP64 orthonormalisation restores.
 struct Rot {
   float c, sr, si, d1, d2, ac, sc;
   int go;
@@ -555,30 +556,32 @@ __device__ __forceinline__ Rot pair_rot(float ha, float hb, float cr, float ci, 
 // by descending diagonal of the final H, and writes R's split image for k_apply.
 // stats[0] += rotations, stats[1] = max over rotated pairs of |h_pq| / sqrt(h_pp h_qq)
 // (as float bits).
+// Layout: complex H and R as interleaved (re, im) pairs, one 64-bit shared-memory access
+// per entry; each pair's rotation as one 16-byte record {c, Re s, Im s, p | q << 8 |
+// active << 16}.
 // Per Jacobi step: warp 0 (lane u: pair u, and u + 32 for real data) reads the step's
-// pairs from H and writes their rotations to shared memory; after a barrier every thread
-// updates 2x2 blocks of H := J^H H J from a list (the off-diagonal blocks u < v first, then
-// the diagonal ones) and columns of R := R J (lane v: pair v, each warp a share of the
-// rows); a second barrier ends the step.
+// pairs from H, writes their rotation records and, for the pairs it rotates, the new 2x2
+// diagonal blocks of H (no other block touches them); after a barrier every thread updates
+// off-diagonal 2x2 blocks (u, v), u < v, of H := J^H H J from a list, and columns of
+// R := R J (lane v: pair v, each warp a share of the rows); a second barrier ends the step.
 constexpr int EVD_THREADS = 256;
 template <bool CPLX>
 __global__ void __launch_bounds__(EVD_THREADS) k_pair_evd(const float *Sred, int sweeps, float tol,
                                                           unsigned char *Rimg, unsigned *stats)
 {
+  using E = typename std::conditional<CPLX, float2, float>::type;
   constexpr int N = CPLX ? 64 : 128;  // order of H
   constexpr int P = N / 2;             // pairs per Jacobi step
   constexpr int PL = P / 32;           // pairs per lane
   constexpr int LD = N + 1;
   constexpr int NO = P * (P - 1) / 2;  // off-diagonal blocks u < v
-  constexpr int NB = NO + P;           // and the diagonal ones
   constexpr int NW = EVD_THREADS / 32;
   extern __shared__ __align__(16) float fsm[];
-  float *Hr = fsm, *Hi = Hr + N * LD;
-  float *Rr = Hi + (CPLX ? N * LD : 0), *Ri = Rr + N * LD;
-  float *rc = Ri + (CPLX ? N * LD : 0), *rsr = rc + P, *rsi = rsr + P, *rd1 = rsi + P, *rd2 = rd1 + P;
-  int *rp = reinterpret_cast<int *>(rd2 + P), *rq = rp + P, *ract = rq + P;
-  unsigned short *tri = reinterpret_cast<unsigned short *>(ract + P);  // NB entries: u << 8 | v
-  int *rank = reinterpret_cast<int *>(tri + ((NB + 1) & ~1));
+  float4 *rot = reinterpret_cast<float4 *>(fsm);  // P records
+  E *H = reinterpret_cast<E *>(rot + P);
+  E *R = H + N * LD;
+  unsigned short *tri = reinterpret_cast<unsigned short *>(R + N * LD);  // NO entries: u << 8 | v
+  int *rank = reinterpret_cast<int *>(tri + ((NO + 1) & ~1));
   __shared__ unsigned nrot_s, mu_s;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const float *S0 = Sred + (size_t)blockIdx.x * TILE * TILE;
@@ -590,41 +593,45 @@ __global__ void __launch_bounds__(EVD_THREADS) k_pair_evd(const float *Sred, int
     const int u = q / P, v = q % P;
     if (u < v)
       tri[u * P - u * (u + 1) / 2 + (v - u - 1)] = (unsigned short)((u << 8) | v);
-    else if (u == v)
-      tri[NO + u] = (unsigned short)((u << 8) | u);
   }
-  // S = sum of the partials; H from S (upper triangle, mirrored: exactly Hermitian)
+  // H from S (upper triangle, mirrored: exactly Hermitian); R := I
   for (int q = tid; q < N * N; q += EVD_THREADS) {
     const int i = q / N, j = q % N;
     if (i > j)
       continue;
     auto S = [&](int a, int b) { return S0[a * TILE + b]; };
-    if (CPLX) {
+    if constexpr (CPLX) {
       const float hr = S(i, j) + S(64 + i, 64 + j);
       const float hi = (i == j) ? 0.f : (S(i, 64 + j) - S(64 + i, j));
-      Hr[i * LD + j] = hr;
-      Hi[i * LD + j] = hi;
-      Hr[j * LD + i] = hr;
-      Hi[j * LD + i] = -hi;
+      H[i * LD + j] = make_float2(hr, hi);
+      H[j * LD + i] = make_float2(hr, -hi);
     }
     else {
       const float h = S(i, j);
-      Hr[i * LD + j] = h;
-      Hr[j * LD + i] = h;
+      H[i * LD + j] = h;
+      H[j * LD + i] = h;
     }
   }
   for (int q = tid; q < N * N; q += EVD_THREADS) {
     const int i = q / N, j = q % N;
-    Rr[i * LD + j] = (i == j) ? 1.f : 0.f;
-    if (CPLX)
-      Ri[i * LD + j] = 0.f;
+    if constexpr (CPLX)
+      R[i * LD + j] = make_float2((i == j) ? 1.f : 0.f, 0.f);
+    else
+      R[i * LD + j] = (i == j) ? 1.f : 0.f;
   }
   __syncthreads();
+  auto re = [](const E &x) -> float {
+    if constexpr (CPLX)
+      return x.x;
+    else
+      return x;
+  };
   unsigned nrot = 0u;
   float mu = 0.f;
   for (int sw = 0; sw < sweeps; ++sw)
     for (int stp = 0; stp < N - 1; ++stp) {
-      // the step's pairs and their rotations (warp 0; lane u: pairs u, u + 32)
+      // the step's pairs, their rotations and new diagonal blocks (warp 0; lane u: pairs
+      // u, u + 32)
       if (warp == 0) {
 #pragma unroll
         for (int h = 0; h < PL; ++h) {
@@ -644,16 +651,32 @@ __global__ void __launch_bounds__(EVD_THREADS) k_pair_evd(const float *Sred, int
           // modulo N - 1, and so are the second ones, so that the row and column accesses of
           // the updates fall into distinct shared-memory banks)
           const int p = a, q = c;
-          const Rot r = pair_rot(fmaxf(Hr[p * LD + p], 0.f), fmaxf(Hr[q * LD + q], 0.f), Hr[p * LD + q],
-                                 CPLX ? Hi[p * LD + q] : 0.f, tol);
-          rc[u] = r.c;
-          rsr[u] = r.sr;
-          rsi[u] = r.si;
-          rd1[u] = r.d1;
-          rd2[u] = r.d2;
-          rp[u] = p;
-          rq[u] = q;
-          ract[u] = r.go && ((r.sr != 0.f) || (r.si != 0.f));
+          const E hpq = H[p * LD + q];
+          float cr, ci = 0.f;
+          if constexpr (CPLX) {
+            cr = hpq.x;
+            ci = hpq.y;
+          }
+          else
+            cr = hpq;
+          const Rot r = pair_rot(fmaxf(re(H[p * LD + p]), 0.f), fmaxf(re(H[q * LD + q]), 0.f), cr, ci, tol);
+          const bool act = r.go && ((r.sr != 0.f) || (r.si != 0.f));
+          const unsigned tag = (unsigned)p | ((unsigned)q << 8) | (act ? (1u << 16) : 0u);
+          rot[u] = act ? make_float4(r.c, r.sr, r.si, __uint_as_float(tag)) : make_float4(1.f, 0.f, 0.f, __uint_as_float(tag));
+          if (act) {
+            if constexpr (CPLX) {
+              H[p * LD + p] = make_float2(r.d1, 0.f);
+              H[q * LD + q] = make_float2(r.d2, 0.f);
+              H[p * LD + q] = make_float2(0.f, 0.f);
+              H[q * LD + p] = make_float2(0.f, 0.f);
+            }
+            else {
+              H[p * LD + p] = r.d1;
+              H[q * LD + q] = r.d2;
+              H[p * LD + q] = 0.f;
+              H[q * LD + p] = 0.f;
+            }
+          }
           if (r.go) {
             ++nrot;
             mu = fmaxf(mu, (r.sc > 0.f) ? r.ac / r.sc : 1.f);
@@ -661,93 +684,83 @@ __global__ void __launch_bounds__(EVD_THREADS) k_pair_evd(const float *Sred, int
         }
       }
       __syncthreads();
-      // H := J^H H J, one 2x2 block (u, v) per item, the (v, u) block its conjugate transpose
-      for (int q = tid; q < NB; q += EVD_THREADS) {
-        const int u = tri[q] >> 8, v = tri[q] & 255;
-        const int au = ract[u], av = ract[v];
-        if (!(au | av))
+      // H := J^H H J, one off-diagonal 2x2 block (u, v) per item, the (v, u) block its
+      // conjugate transpose (an inactive side is the identity)
+      for (int it = tid; it < NO; it += EVD_THREADS) {
+        const unsigned uv = tri[it];
+        const float4 ru = rot[uv >> 8], rv = rot[uv & 255];
+        const unsigned tu = __float_as_uint(ru.w), tv = __float_as_uint(rv.w);
+        if (!((tu | tv) >> 16))
           continue;
-        const int pu = rp[u], qu = rq[u];
-        if (u == v) {
-          Hr[pu * LD + pu] = rd1[u];
-          Hr[qu * LD + qu] = rd2[u];
-          Hr[pu * LD + qu] = 0.f;
-          Hr[qu * LD + pu] = 0.f;
-          if (CPLX) {
-            Hi[pu * LD + qu] = 0.f;
-            Hi[qu * LD + pu] = 0.f;
-          }
-          continue;
+        const int pu = tu & 255, qu = (tu >> 8) & 255, pv = tv & 255, qv = (tv >> 8) & 255;
+        const float cu = ru.x, sur = ru.y, sui = ru.z;
+        const float cv = rv.x, svr = rv.y, svi = rv.z;
+        if constexpr (CPLX) {
+          const float2 b00 = H[pu * LD + pv], b01 = H[pu * LD + qv], b10 = H[qu * LD + pv], b11 = H[qu * LD + qv];
+          // C = B J_v: C[:,0] = cv B[:,0] - conj(s_v) B[:,1], C[:,1] = cv B[:,1] + s_v B[:,0]
+          const float c00r = fmaf(cv, b00.x, -fmaf(svr, b01.x, svi * b01.y));
+          const float c00i = fmaf(cv, b00.y, -fmaf(svr, b01.y, -(svi * b01.x)));
+          const float c10r = fmaf(cv, b10.x, -fmaf(svr, b11.x, svi * b11.y));
+          const float c10i = fmaf(cv, b10.y, -fmaf(svr, b11.y, -(svi * b11.x)));
+          const float c01r = fmaf(cv, b01.x, fmaf(svr, b00.x, -(svi * b00.y)));
+          const float c01i = fmaf(cv, b01.y, fmaf(svr, b00.y, svi * b00.x));
+          const float c11r = fmaf(cv, b11.x, fmaf(svr, b10.x, -(svi * b10.y)));
+          const float c11i = fmaf(cv, b11.y, fmaf(svr, b10.y, svi * b10.x));
+          // B' = J_u^H C: row 0 = cu C[0,:] - s_u C[1,:], row 1 = cu C[1,:] + conj(s_u) C[0,:]
+          const float n00r = fmaf(cu, c00r, -fmaf(sur, c10r, -(sui * c10i)));
+          const float n00i = fmaf(cu, c00i, -fmaf(sur, c10i, sui * c10r));
+          const float n01r = fmaf(cu, c01r, -fmaf(sur, c11r, -(sui * c11i)));
+          const float n01i = fmaf(cu, c01i, -fmaf(sur, c11i, sui * c11r));
+          const float n10r = fmaf(cu, c10r, fmaf(sur, c00r, sui * c00i));
+          const float n10i = fmaf(cu, c10i, fmaf(sur, c00i, -(sui * c00r)));
+          const float n11r = fmaf(cu, c11r, fmaf(sur, c01r, sui * c01i));
+          const float n11i = fmaf(cu, c11i, fmaf(sur, c01i, -(sui * c01r)));
+          H[pu * LD + pv] = make_float2(n00r, n00i);
+          H[pu * LD + qv] = make_float2(n01r, n01i);
+          H[qu * LD + pv] = make_float2(n10r, n10i);
+          H[qu * LD + qv] = make_float2(n11r, n11i);
+          H[pv * LD + pu] = make_float2(n00r, -n00i);
+          H[qv * LD + pu] = make_float2(n01r, -n01i);
+          H[pv * LD + qu] = make_float2(n10r, -n10i);
+          H[qv * LD + qu] = make_float2(n11r, -n11i);
         }
-        const int pv = rp[v], qv = rq[v];
-        const float cu = rc[u], sur = rsr[u], sui = rsi[u];
-        const float cv = rc[v], svr = rsr[v], svi = rsi[v];
-        const float b00r = Hr[pu * LD + pv], b01r = Hr[pu * LD + qv], b10r = Hr[qu * LD + pv], b11r = Hr[qu * LD + qv];
-        float b00i = 0.f, b01i = 0.f, b10i = 0.f, b11i = 0.f;
-        if (CPLX) {
-          b00i = Hi[pu * LD + pv];
-          b01i = Hi[pu * LD + qv];
-          b10i = Hi[qu * LD + pv];
-          b11i = Hi[qu * LD + qv];
-        }
-        // C = B J_v: C[:,0] = cv B[:,0] - conj(s_v) B[:,1], C[:,1] = cv B[:,1] + s_v B[:,0]
-        const float c00r = fmaf(cv, b00r, -fmaf(svr, b01r, svi * b01i));
-        const float c00i = fmaf(cv, b00i, -fmaf(svr, b01i, -(svi * b01r)));
-        const float c10r = fmaf(cv, b10r, -fmaf(svr, b11r, svi * b11i));
-        const float c10i = fmaf(cv, b10i, -fmaf(svr, b11i, -(svi * b11r)));
-        const float c01r = fmaf(cv, b01r, fmaf(svr, b00r, -(svi * b00i)));
-        const float c01i = fmaf(cv, b01i, fmaf(svr, b00i, svi * b00r));
-        const float c11r = fmaf(cv, b11r, fmaf(svr, b10r, -(svi * b10i)));
-        const float c11i = fmaf(cv, b11i, fmaf(svr, b10i, svi * b10r));
-        // B' = J_u^H C: row 0 = cu C[0,:] - s_u C[1,:], row 1 = cu C[1,:] + conj(s_u) C[0,:]
-        const float n00r = fmaf(cu, c00r, -fmaf(sur, c10r, -(sui * c10i)));
-        const float n00i = fmaf(cu, c00i, -fmaf(sur, c10i, sui * c10r));
-        const float n01r = fmaf(cu, c01r, -fmaf(sur, c11r, -(sui * c11i)));
-        const float n01i = fmaf(cu, c01i, -fmaf(sur, c11i, sui * c11r));
-        const float n10r = fmaf(cu, c10r, fmaf(sur, c00r, sui * c00i));
-        const float n10i = fmaf(cu, c10i, fmaf(sur, c00i, -(sui * c00r)));
-        const float n11r = fmaf(cu, c11r, fmaf(sur, c01r, sui * c01i));
-        const float n11i = fmaf(cu, c11i, fmaf(sur, c01i, -(sui * c01r)));
-        Hr[pu * LD + pv] = n00r;
-        Hr[pu * LD + qv] = n01r;
-        Hr[qu * LD + pv] = n10r;
-        Hr[qu * LD + qv] = n11r;
-        Hr[pv * LD + pu] = n00r;
-        Hr[qv * LD + pu] = n01r;
-        Hr[pv * LD + qu] = n10r;
-        Hr[qv * LD + qu] = n11r;
-        if (CPLX) {
-          Hi[pu * LD + pv] = n00i;
-          Hi[pu * LD + qv] = n01i;
-          Hi[qu * LD + pv] = n10i;
-          Hi[qu * LD + qv] = n11i;
-          Hi[pv * LD + pu] = -n00i;
-          Hi[qv * LD + pu] = -n01i;
-          Hi[pv * LD + qu] = -n10i;
-          Hi[qv * LD + qu] = -n11i;
+        else {
+          const float b00 = H[pu * LD + pv], b01 = H[pu * LD + qv], b10 = H[qu * LD + pv], b11 = H[qu * LD + qv];
+          const float c00 = fmaf(cv, b00, -(svr * b01)), c10 = fmaf(cv, b10, -(svr * b11));
+          const float c01 = fmaf(cv, b01, svr * b00), c11 = fmaf(cv, b11, svr * b10);
+          const float n00 = fmaf(cu, c00, -(sur * c10)), n01 = fmaf(cu, c01, -(sur * c11));
+          const float n10 = fmaf(cu, c10, sur * c00), n11 = fmaf(cu, c11, sur * c01);
+          H[pu * LD + pv] = n00;
+          H[pu * LD + qv] = n01;
+          H[qu * LD + pv] = n10;
+          H[qu * LD + qv] = n11;
+          H[pv * LD + pu] = n00;
+          H[qv * LD + pu] = n01;
+          H[pv * LD + qu] = n10;
+          H[qv * LD + qu] = n11;
         }
       }
       // R := R J: lane v takes pair v (and v + 32), warp w the rows w, w + NW, ...
 #pragma unroll
       for (int h = 0; h < PL; ++h) {
         const int v = lane + 32 * h;
-        if (!ract[v])
+        const float4 rv = rot[v];
+        const unsigned tv = __float_as_uint(rv.w);
+        if (!(tv >> 16))
           continue;
-        const int pv = rp[v], qv = rq[v];
-        const float cv = rc[v], svr = rsr[v], svi = rsi[v];
+        const int pv = tv & 255, qv = (tv >> 8) & 255;
+        const float cv = rv.x, svr = rv.y, svi = rv.z;
 #pragma unroll 4
         for (int r = warp; r < N; r += NW) {
-          const float xr = Rr[r * LD + pv], yr = Rr[r * LD + qv];
-          if (CPLX) {
-            const float xi = Ri[r * LD + pv], yi = Ri[r * LD + qv];
-            Rr[r * LD + pv] = fmaf(cv, xr, -fmaf(svr, yr, svi * yi));
-            Rr[r * LD + qv] = fmaf(cv, yr, fmaf(svr, xr, -(svi * xi)));
-            Ri[r * LD + pv] = fmaf(cv, xi, -fmaf(svr, yi, -(svi * yr)));
-            Ri[r * LD + qv] = fmaf(cv, yi, fmaf(svr, xi, svi * xr));
+          if constexpr (CPLX) {
+            const float2 x = R[r * LD + pv], y = R[r * LD + qv];
+            R[r * LD + pv] = make_float2(fmaf(cv, x.x, -fmaf(svr, y.x, svi * y.y)), fmaf(cv, x.y, -fmaf(svr, y.y, -(svi * y.x))));
+            R[r * LD + qv] = make_float2(fmaf(cv, y.x, fmaf(svr, x.x, -(svi * x.y))), fmaf(cv, y.y, fmaf(svr, x.y, svi * x.x)));
           }
           else {
-            Rr[r * LD + pv] = fmaf(cv, xr, -(svr * yr));
-            Rr[r * LD + qv] = fmaf(cv, yr, svr * xr);
+            const float x = R[r * LD + pv], y = R[r * LD + qv];
+            R[r * LD + pv] = fmaf(cv, x, -(svr * y));
+            R[r * LD + qv] = fmaf(cv, y, svr * x);
           }
         }
       }
@@ -756,7 +769,7 @@ __global__ void __launch_bounds__(EVD_THREADS) k_pair_evd(const float *Sred, int
   // descending order of the diagonal (ties by index): column rank[r] of R goes to place r
   // (a NaN sorts as -inf, so that the ranks stay a permutation)
   auto key = [&](int i) {
-    const float d = Hr[i * LD + i];
+    const float d = re(H[i * LD + i]);
     return (d == d) ? d : -INFINITY;
   };
   for (int i = tid; i < N; i += EVD_THREADS) {
@@ -776,15 +789,14 @@ __global__ void __launch_bounds__(EVD_THREADS) k_pair_evd(const float *Sred, int
   }
   __syncthreads();
   unsigned char *img = Rimg + (size_t)blockIdx.x * 6 * PLANE;
-  if (CPLX)
+  if constexpr (CPLX)
     // Rb = [[Re R, Im R], [-Im R, Re R]] with R's columns reordered
     write_rimg(img, [&](int k, int i) {
-      const int kr = k & 63, ic = rank[i & 63];
-      const float re = Rr[kr * LD + ic], im = Ri[kr * LD + ic];
-      return (k < 64) ? ((i < 64) ? re : im) : ((i < 64) ? -im : re);
+      const float2 x = R[(k & 63) * LD + rank[i & 63]];
+      return (k < 64) ? ((i < 64) ? x.x : x.y) : ((i < 64) ? -x.y : x.x);
     });
   else
-    write_rimg(img, [&](int k, int i) { return Rr[k * LD + rank[i]]; });
+    write_rimg(img, [&](int k, int i) { return R[k * LD + rank[i]]; });
   if (tid == 0) {
     if (nrot_s)
       atomicAdd(stats, nrot_s);
@@ -803,8 +815,8 @@ __global__ void __launch_bounds__(256) k_rimg(const float *R, unsigned char *Rim
 
 static size_t evd_smem(bool cplx)
 {
-  const int N = cplx ? 64 : 128, P = N / 2, LD = N + 1, NB = P * (P + 1) / 2;
-  return (size_t)(cplx ? 4 : 2) * N * LD * 4 + (size_t)8 * P * 4 + (size_t)((NB + 1) & ~1) * 2 + (size_t)N * 4;
+  const int N = cplx ? 64 : 128, P = N / 2, LD = N + 1, NO = P * (P - 1) / 2;
+  return (size_t)P * 16 + (size_t)2 * N * LD * (cplx ? 8 : 4) + (size_t)((NO + 1) & ~1) * 2 + (size_t)N * 4;
 }
 
 constexpr size_t GRAM_SMEM = 2 * 3 * PLANE + 1024;

@@ -4,13 +4,13 @@
 // done in FP32 and only the last ones in FP64. Starting from G_0 = A (FP64), V_0 = I, each
 // preconditioning stage s = 1..S
 //   1. rounds G_{s-1} (scaled by a power of two to max |g_ij| <= 1) to FP32;
-//   2. runs FP32 one-sided Jacobi sweeps on it (k_presweep_reg / k_presweep, Hestenes
-//      rotations from plain FP32 dot products) from W := I until no pair exceeds the FP32
-//      tolerance;
-//   3. widens W to FP64 and makes it orthonormal to FP64 accuracy with Newton-Schulz polar
-//      steps, W <- W (3I - W^H W) / 2 (each step maps an error e of W^H W - I to about
-//      3e^2/4; the number of steps, 2 to 5, follows from the error measured first);
-//   4. forms G_s = G_{s-1} W and V_s = V_{s-1} W (FP64 GEMMs).
+//   2. runs FP32 one-sided Jacobi sweeps on it from W := I until no pair exceeds the FP32
+//      tolerance: block sweeps with split-BF16x3 tensor-core products (blockjac.cu) where
+//      n is a whole number of block pairs, else column-pair Hestenes sweeps (k_presweep_reg
+//      / k_presweep, rotations from plain FP32 dot products);
+//   3. widens W to FP64 and makes it unitary to FP64 accuracy by a Cholesky QR with its
+//      columns in ascending order of norm (cuSOLVER's Cholesky, a triangular solve);
+//   4. forms G_s = G_{s-1} Q and V_s = V_{s-1} Q (FP64 GEMMs).
 // FP32 rounding is relative to each element, so from the second stage on the FP32 sweeps
 // see the columns of G_{s-1} to their own relative accuracy and resolve the directions of
 // small singular values that the first stage (on A itself) could not. FP64 sweeps with
@@ -18,9 +18,10 @@
 // columns to FP64 orthogonality. Finally dvjsvd_/zvjsvd_'s algorithm runs on G with V as
 // the preset matrix (the reference's iwork[0] != 0 mode, src/dvjsvd.c:88-96,
 // src/zvjsvd.c:100-110): G R = U Sigma and V R = V, so A = U Sigma V^H with the FP64
-// algorithm's accuracy and convergence test, after one or two of its sweeps instead of a
-// full run. The GEMMs are plain library GEMMs (cuBLAS DGEMM; four
-// real products per complex one on the split planes).
+// algorithm's accuracy and convergence test; its first sweep is checked for every pair at
+// once (jsvd.cu, k_confirm) and skipped when it would transform nothing. The FP64 GEMMs
+// are plain library GEMMs (cuBLAS DGEMM; four or three real products per complex one on
+// the split planes).
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -31,6 +32,7 @@
 
 #include <cublas_v2.h>
 #include <cuda_runtime.h>
+#include <cusolverDn.h>
 
 #include "svd_core.cuh"
 #include "vj_fp.cuh"
@@ -421,6 +423,57 @@ static cublasHandle_t cublas()
   return h;
 }
 
+static cusolverDnHandle_t cusolver()
+{
+  static cusolverDnHandle_t h = nullptr;
+  if (!h && cusolverDnCreate(&h) != CUSOLVER_STATUS_SUCCESS)
+    h = nullptr;
+  return h;
+}
+
+// squared 2-norms of the columns of planar FP32 G (one CTA per column): the order key of
+// the orthonormalisation below
+template <bool CPLX>
+__global__ void __launch_bounds__(256) k_colnorm2_f32(int m, const float *Gr, const float *Gi, double *out)
+{
+  __shared__ double red[8];
+  const int j = blockIdx.x;
+  double a = 0;
+  for (int i = threadIdx.x; i < m; i += blockDim.x) {
+    const double x = Gr[(size_t)j * m + i];
+    a = fma(x, x, a);
+    if (CPLX) {
+      const double y = Gi[(size_t)j * m + i];
+      a = fma(y, y, a);
+    }
+  }
+  for (int o = 16; o >= 1; o >>= 1)
+    a += __shfl_xor_sync(0xffffffffu, a, o);
+  if ((threadIdx.x & 31) == 0)
+    red[threadIdx.x >> 5] = a;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    a = 0;
+    for (int w = 0; w < 8; ++w)
+      a += red[w];
+    out[j] = a;
+  }
+}
+
+// planar (re, im) n x n <-> interleaved complex n x n (both with leading dimension n)
+__global__ void k_to_interleaved(const double *re, const double *im, long long nn, double2 *z)
+{
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nn; i += (long long)gridDim.x * blockDim.x)
+    z[i] = make_double2(re[i], im[i]);
+}
+__global__ void k_from_interleaved(const double2 *z, long long nn, double *re, double *im)
+{
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < nn; i += (long long)gridDim.x * blockDim.x) {
+    re[i] = z[i].x;
+    im[i] = z[i].y;
+  }
+}
+
 // split-plane complex matrix: real and imaginary planes with their leading dimensions
 struct Planes {
   double *re, *im;
@@ -442,42 +495,6 @@ static bool zgemm(cublasHandle_t h, bool cplx, bool conjA, int m, int n, int k, 
   // imaginary part: Ar Bi + Ai Br, or Ar^T Bi - Ai^T Br for A^H
   ok = ok && g(A.re, A.ldr, B.im, B.ldi, 1.0, 0.0, Cm.im, Cm.ldi) && g(A.im, A.ldi, B.re, B.ldr, -sgn, 1.0, Cm.im, Cm.ldi);
   return ok;
-}
-
-// d_c = Y(c, c)^-1/2 from the real plane of Y = X^H X (the squared column norms of X)
-__global__ void k_diag_rsqrt(const double *Y, long long n, double *d)
-{
-  for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (long long)gridDim.x * blockDim.x)
-    d[c] = 1.0 / sqrt(Y[c * n + c]);
-}
-
-// X(r, c) *= d_c and Y(r, c) *= d_r d_c for one plane of the n x n matrices X and Y
-__global__ void k_unit_cols(double *X, double *Y, const double *d, long long n)
-{
-  for (long long c = blockIdx.y; c < n; c += gridDim.y)
-    for (long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (long long)gridDim.x * blockDim.x) {
-      X[c * n + r] *= d[c];
-      Y[c * n + r] *= d[r] * d[c];
-    }
-}
-
-// max |Y(r, c) - I(r, c)| of one plane of an n x n matrix (diag: the real plane, which holds
-// the identity's ones) into *out, as the bits of a non-negative double
-__global__ void k_dev_identity(const double *Y, long long n, int diag, unsigned long long *out)
-{
-  unsigned long long mx = 0ull;
-  for (long long c = blockIdx.y; c < n; c += gridDim.y)
-    for (long long r = (long long)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (long long)gridDim.x * blockDim.x) {
-      const double d = fabs(Y[c * n + r] - ((diag && r == c) ? 1.0 : 0.0));
-      const unsigned long long b = (d == d) ? (unsigned long long)__double_as_longlong(d) : 0x7ff0000000000000ull;
-      mx = (b > mx) ? b : mx;
-    }
-  for (int o = 16; o >= 1; o >>= 1) {
-    const unsigned long long w = __shfl_xor_sync(0xffffffffu, mx, o);
-    mx = (w > mx) ? w : mx;
-  }
-  if ((threadIdx.x & 31) == 0 && mx)
-    atomicMax(out, mx);
 }
 
 // T(r, c) = T(c, r) for r < c (fill the upper triangle of an n x n matrix from the lower)
@@ -678,6 +695,9 @@ static vj_fint mixed_dev(vj_fnat m_, vj_fnat n_, double *G, vj_fnat ldG, double 
                                       n, js, stp, tol, cnt, s, &mu);
       if (hc < 0)
         return VJ_ERR_CUDA;
+      if (trace)
+        std::fprintf(stderr, "mixed SVD stage %u sweep %u: %lld rotations, max scaled |h_pq| %.3e\n", stage, sw, hc,
+                     (double)mu);
       if (!hc)
         break;
       if (mu < stop) {
@@ -695,55 +715,86 @@ static vj_fint mixed_dev(vj_fnat m_, vj_fnat n_, double *G, vj_fnat ldG, double 
     }
     if (!sw)
       break;  // already orthogonal to the FP32 level: later stages would change nothing
-    // 3. W (FP64) with two Newton-Schulz steps: Y = W^H W, T = W Y, W = 1.5 W - 0.5 T
+    // 3. W (FP64) made unitary by one Cholesky QR, Q = W R^-1 with R^H R = W^H W (a Gram
+    //    product, cuSOLVER's Cholesky factorisation, a triangular solve): W^H W is within
+    //    1e-4 of I after the FP32 stage, so one pass is unitary to FP64 accuracy, at about
+    //    half the cost of the two Newton-Schulz steps that the same accuracy needs. W's
+    //    columns go in ascending order of the norms of the FP32 G's columns first: R^-1 is
+    //    upper triangular, so the correction mixes into each column of G Q only columns of
+    //    smaller norm (the polar factor would also spread large columns into small ones).
+    //    (The first FP64 sweep below still meets scaled inner products of up to ~1e-2: the
+    //    FP32 rounding of W's own entries couples large columns of G into small ones.)
     for (int pl = 0; pl < P; ++pl)
       k_to_f64<<<(unsigned)((nn + 255) / 256 < 4096 ? (nn + 255) / 256 : 4096), 256, 0, s>>>(
           W32 + pl * nn, (long long)nn, X + pl * nn);
-    // (the Gram product by symmetric rank-k updates, the products of near-unitary
-    // matrices by 3M; the Gp scratch, free until step 4, holds their temporaries)
-    // (as many steps as W's distance from unitarity needs: each step maps an error e of
-    // W^H W - I to about 3e^2/4, and the FP32 stage leaves e between 1e-6 and 1e-3)
-    int nsteps = 2;
-    for (int it = 0; it < nsteps; ++it) {
-      if (!gram(h, CPLX, ni, Xp, Yp, Gp, s))
+    {
+      double *nrm = Y;  // n entries of scratch, free until the Gram product below
+      int *perm = reinterpret_cast<int *>(Y + n);
+      k_colnorm2_f32<CPLX><<<(unsigned)n, 256, 0, s>>>(mi, G32, CPLX ? G32 + mn : nullptr, nrm);
+      std::vector<double> hn((size_t)n);
+      std::vector<int> hp((size_t)n);
+      if (cudaMemcpyAsync(hn.data(), nrm, (size_t)n * 8, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+          cudaStreamSynchronize(s) != cudaSuccess)
         return VJ_ERR_CUDA;
-      if (it == 0) {
-        // columns of W to unit length first (X := X D, Y := D Y D with D = diag(Y)^-1/2):
-        // the FP32 stage's rounding shrinks or stretches W's columns slowly, and scaling is
-        // free of the Newton-Schulz steps that the off-diagonal error alone would need
-        double *dsc = T;  // n entries of scratch, free until the product below
-        k_diag_rsqrt<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(Y, n, dsc);
-        for (int pl = 0; pl < P; ++pl)
-          k_unit_cols<<<grid2(n, n), 256, 0, s>>>(X + pl * nn, Y + pl * nn, dsc, n);
-        if (cudaMemsetAsync(cell, 0, 8, s) != cudaSuccess)
-          return VJ_ERR_CUDA;
-        for (int pl = 0; pl < P; ++pl)
-          k_dev_identity<<<grid2(n, n), 256, 0, s>>>(Y + pl * nn, n, pl == 0, cell);
-        unsigned long long eb = 0;
-        if (cudaMemcpyAsync(&eb, cell, 8, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
-            cudaStreamSynchronize(s) != cudaSuccess)
-          return VJ_ERR_CUDA;
-        double e0;
-        memcpy(&e0, &eb, 8);
-        // steps until the predicted error is below 1e-16 (at least 2, at most 5)
-        nsteps = 0;
-        for (double e = e0; e > 1e-16 && nsteps < 5; e = 0.75 * e * e)
-          ++nsteps;
-        if (nsteps < 2)
-          nsteps = 2;
-        if (!(e0 < 0.5))
-          nsteps = 5;
-        if (trace)
-          std::fprintf(stderr, "mixed SVD stage %u: max |W^H W - I| = %.3g, %d Newton-Schulz steps\n", stage, e0,
-                       nsteps);
-      }
-      if (!zgemm3m(h, CPLX, ni, ni, ni, Xp, Yp, Tp, Gp, s))
+      for (int j = 0; j < ni; ++j)
+        hp[(size_t)j] = j;
+      std::stable_sort(hp.begin(), hp.end(), [&](int x, int y) { return hn[(size_t)x] < hn[(size_t)y]; });
+      if (cudaMemcpyAsync(perm, hp.data(), (size_t)n * 4, cudaMemcpyHostToDevice, s) != cudaSuccess)
         return VJ_ERR_CUDA;
-      const double a15 = 1.5, am05 = -0.5;
+      // T := W with its columns permuted (the copy reads the host vector: wait for it)
       for (int pl = 0; pl < P; ++pl)
-        if (cublasDgeam(h, CUBLAS_OP_N, CUBLAS_OP_N, ni, ni, &a15, X + pl * nn, ni, &am05, T + pl * nn, ni,
-                        X + pl * nn, ni) != CUBLAS_STATUS_SUCCESS)
+        k_gather_cols<<<grid2(n, n), 256, 0, s>>>(ni, ni, X + pl * nn, n, perm, T + pl * nn);
+      if (cudaStreamSynchronize(s) != cudaSuccess)
+        return VJ_ERR_CUDA;
+    }
+    if (!gram(h, CPLX, ni, Tp, Yp, Gp, s))
+      return VJ_ERR_CUDA;
+    {
+      cusolverDnHandle_t hs = cusolver();
+      if (!hs || cusolverDnSetStream(hs, s) != CUSOLVER_STATUS_SUCCESS)
+        return VJ_ERR_CUDA;
+      int *info = reinterpret_cast<int *>(cell);
+      static host::Staging wsp;  // the factorisation's workspace
+      const double one = 1.0;
+      int lw = 0, hinfo = 0;
+      if (!CPLX) {
+        // R overwrites the upper triangle of Y; T := T R^-1
+        if (cusolverDnDpotrf_bufferSize(hs, CUBLAS_FILL_MODE_UPPER, ni, Y, ni, &lw) != CUSOLVER_STATUS_SUCCESS ||
+            !wsp.reserve((size_t)(lw > 0 ? lw : 1) * 8) ||
+            cusolverDnDpotrf(hs, CUBLAS_FILL_MODE_UPPER, ni, Y, ni, reinterpret_cast<double *>(wsp.ptr), lw, info) !=
+                CUSOLVER_STATUS_SUCCESS ||
+            cublasDtrsm(h, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, ni, ni, &one,
+                        Y, ni, T, ni) != CUBLAS_STATUS_SUCCESS)
           return VJ_ERR_CUDA;
+      }
+      else {
+        // interleaved copies for the complex factorisation: Z = W^H W (in Gp), Xz = W (in Y)
+        cuDoubleComplex *Z = reinterpret_cast<cuDoubleComplex *>(Gp);
+        cuDoubleComplex *Xz = reinterpret_cast<cuDoubleComplex *>(Y);
+        const unsigned g1 = (unsigned)((nn + 255) / 256 < 4096 ? (nn + 255) / 256 : 4096);
+        k_to_interleaved<<<g1, 256, 0, s>>>(Y, Y + nn, (long long)nn, reinterpret_cast<double2 *>(Z));
+        k_to_interleaved<<<g1, 256, 0, s>>>(T, T + nn, (long long)nn, reinterpret_cast<double2 *>(Xz));
+        const cuDoubleComplex zone = make_cuDoubleComplex(1.0, 0.0);
+        if (cusolverDnZpotrf_bufferSize(hs, CUBLAS_FILL_MODE_UPPER, ni, Z, ni, &lw) != CUSOLVER_STATUS_SUCCESS ||
+            !wsp.reserve((size_t)(lw > 0 ? lw : 1) * 16) ||
+            cusolverDnZpotrf(hs, CUBLAS_FILL_MODE_UPPER, ni, Z, ni, reinterpret_cast<cuDoubleComplex *>(wsp.ptr), lw,
+                             info) != CUSOLVER_STATUS_SUCCESS ||
+            cublasZtrsm(h, CUBLAS_SIDE_RIGHT, CUBLAS_FILL_MODE_UPPER, CUBLAS_OP_N, CUBLAS_DIAG_NON_UNIT, ni, ni, &zone,
+                        Z, ni, Xz, ni) != CUBLAS_STATUS_SUCCESS)
+          return VJ_ERR_CUDA;
+        k_from_interleaved<<<g1, 256, 0, s>>>(reinterpret_cast<const double2 *>(Xz), (long long)nn, T, T + nn);
+      }
+      if (cudaMemcpyAsync(&hinfo, info, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+          cudaStreamSynchronize(s) != cudaSuccess)
+        return VJ_ERR_CUDA;
+      if (hinfo != 0)
+        return VJ_ERR_CUDA;  // W^H W not positive definite: W was not near unitary
+      // Q (in T) becomes the stage's transformation X
+      for (int pl = 0; pl < P; ++pl)
+        if (!copy2d(X + pl * nn, n, T + pl * nn, n, n, n, s))
+          return VJ_ERR_CUDA;
+      if (trace)
+        std::fprintf(stderr, "mixed SVD stage %u: Cholesky QR of W\n", stage);
     }
     // 4. V <- V W (V_0 = I, so the first stage that rotates sets V = W), G <- G W
     if (total32 == sw) {
@@ -797,6 +848,8 @@ static vj_fint mixed_dev(vj_fnat m_, vj_fnat n_, double *G, vj_fnat ldG, double 
                                                   cnt, s, &mu);
       if (hc < 0)
         return VJ_ERR_CUDA;
+      if (trace)
+        std::fprintf(stderr, "mixed SVD FP64 sweep %u: %lld rotations, max |cos| %.3e\n", sw64, hc, (double)mu);
       if (!hc)
         break;
       if (mu <= 1e-11f) {
@@ -845,7 +898,7 @@ static vj_fint mixed_dev(vj_fnat m_, vj_fnat n_, double *G, vj_fnat ldG, double 
     t0 = t1;
   }
   // 6. FP64 finishing sweeps (the reference's algorithm) with V preset
-  const vj_fint r = svd_dev_entry<double, CPLX>(m_, n_, G, ldG, Gi, ldGi, V, ldV, Vi, ldVi, eS, fS, js, stp, swp, 1, s);
+  const vj_fint r = svd_dev_entry<double, CPLX>(m_, n_, G, ldG, Gi, ldGi, V, ldV, Vi, ldVi, eS, fS, js, stp, swp, 2, s);
   const double msfin = std::chrono::duration<double, std::milli>(now() - t0).count();
   // FP32 launches: 3 per block step (n/b - 1 steps per block sweep), else 1 per pivot step
   const double steps32 = blk ? (double)total32 * (double)(n / (CPLX ? 32 : 64) - 1) * 3.0 : (double)total32 * stp;
