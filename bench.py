@@ -205,6 +205,37 @@ def device_info():
     return out
 
 
+def bench_fma_probe(args, vj):
+    """The FMA pipes in several shapes (vj_measure_fma_shape): throughput per active lane
+    with 32, 16 and 8 active lanes per warp, and the latency of one dependent chain. On
+    GB300 the FP64 pipe completes about one warp instruction per 77 cycles per
+    sub-partition whatever the number of active lanes, and a dependent DFMA takes about as
+    long: one warp of one serial chain per sub-partition keeps it busy, and lanes left
+    idle are lost."""
+    import ctypes as C
+    import torch
+    props = torch.cuda.get_device_properties(torch.cuda.current_device())
+    sms = int(props.multi_processor_count)
+    L = vj.lib()
+    rows = []
+    for f64 in (1, 0):
+        for wps, lanes, ch in ((4, 32, 8), (4, 16, 8), (4, 8, 8), (8, 32, 8), (8, 16, 8), (16, 16, 8),
+                               (64, 32, 8), (4, 32, 1), (8, 32, 1), (16, 32, 1)):
+            v = C.c_double(0.0)
+            r = L.vj_measure_fma_shape(C.c_int(f64), C.c_int(wps), C.c_int(lanes), C.c_int(ch), C.byref(v), None)
+            if r != 0:
+                continue
+            per_sm = v.value / sms
+            rows.append({"pipe": "fp64" if f64 else "fp32", "warps_per_sm": wps, "lanes": lanes, "chains": ch,
+                         "active_lane_fma_per_s": v.value, "per_sm_per_ns": round(per_sm * 1e-9, 3),
+                         "ns_per_dependent_fma": (round(1e9 * wps * lanes * sms / v.value, 3) if ch == 1
+                                                  else None)})
+    return {"metric": "FMA pipe probe (active-lane FMAs per second)", "value": rows[0]["active_lane_fma_per_s"],
+            "unit": "FMA/s", "n_gpus": 1, "steps": 3, "warmup": 1, "higher_is_better": True,
+            "data": "synthetic", "dtype": "f64+f32", "config": {"workload": "FMA chains on every SM, %d SMs" % sms},
+            "shapes": rows}
+
+
 def issue_bound(kind, sm_mhz, sms):
     """Element-rate bound of the FP64 2x2 from instruction issue: each SM issues at most one
     warp instruction per clock on each of its 4 sub-partitions (128 thread instructions per
@@ -1021,7 +1052,7 @@ def main():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="bjac2", choices=["bjac2", "svd1024", "zsvd", "zsvd_mixed", "dsvd_mixed",
+    ap.add_argument("--workload", default="bjac2", choices=["bjac2", "fma_probe", "svd1024", "zsvd", "zsvd_mixed", "dsvd_mixed",
                                                              "batch_d", "batch_s", "diff"])
     ap.add_argument("--diff-count", type=int, default=4096, help="matrices of the differentiable batch")
     ap.add_argument("--svd-m", type=int, default=0, help="rows of the SVD workloads (0: the workload's own)")
@@ -1054,6 +1085,8 @@ def main():
     import vecjac_gb300 as vj
     if args.workload == "bjac2":
         out = bench_bjac2(args, vj, dist, rank, world)
+    elif args.workload == "fma_probe":
+        out = bench_fma_probe(args, vj)
     elif args.workload == "svd1024":
         out = bench_svd(args, vj, dist, rank, world, "d", 1024, 1024)
     elif args.workload.startswith("batch_"):

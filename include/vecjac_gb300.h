@@ -111,8 +111,12 @@ vj_fint cvjsvd_(const vj_fnat m[1], const vj_fnat n[1], float Gr[], const vj_fna
                 float work[], unsigned iwork[]);
 
 /* Device-pointer SVD: all arrays (G, V, eS, fS, js) on the GPU; Gi/Vi NULL for real
- * data. preset != 0 means V holds a preset matrix. Synchronises `stream` once per
- * sweep (to test convergence). Returns like the host form. */
+ * data. preset != 0 means V holds a preset matrix. preset == 2 (FP64 only) also checks
+ * every pair of the first sweep at once before it runs (plain FP64 cosines with a rigorous
+ * error bound, and the reference's own arithmetic for the pairs without a certificate) and
+ * skips that sweep when it would transform or swap nothing: the results are those of
+ * preset == 1 bit for bit, sooner when the columns are orthogonal already. Synchronises
+ * `stream` once per sweep (to test convergence). Returns like the host form. */
 vj_fint vj_dvjsvd_dev(vj_fnat m, vj_fnat n, double *G, vj_fnat ldG, double *V, vj_fnat ldV, double *eS, double *fS,
                       const unsigned *js, unsigned stp, unsigned swp, int preset, void *stream);
 vj_fint vj_zvjsvd_dev(vj_fnat m, vj_fnat n, double *Gr, vj_fnat ldGr, double *Gi, vj_fnat ldGi, double *Vr,
@@ -286,6 +290,11 @@ const char *vj_version(void);
  * SM (CUDA-event timed, best of 3) to *ops_per_s; the roofline denominator of the kernels
  * bound by arithmetic. Returns 0 or a VJ_ERR_* code. No counterpart in the reference. */
 vj_fint vj_measure_fma_rate(int fp64, double *ops_per_s, void *stream);
+/* The same probe in a given shape: warps_per_sm warps on every SM (1 to 8, or a multiple
+ * of 8 up to 64), `lanes` active lanes per warp (the others exit first), `chains` FMA
+ * chains per lane (8 independent, or 1: a dependent chain, whose rate gives the latency).
+ * *ops_per_s: active-lane FMAs per second. No counterpart in the reference. */
+vj_fint vj_measure_fma_shape(int fp64, int warps_per_sm, int lanes, int chains, double *ops_per_s, void *stream);
 /* Width in bits of vj_fint / vj_fnat in this build: 64 (ILP64, the default, as the
  * reference's ABI=ilp64) or 32 (built with -DVJ_LP64, as the reference's ABI=lp64). */
 int vj_abi_int_bits(void);
