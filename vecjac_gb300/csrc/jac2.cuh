@@ -120,16 +120,15 @@ __device__ __forceinline__ angle<T> jac_angle(T a1, T a2, T ab, T &ad_out)
   return angle<T>{t1, s2, FAST ? sqrt_ge1(s2) : F::sqrt_(s2)};
 }
 
-template <typename T, int KIND>
-__device__ __forceinline__ unsigned rjac2(T a1, T a2, T ar, T &c, T &at, T &l1, T &l2)
+template <typename T, int KIND, bool GEN>
+__device__ __forceinline__ unsigned rjac2_body(T a1, T a2, T ar, T &c, T &at, T &l1, T &l2, int bmax)
 {
   using F = fp<T>;
   const T one = (T)1;
   T L1, L2, t1, s1, s2, as;
   bool fin = false;  // L1, L2 finite: compared on the integer pipes
-  const int b1 = bexp(a1), b2 = bexp(a2), br = bexp(ar);
-  const int bmax = max(max(b1, b2), br), bmin = min(min(b1, b2), br);
-  if (bmin > 0 && bmax <= F::EMAXB && bmax - bmin < fastc<T>::TOP) {
+  (void)bmax;
+  if constexpr (!GEN) {
     const int es = fastc<T>::TOP - bmax;
     ar = addexp(ar, es);
     a1 = addexp(a1, es);
@@ -194,16 +193,45 @@ __device__ __forceinline__ unsigned rjac2(T a1, T a2, T ar, T &c, T &at, T &l1, 
   return (fin ? lt_fin(L1, L2) : (L1 < L2)) ? 1u : 0u;
 }
 
+
+// the general finite path and the inf/NaN transcription, out of line: their code is not
+// laid out (or predicated) into the lanes of the fast path; results by value, so that the
+// caller's outputs never have their address taken (they stay in registers)
+template <typename T> struct r2out {
+  T c, at, l1, l2;
+  unsigned bit;
+};
+template <typename T, int KIND> __device__ __noinline__ r2out<T> rjac2_gen(T a1, T a2, T ar)
+{
+  r2out<T> r;
+  r.bit = rjac2_body<T, KIND, true>(a1, a2, ar, r.c, r.at, r.l1, r.l2, 0);
+  return r;
+}
+
 template <typename T, int KIND>
-__device__ __forceinline__ unsigned cjac2(T a1, T a2, T ar, T ai, T &c, T &cat, T &sat, T &l1, T &l2)
+__device__ __forceinline__ unsigned rjac2(T a1, T a2, T ar, T &c, T &at, T &l1, T &l2)
+{
+  const int b1 = bexp(a1), b2 = bexp(a2), br = bexp(ar);
+  const int bmax = max(max(b1, b2), br), bmin = min(min(b1, b2), br);
+  if (bmin > 0 && bmax <= fp<T>::EMAXB && bmax - bmin < fastc<T>::TOP)
+    return rjac2_body<T, KIND, false>(a1, a2, ar, c, at, l1, l2, bmax);
+  const r2out<T> r = rjac2_gen<T, KIND>(a1, a2, ar);
+  c = r.c;
+  at = r.at;
+  l1 = r.l1;
+  l2 = r.l2;
+  return r.bit;
+}
+
+template <typename T, int KIND, bool GEN>
+__device__ __forceinline__ unsigned cjac2_body(T a1, T a2, T ar, T ai, T &c, T &cat, T &sat, T &l1, T &l2, int bmax)
 {
   using F = fp<T>;
   const T one = (T)1, zero = (T)0;
   T L1, L2, t1, s1, s2, ar_, ai_;
   bool fin = false;
-  const int b1 = bexp(a1), b2 = bexp(a2), br = bexp(ar), bi = bexp(ai);
-  const int bmax = max(max(b1, b2), max(br, bi)), bmin = min(min(b1, b2), min(br, bi));
-  if (bmin > 0 && bmax <= F::EMAXB && bmax - bmin < fastc<T>::TOP) {
+  (void)bmax;
+  if constexpr (!GEN) {
     const int es = fastc<T>::TOP - bmax;
     ar = addexp(ar, es);
     ai = addexp(ai, es);
@@ -303,6 +331,33 @@ __device__ __forceinline__ unsigned cjac2(T a1, T a2, T ar, T ai, T &c, T &cat, 
   cat = ar_;
   sat = ai_;
   return (fin ? lt_fin(L1, L2) : (L1 < L2)) ? 1u : 0u;
+}
+
+template <typename T> struct c2out {
+  T c, cat, sat, l1, l2;
+  unsigned bit;
+};
+template <typename T, int KIND> __device__ __noinline__ c2out<T> cjac2_gen(T a1, T a2, T ar, T ai)
+{
+  c2out<T> r;
+  r.bit = cjac2_body<T, KIND, true>(a1, a2, ar, ai, r.c, r.cat, r.sat, r.l1, r.l2, 0);
+  return r;
+}
+
+template <typename T, int KIND>
+__device__ __forceinline__ unsigned cjac2(T a1, T a2, T ar, T ai, T &c, T &cat, T &sat, T &l1, T &l2)
+{
+  const int b1 = bexp(a1), b2 = bexp(a2), br = bexp(ar), bi = bexp(ai);
+  const int bmax = max(max(b1, b2), max(br, bi)), bmin = min(min(b1, b2), min(br, bi));
+  if (bmin > 0 && bmax <= fp<T>::EMAXB && bmax - bmin < fastc<T>::TOP)
+    return cjac2_body<T, KIND, false>(a1, a2, ar, ai, c, cat, sat, l1, l2, bmax);
+  const c2out<T> r = cjac2_gen<T, KIND>(a1, a2, ar, ai);
+  c = r.c;
+  cat = r.cat;
+  sat = r.sat;
+  l1 = r.l1;
+  l2 = r.l2;
+  return r.bit;
 }
 
 }  // namespace vj
