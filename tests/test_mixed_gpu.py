@@ -122,11 +122,17 @@ def test_mixed_relative_accuracy_vs_plain(vj, kind, m, n):
     assert rel <= 64 * n * EPS, rel
 
 
+# the FP32 stages take block sweeps on the tensor cores by default from 16 block pairs per
+# step (n >= 2048 real, 1024 complex); VJ_BLOCK=1 forces them at these sizes, VJ_BLOCK=0
+# forces the column-pair sweeps
+@pytest.mark.parametrize("blk", ["0", "1"])
 @pytest.mark.parametrize("kind,m,n", [("d", 1024, 512), ("z", 512, 256)])
-def test_mixed_large(vj, kind, m, n):
+def test_mixed_large(vj, kind, m, n, blk, monkeypatch):
     from vecjac_gb300 import workloads as W
+    monkeypatch.setenv("VJ_BLOCK", blk)
     A, s = W.svd_matrix(m, n, seed=11, complex_=(kind == "z"))
     r, r32, U, V, sig = run_mixed(vj, kind, A)
+    assert vj.last_mixed_phases()["fp32_block_sweeps"] == (blk == "1")
     assert r >= 0 and r32 > 0
     # the reference's FP64 phase starts from columns orthogonal to twice its tolerance: it
     # confirms convergence within a few sweeps
@@ -177,10 +183,12 @@ def test_mixed_stages(vj, stages):
     check_props(A, G.cpu().numpy().T, V.cpu().numpy().T, sig)
 
 
-def test_mixed_graded_and_rank_deficient(vj, rst):
+@pytest.mark.parametrize("blk", ["0", "1"])
+def test_mixed_graded_and_rank_deficient(vj, rst, blk, monkeypatch):
     # column-graded (one-sided Jacobi's high relative accuracy must survive the FP32
     # stages) and rank-deficient (zero columns) matrices: singular values relative to the
-    # oracle's FP64 SVD of the same matrix
+    # oracle's FP64 SVD of the same matrix, with the column-pair and the block FP32 sweeps
+    monkeypatch.setenv("VJ_BLOCK", blk)
     rng = np.random.default_rng(21)
     m, n = 256, 128
     B = rng.standard_normal((m, n))

@@ -617,12 +617,16 @@ static vj_fint mixed_dev(vj_fnat m_, vj_fnat n_, double *G, vj_fnat ldG, double 
   // (3 n n doubles)
   const size_t gpn = ((size_t)P * mn > 3 * nn) ? (size_t)P * mn : 3 * nn;
   const size_t f64b = (gpn + P * 3 * nn) * 8;
-  // FP32 stages: block sweeps on the tensor cores where the shape has whole blocks
-  // (VJ_BLOCK=0 in the environment selects the column-pair sweeps), with the terms of the
-  // split products (VJ_BLOCK_TERMS, 6 or 3) and inner Jacobi sweeps per block pair
-  // (VJ_BLOCK_INNER)
+  // FP32 stages: block sweeps on the tensor cores where the shape has whole blocks and at
+  // least 16 block pairs per step (fewer pairs leave most SMs idle in the pair
+  // eigenproblems: at 1024 x 1024 real the column-pair sweeps take 109 ms against 176 ms,
+  // at 4096 x 2048 real the block sweeps 495 ms against 685 ms). VJ_BLOCK=0 in the
+  // environment selects the column-pair sweeps, VJ_BLOCK=1 the block sweeps wherever the
+  // shape allows; VJ_BLOCK_TERMS (6 or 3) the terms of the split products, VJ_BLOCK_INNER
+  // the inner Jacobi sweeps per block pair.
   const char *eb = getenv("VJ_BLOCK");
-  const bool blk = !(eb && *eb == '0') && block_sweeps_apply(CPLX, m, n, m);
+  const bool blk = !(eb && *eb == '0') && block_sweeps_apply(CPLX, m, n, m) &&
+                   ((eb && *eb == '1') || n >= (CPLX ? 1024 : 2048));
   const char *et = getenv("VJ_BLOCK_TERMS");
   const int terms = (et && atoi(et) == 3) ? 3 : 6;
   const char *ei = getenv("VJ_BLOCK_INNER");
