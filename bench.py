@@ -174,13 +174,13 @@ class Batch:
 
 
 # thread instructions per element of k_bjac2 (ncu smsp__inst_executed.sum x 32 / elements,
-# 2^24 real and 2^23 complex launches; the profile summary k_bjac2_fp64_pipe_2e24)
-BJAC2_INST_PER_ELEM = {"d": 1277.0, "z": 1973.0}
+# issue slots: 2^24 real and 2^23 complex launches; the profile summary k_bjac2_fp64_pipe_2e24)
+BJAC2_INST_PER_ELEM = {"d": 1278.0, "z": 1979.0}
 # thread instructions per element that execute on the FP64 pipe (ncu
 # smsp__inst_executed_pipe_fp64.sum x 32 / elements; profile summary k_bjac2_fp64_pipe_2e24)
 BJAC2_FP64_PIPE_PER_ELEM = {"d": 25.0, "z": 50.0}
 # DRAM bytes (read + write) of one 2^24-element real FP64 launch, from the same capture
-BJAC2_D_DRAM_2E24 = 402.791680e6 + 487.371776e6
+BJAC2_D_DRAM_2E24 = 402.788096e6 + 495.165696e6
 # the reference's own AVX-512 dbjac2_/zbjac2_ (src/dbjac2.c, src/zbjac2.c, compiled from its
 # sources) on an x86-64 host with AVX-512, 8 threads, 2^24 elements of the same distribution,
 # best of 5; it cannot be built on this Arm host (src/vec.h:11), so the figure is not measured
