@@ -853,7 +853,8 @@ static vj_fint mixed_dev(vj_fnat m_, vj_fnat n_, double *G, vj_fnat ldG, double 
       if (hc < 0)
         return VJ_ERR_CUDA;
       if (trace)
-        std::fprintf(stderr, "mixed SVD FP64 sweep %u: %lld rotations, max |cos| %.3e\n", sw64, hc, (double)mu);
+        std::fprintf(stderr, "mixed SVD FP64 sweep %u: %lld rotations, max |cos| %.3e, %.1f ms since the phase began\n",
+                     sw64, hc, (double)mu, std::chrono::duration<double, std::milli>(now() - t0).count());
       if (!hc)
         break;
       if (mu <= 1e-11f) {
