@@ -956,8 +956,8 @@ def bench_batch(args, vj, dist, rank, world, kind):
     from vecjac_gb300 import batch as B
     mats = gen_uneven(args.batch_count, 77 + rank, kind)
     b = B.Batch(mats, kind)
-    blk = B.autotune(b, args.pivot)
-    g = B.capture(b, args.pivot, block=blk)
+    blk, occ = B.autotune(b, args.pivot)
+    g = B.capture(b, args.pivot, block=blk, occupancy=occ)
     for _ in range(max(0, args.warmup - 1)):
         g.replay()
     torch.cuda.synchronize()
@@ -998,8 +998,9 @@ def bench_batch(args, vj, dist, rank, world, kind):
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 2), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64" if kind == "d" else "f32",
             "data": "synthetic (m~U[16,512], n~U[8,m], Q1 diag(sigma) Q2^T, sigma=10^U(-4,0))",
-            "config": {"workload": "%d matrices in one persistent launch (CUDA graph), pivot id %d, block %d"
-                       % (len(mats), args.pivot, blk), "errors": int((info < 0).sum()),
+            "config": {"workload": "%d matrices in one persistent launch (CUDA graph), pivot id %d, block %d, "
+                       "register bound for %d CTAs of 256 threads per SM (autotuned)"
+                       % (len(mats), args.pivot, blk, occ), "errors": int((info < 0).sum()),
                        "mean_sweeps": float(info[info >= 0].mean())},
             "flops_per_s": flops / (ms * 1e-3),
             "one_launch_per_matrix_s_estimate": round(per_launch, 2),

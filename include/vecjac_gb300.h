@@ -216,6 +216,18 @@ vj_fint vj_dvjsvd_batch_dev(vj_fint count, const long long *m, const long long *
 vj_fint vj_svjsvd_batch_dev(vj_fint count, const long long *m, const long long *n, float *G, const long long *offG,
                             float *V, const long long *offV, float *eS, float *fS, const long long *offS,
                             const int *order, long strategy, unsigned swp, long long *info, int block, void *stream);
+/* The same with the kernel's register bound chosen: `occupancy` resident CTAs of 256
+ * threads per SM (2 to 6; fewer registers per thread, more CTAs, some spills above 4 for
+ * FP32 and 3 for FP64; 0 = the default, 4 for FP32 and 2 for FP64). The package's
+ * autotuner searches (block, occupancy) per batch. */
+vj_fint vj_dvjsvd_batch_tuned_dev(vj_fint count, const long long *m, const long long *n, double *G,
+                                  const long long *offG, double *V, const long long *offV, double *eS, double *fS,
+                                  const long long *offS, const int *order, long strategy, unsigned swp,
+                                  long long *info, int block, int occupancy, void *stream);
+vj_fint vj_svjsvd_batch_tuned_dev(vj_fint count, const long long *m, const long long *n, float *G,
+                                  const long long *offG, float *V, const long long *offV, float *eS, float *fS,
+                                  const long long *offS, const int *order, long strategy, unsigned swp,
+                                  long long *info, int block, int occupancy, void *stream);
 
 /* Allocation-free FP64 SVD. No counterpart in the reference. For callers that must not
  * allocate GPU memory while they run -- for example an application whose memory pool owns

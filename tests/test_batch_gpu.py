@@ -66,24 +66,29 @@ def test_batch_vs_oracle(env, kind, strategy):
             assert same(x, y), A.shape
 
 
-def test_batch_autotune_and_graph(env):
+@pytest.mark.parametrize("kind", ["d", "s"])
+def test_batch_autotune_and_graph(env, kind):
     import torch
     from vecjac_gb300 import batch as B
     mats = uneven(64, seed=11, mmax=160)
-    b = B.Batch(mats, "d")
-    blk = B.autotune(b, 4, sample=32)
-    assert blk in (64, 128, 256)
-    b.run(4, block=blk)
+    if kind == "s":
+        mats = [A.astype(np.float32) for A in mats]
+    b = B.Batch(mats, kind)
+    blk, occ = B.autotune(b, 4, sample=32)
+    assert blk in (64, 128, 256) and occ in (0, 2, 3, 4, 5)
+    b.run(4, block=blk, occupancy=occ)
     torch.cuda.synchronize()
     first = b.results()
-    ref = B.Batch(mats, "d")
-    ref.run(4, block=64 if blk != 64 else 128)
-    torch.cuda.synchronize()
-    for x, y in zip(first, ref.results()):
-        assert x[0] == y[0]
-        for u, v in zip(x[1:], y[1:]):
-            assert same(u, v)
-    g = B.capture(b, 4, block=blk)
+    # every launch configuration gives the same bits (each matrix's arithmetic is fixed)
+    for rb, ro in ((64 if blk != 64 else 128, 0), (256, 3), (128, 4), (64, 6)):
+        ref = B.Batch(mats, kind)
+        ref.run(4, block=rb, occupancy=ro)
+        torch.cuda.synchronize()
+        for x, y in zip(first, ref.results()):
+            assert x[0] == y[0]
+            for u, v in zip(x[1:], y[1:]):
+                assert same(u, v)
+    g = B.capture(b, 4, block=blk, occupancy=occ)
     g.replay()
     torch.cuda.synchronize()
     for x, y in zip(first, b.results()):
@@ -106,8 +111,8 @@ def test_full_size_fp32_batch(env):
     rng = np.random.default_rng(32)
     mats = [rng.standard_normal((int(a), int(b))).astype(np.float32) for a, b in zip(m, n)]
     b = B.Batch(mats, "s")
-    blk = B.autotune(b, 4)
-    b.run(4, block=blk)
+    blk, occ = B.autotune(b, 4)
+    b.run(4, block=blk, occupancy=occ)
     torch.cuda.synchronize()
     info = b.info.cpu().numpy()
     assert np.all(info > 0) and np.all(info < 999), (info.min(), info.max())

@@ -44,7 +44,8 @@ def lib():
                      "svjsvd_", "cvjsvd_", "vj_dvjsvd_dev", "vj_zvjsvd_dev", "vj_svjsvd_dev", "vj_cvjsvd_dev",
                      "vj_pjs_dev", "vj_dvjsvd_mixed_dev", "vj_zvjsvd_mixed_dev",
                      "vj_ssvd_adjoint_batch_dev", "vj_dsvd_adjoint_batch_dev", "vj_dvjsvd_batch_dev",
-                     "vj_svjsvd_batch_dev", "vj_last_mixed_phases", "zsplit_", "zmerge_", "csplit_", "cmerge_",
+                     "vj_svjsvd_batch_dev", "vj_dvjsvd_batch_tuned_dev", "vj_svjsvd_batch_tuned_dev",
+                     "vj_last_mixed_phases", "zsplit_", "zmerge_", "csplit_", "cmerge_",
                      "vj_zsplit_dev", "vj_zmerge_dev", "vj_csplit_dev", "vj_cmerge_dev"):
             if hasattr(_LIB, name):
                 getattr(_LIB, name).restype = _ll

@@ -1,5 +1,6 @@
 """Batched SVD of many uneven real matrices in one persistent launch, with an autotuner
-for the CTA size and CUDA-graph capture of the launch.
+for the launch configuration (CTA size and the kernel's register bound, i.e. resident
+CTAs per SM) and CUDA-graph capture of the launch.
 
 `svd_batch(mats, kind)` pads every matrix to the reference's shape rules (zero rows and
 columns; dvjsvd_/svjsvd_ need m % 8 / % 16 and (n/2) % 8 / % 16), packs all of them into
@@ -58,16 +59,18 @@ class Batch:
         self.doffG, self.doffV, self.doffS = d(offG), d(offV), d(offS)
         self.dorder = d(self.order_np)
 
-    def run(self, strategy=4, swp=999, block=128, stream=None, reset=True):
-        """Enqueue the batch (asynchronous). reset=True first restores G from the packed input."""
+    def run(self, strategy=4, swp=999, block=128, stream=None, reset=True, occupancy=0):
+        """Enqueue the batch (asynchronous). reset=True first restores G from the packed input.
+        block: threads per CTA (64, 128, 256); occupancy: the kernel's register bound in
+        resident 256-thread CTAs per SM (2..6, 0 = the library's default)."""
         if reset:
             self.G.copy_(self.G0)
-        f = getattr(api.lib(), "vj_%svjsvd_batch_dev" % self.kind)
+        f = getattr(api.lib(), "vj_%svjsvd_batch_tuned_dev" % self.kind)
         f.restype = C.c_longlong
         p = lambda t: C.c_void_p(t.data_ptr())
         r = f(C.c_longlong(self.count), p(self.dm), p(self.dn), p(self.G), p(self.doffG), p(self.V), p(self.doffV),
               p(self.eS), p(self.fS), p(self.doffS), p(self.dorder), C.c_long(strategy), C.c_uint(swp), p(self.info),
-              C.c_int(block), C.c_void_p(stream) if stream else None)
+              C.c_int(block), C.c_int(occupancy), C.c_void_p(stream) if stream else None)
         if r != 0:
             raise RuntimeError("batched SVD launch failed: %d" % r)
 
@@ -92,16 +95,24 @@ class Batch:
         return float(np.sum(np.asarray(sweeps, np.float64) * n * (n - 1) / 2 * (12 * m + 6 * n)))
 
 
-def autotune(batch, strategy=4, candidates=(64, 128, 256), sample=None):
-    """Pick the CTA size for this batch's size mix: time each candidate on a random sample
-    of its matrices (CUDA events, after one warm-up) and return the fastest. The choice is
-    cached per (precision, coarse size histogram)."""
+def autotune(batch, strategy=4, blocks=(64, 128, 256), occupancies=None, sample=None):
+    """Pick the launch configuration for this batch's size mix: the CTA size (threads per
+    matrix) and the kernel's register bound (resident CTAs per SM), by timing candidates
+    on a random sample of the batch's matrices (CUDA events, after one warm-up): first the
+    CTA sizes at the default bound, then the bounds at the best CTA size. The sample is
+    large enough to fill the GPU several times (2432 matrices by default), so that it
+    measures throughput rather than its largest matrix. Returns (block, occupancy); cached
+    per (precision, coarse size histogram)."""
     import torch
-    key = (batch.kind, tuple(np.histogram(batch.n, bins=[0, 64, 128, 256, 513])[0] > 0))
+    if occupancies is None:
+        occupancies = (3, 4, 5) if batch.kind == "s" else (2, 3, 4)
+    key = (batch.kind, tuple(np.histogram(batch.n, bins=[0, 32, 64, 128, 256, 513])[0] > 0), tuple(blocks),
+           tuple(occupancies))
     if key in _TUNED:
         return _TUNED[key]
     rng = np.random.default_rng(0)
-    idx = rng.choice(batch.count, min(batch.count, sample or 512), replace=False)
+    size = min(batch.count, sample or 2432)
+    idx = rng.choice(batch.count, size, replace=False)
     mats = []
     G = batch.G0.cpu().numpy()
     for b in idx:
@@ -109,34 +120,40 @@ def autotune(batch, strategy=4, candidates=(64, 128, 256), sample=None):
         o = int(batch.offG[b])
         mats.append(G[o:o + mm * nn].reshape((mm, nn), order="F"))
     sub = Batch(mats, batch.kind)
-    best, best_t = candidates[0], None
-    for blk in candidates:
-        sub.run(strategy, block=blk)
+
+    def timed(blk, occ):
+        sub.run(strategy, block=blk, occupancy=occ)
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record()
-        sub.run(strategy, block=blk)
+        sub.run(strategy, block=blk, occupancy=occ)
         e1.record()
         torch.cuda.synchronize()
-        t = e0.elapsed_time(e1)
-        if best_t is None or t < best_t:
-            best, best_t = blk, t
+        return e0.elapsed_time(e1)
+
+    times = {}
+    for blk in blocks:
+        times[(blk, 0)] = timed(blk, 0)
+    best_blk = min(blocks, key=lambda b_: times[(b_, 0)])
+    for occ in occupancies:
+        times[(best_blk, occ)] = timed(best_blk, occ)
+    best = min(times, key=times.get)
     _TUNED[key] = best
     return best
 
 
-def capture(batch, strategy=4, swp=999, block=128):
+def capture(batch, strategy=4, swp=999, block=128, occupancy=0):
     """Capture restore-and-run of the batch into a CUDA graph; returns the graph (replay())."""
     import torch
     s = torch.cuda.Stream()
     s.wait_stream(torch.cuda.current_stream())
     with torch.cuda.stream(s):
-        batch.run(strategy, swp, block, stream=s.cuda_stream)   # warm-up outside capture
+        batch.run(strategy, swp, block, stream=s.cuda_stream, occupancy=occupancy)   # warm-up outside capture
     torch.cuda.current_stream().wait_stream(s)
     torch.cuda.synchronize()
     g = torch.cuda.CUDAGraph()
     with torch.cuda.graph(g):
-        batch.run(strategy, swp, block, stream=torch.cuda.current_stream().cuda_stream)
+        batch.run(strategy, swp, block, stream=torch.cuda.current_stream().cuda_stream, occupancy=occupancy)
     return g
 
 
@@ -144,7 +161,7 @@ def svd_batch(mats, kind="d", strategy=4, swp=999, block=None):
     """SVD of every matrix in `mats` (real numpy arrays of any m >= n <= 512) in one launch."""
     import torch
     b = Batch(mats, kind)
-    blk = block or autotune(b, strategy)
-    b.run(strategy, swp, blk)
+    blk, occ = (block, 0) if block else autotune(b, strategy)
+    b.run(strategy, swp, blk, occupancy=occ)
     torch.cuda.synchronize()
     return b.results()

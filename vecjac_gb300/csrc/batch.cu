@@ -17,11 +17,13 @@
 
 namespace vj {
 
-// FP32: 3 CTAs of 256 threads per SM (80 registers, no spills; faster than 116 registers
-// at 2 CTAs per SM). FP64: 2 CTAs per SM (118 registers; a bound of 3 spills, none lets
-// the compiler take 162).
-template <typename T>
-__global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k_batch(BatchArgs<T> a)
+// MINB: the register bound for MINB resident CTAs of 256 threads per SM (more, smaller
+// CTAs when the caller launches fewer threads per CTA). The best bound depends on the
+// batch (the autotuner of vecjac_gb300/batch.py searches it with the CTA size): on the
+// 20,000-matrix FP32 batch 4 CTAs of 256 threads (64 registers) gave 1434 matrices/s,
+// 3 (80 registers) 1221, 2 (128) 937.
+template <typename T, int MINB>
+__global__ void __launch_bounds__(256, MINB) k_batch(BatchArgs<T> a)
 {
   __shared__ BatchShared<T> sh;
   __shared__ long long s_b;
@@ -42,10 +44,16 @@ __global__ void __launch_bounds__(256, sizeof(T) == 4 ? 3 : 2) k_batch(BatchArgs
   }
 }
 
+// default register bound: FP32 4 CTAs of 256 threads per SM, FP64 2 (118 registers; a
+// bound of 3 spills)
+template <typename T> constexpr int batch_occ_default() { return sizeof(T) == 4 ? 4 : 2; }
+
+template <typename T, int MINB> static void *batch_kernel() { return reinterpret_cast<void *>(k_batch<T, MINB>); }
+
 template <typename T>
 static vj_fint batch_dev(vj_fint count, const long long *m, const long long *n, T *G, const long long *offG, T *V,
                          const long long *offV, T *eS, T *fS, const long long *offS, const int *order,
-                         long strategy, unsigned swp, long long *info, int block, void *stream)
+                         long strategy, unsigned swp, long long *info, int block, int occ, void *stream)
 {
   if (count < 0 || (strategy != 2l && strategy != 4l))
     return VJ_ERR_ARG;
@@ -55,6 +63,8 @@ static vj_fint batch_dev(vj_fint count, const long long *m, const long long *n, 
     return VJ_ERR_NO_GPU;
   if (block != 64 && block != 128 && block != 256)
     block = 128;
+  if (occ < 2 || occ > 6)
+    occ = batch_occ_default<T>();
   cudaStream_t s = (cudaStream_t)stream;
   unsigned *queue = host::batch_queue();
   if (!queue)
@@ -67,13 +77,20 @@ static vj_fint batch_dev(vj_fint count, const long long *m, const long long *n, 
   a.G = G; a.V = V; a.eS = eS; a.fS = fS; a.info = info; a.queue = queue;
   a.strategy = (int)strategy;
   a.swp = swp;
+  void *k = (occ == 2)   ? batch_kernel<T, 2>()
+            : (occ == 3) ? batch_kernel<T, 3>()
+            : (occ == 4) ? batch_kernel<T, 4>()
+            : (occ == 5) ? batch_kernel<T, 5>()
+                         : batch_kernel<T, 6>();
   int per_sm = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch<T>, block, 0) != cudaSuccess || per_sm < 1)
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k, block, 0) != cudaSuccess || per_sm < 1)
     per_sm = 1;
   long long grid = (long long)host::sm_count() * per_sm;
   if (grid > count)
     grid = count;
-  k_batch<T><<<(unsigned)grid, block, 0, s>>>(a);
+  void *args[] = {&a};
+  if (cudaLaunchKernel(k, dim3((unsigned)grid), dim3((unsigned)block), args, 0, s) != cudaSuccess)
+    return VJ_ERR_CUDA;
   return (cudaGetLastError() == cudaSuccess) ? 0 : VJ_ERR_CUDA;
 }
 
@@ -85,7 +102,7 @@ vj_fint vj_dvjsvd_batch_dev(vj_fint count, const long long *m, const long long *
                             double *V, const long long *offV, double *eS, double *fS, const long long *offS,
                             const int *order, long strategy, unsigned swp, long long *info, int block, void *stream)
 {
-  return vj::batch_dev<double>(count, m, n, G, offG, V, offV, eS, fS, offS, order, strategy, swp, info, block,
+  return vj::batch_dev<double>(count, m, n, G, offG, V, offV, eS, fS, offS, order, strategy, swp, info, block, 0,
                                stream);
 }
 
@@ -93,8 +110,26 @@ vj_fint vj_svjsvd_batch_dev(vj_fint count, const long long *m, const long long *
                             float *V, const long long *offV, float *eS, float *fS, const long long *offS,
                             const int *order, long strategy, unsigned swp, long long *info, int block, void *stream)
 {
-  return vj::batch_dev<float>(count, m, n, G, offG, V, offV, eS, fS, offS, order, strategy, swp, info, block,
+  return vj::batch_dev<float>(count, m, n, G, offG, V, offV, eS, fS, offS, order, strategy, swp, info, block, 0,
                               stream);
+}
+
+vj_fint vj_dvjsvd_batch_tuned_dev(vj_fint count, const long long *m, const long long *n, double *G,
+                                  const long long *offG, double *V, const long long *offV, double *eS, double *fS,
+                                  const long long *offS, const int *order, long strategy, unsigned swp,
+                                  long long *info, int block, int occupancy, void *stream)
+{
+  return vj::batch_dev<double>(count, m, n, G, offG, V, offV, eS, fS, offS, order, strategy, swp, info, block,
+                               occupancy, stream);
+}
+
+vj_fint vj_svjsvd_batch_tuned_dev(vj_fint count, const long long *m, const long long *n, float *G,
+                                  const long long *offG, float *V, const long long *offV, float *eS, float *fS,
+                                  const long long *offS, const int *order, long strategy, unsigned swp,
+                                  long long *info, int block, int occupancy, void *stream)
+{
+  return vj::batch_dev<float>(count, m, n, G, offG, V, offV, eS, fS, offS, order, strategy, swp, info, block,
+                              occupancy, stream);
 }
 
 }  // extern "C"

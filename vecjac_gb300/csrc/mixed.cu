@@ -687,9 +687,18 @@ static vj_fint mixed_dev(vj_fnat m_, vj_fnat n_, double *G, vj_fnat ldG, double 
       k_eye_p<float><<<grid2(n, n), 256, 0, s>>>(W32 + nn, n, n, 0);
     // 2. FP32 sweeps until a sweep rotates nothing
     // (a sweep whose rotated pairs were all within 4x the tolerance ends the stage without
-    // a confirming sweep: the stage is a preconditioner, the next one finishes the work)
+    // a confirming sweep: the stage is a preconditioner, the next one finishes the work;
+    // a stage that another one follows also ends once a sweep rotates fewer than half of
+    // all possible pairs: the first stage works on A rounded to FP32, where the directions
+    // of singular values below FP32 resolution are noise that the next stage resolves
+    // properly, and its long tail of sweeps over them costs more than the next stage's
+    // extra sweeps -- at 4096 x 2048 complex, 31 + 16 FP32 sweeps in 2.58 s against
+    // 18 + 18 in 2.47 s)
     unsigned sw = 0;
     const float stop = 4.f * tol;
+    const long long nbk = n / (CPLX ? 32 : 64), hw = CPLX ? 32 : 64;
+    const double every = blk ? (double)(nbk - 1) * (double)(nbk / 2) * inner * (double)(2 * hw - 1) * (double)hw
+                             : (double)stp * (double)(n / 2);
     for (; sw < maxsw; ++sw) {
       float mu = 0.f;
       const long long hc =
@@ -704,7 +713,7 @@ static vj_fint mixed_dev(vj_fnat m_, vj_fnat n_, double *G, vj_fnat ldG, double 
                      (double)mu);
       if (!hc)
         break;
-      if (mu < stop) {
+      if (mu < stop || (stage + 1 < stages && 2.0 * (double)hc < every)) {
         ++sw;
         break;
       }
