@@ -734,9 +734,11 @@ static vj_fint mixed_dev(vj_fnat m_, vj_fnat n_, double *G, vj_fnat ldG, double 
     //    half the cost of the two Newton-Schulz steps that the same accuracy needs. W's
     //    columns go in ascending order of the norms of the FP32 G's columns first: R^-1 is
     //    upper triangular, so the correction mixes into each column of G Q only columns of
-    //    smaller norm (the polar factor would also spread large columns into small ones).
-    //    (The first FP64 sweep below still meets scaled inner products of up to ~1e-2: the
-    //    FP32 rounding of W's own entries couples large columns of G into small ones.)
+    //    smaller norm. (The first FP64 sweep below still meets scaled inner products of up
+    //    to ~5e-3 at 4096 x 2048 complex with sigma down to 1e-8, and 2e-5 at 4096 x 2048 real
+    //    with sigma down to 1e-6: the FP32 rounding of W's own entries couples large columns
+    //    of G into small ones, which no orthonormalisation of W undoes; the descending order
+    //    measured worse, 1e-2 and 1.5e-4, and one FP64 sweep more at 4096 x 2048 complex.)
     for (int pl = 0; pl < P; ++pl)
       k_to_f64<<<(unsigned)((nn + 255) / 256 < 4096 ? (nn + 255) / 256 : 4096), 256, 0, s>>>(
           W32 + pl * nn, (long long)nn, X + pl * nn);
