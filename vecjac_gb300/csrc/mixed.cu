@@ -574,6 +574,30 @@ static bool zgemm3m(cublasHandle_t h, bool cplx, int m, int n, int k, Planes A, 
   return cudaGetLastError() == cudaSuccess;
 }
 
+// C = A B for complex split planes by 3M as above, with A's imaginary plane overwritten by
+// Ar + Ai (A is a scratch copy) so that the temporaries are only P2 (m n) and Br + Bi (k n):
+// tmp holds m n + k n doubles. For G := G Q (m x n by n x n): three products instead of four.
+static bool zgemm3m_overwrite(cublasHandle_t h, int m, int n, int k, Planes A, Planes B, Planes Cm, double *tmp,
+                              cudaStream_t s)
+{
+  const double one = 1.0, zero = 0.0;
+  double *P2 = tmp, *Bs = tmp + (size_t)m * n;
+  bool ok = cublasDgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, m, n, k, &one, A.im, A.ldi, B.im, B.ldi, &zero, P2, m) ==
+                CUBLAS_STATUS_SUCCESS &&
+            cublasDgeam(h, CUBLAS_OP_N, CUBLAS_OP_N, k, n, &one, B.re, B.ldr, &one, B.im, B.ldi, Bs, k) ==
+                CUBLAS_STATUS_SUCCESS &&
+            cublasDgeam(h, CUBLAS_OP_N, CUBLAS_OP_N, m, k, &one, A.re, A.ldr, &one, A.im, A.ldi, A.im, A.ldi) ==
+                CUBLAS_STATUS_SUCCESS &&
+            cublasDgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, m, n, k, &one, A.re, A.ldr, B.re, B.ldr, &zero, Cm.re, Cm.ldr) ==
+                CUBLAS_STATUS_SUCCESS &&
+            cublasDgemm(h, CUBLAS_OP_N, CUBLAS_OP_N, m, n, k, &one, A.im, A.ldi, Bs, k, &zero, Cm.im, Cm.ldi) ==
+                CUBLAS_STATUS_SUCCESS;
+  if (!ok)
+    return false;
+  k_combine3m<<<grid2(m, n), 256, 0, s>>>(m, n, Cm.re, Cm.ldr, Cm.im, Cm.ldi, P2);
+  return cudaGetLastError() == cudaSuccess;
+}
+
 static bool copy2d(double *dst, long long ldd, const double *src, long long lds, long long rows, long long cols,
                    cudaStream_t s)
 {
@@ -824,7 +848,13 @@ static vj_fint mixed_dev(vj_fnat m_, vj_fnat n_, double *G, vj_fnat ldG, double 
     }
     if (!copy2d(Gp, m, G, ldG, m, n, s) || (CPLX && !copy2d(Gp + mn, m, Gi, ldGi, m, n, s)))
       return VJ_ERR_CUDA;
-    if (!zgemm(h, CPLX, false, mi, ni, ni, Gpp, Xp, Gpl))
+    // complex G := G Q by 3M when its temporaries fit in the free T and Y scratch
+    // (m n + n n <= 4 n n doubles), else by four real products
+    if (CPLX && m <= 3 * n) {
+      if (!zgemm3m_overwrite(h, mi, ni, ni, Gpp, Xp, Gpl, T, s))
+        return VJ_ERR_CUDA;
+    }
+    else if (!zgemm(h, CPLX, false, mi, ni, ni, Gpp, Xp, Gpl))
       return VJ_ERR_CUDA;
     {
       if (cudaStreamSynchronize(s) != cudaSuccess)
