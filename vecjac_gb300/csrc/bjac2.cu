@@ -8,6 +8,7 @@
 // group's word with two xor-shuffles. The grid is a multiple of the SM count and
 // strides over the arrays, so every byte of HBM is touched exactly once.
 #include <cfenv>
+#include <cstdlib>
 #include <cuda_runtime.h>
 
 #include "jac2.cuh"
@@ -165,6 +166,21 @@ static vj_fint bjac2_host(vj_fint n, int internal, const T *a11, const T *a22, c
   // copy engines, so outputs are not written in place.) The masked i-variant keeps the
   // caller's outputs for unprocessed groups and takes the fully staged path below.
   auto al16 = [](const void *q) { return q == nullptr || !((uintptr_t)q & 15u); };
+  // Page-locked outputs as well: one launch reads the inputs and writes the outputs in
+  // place over NVLink-C2C (both directions of the link at once, no copy-engine pass)
+  const char *eo = getenv("VJ_E2E_OUT");
+  if (!internal && host::pageable_access() && !(eo && *eo == 'c') && al16(a11) && al16(a22) && al16(a21r) &&
+      al16(a21i) && al16(c) && al16(cat) && al16(sat) && al16(l1) && al16(l2) && host::host_pinned(c) &&
+      host::host_pinned(cat) && host::host_pinned(sat) && host::host_pinned(l1) && host::host_pinned(l2) &&
+      host::host_pinned(p)) {
+    cudaStream_t st[2];
+    if (!host::streams2(st))
+      return VJ_ERR_CUDA;
+    const vj_fint r = bjac2_dev<T, CPLX>(n, 0, a11, a22, a21r, a21i, c, cat, sat, l1, l2, p, st[0]);
+    if (r < 0)
+      return r;
+    return (cudaStreamSynchronize(st[0]) == cudaSuccess) ? 1 : VJ_ERR_CUDA;
+  }
   if (!internal && host::pageable_access() && al16(a11) && al16(a22) && al16(a21r) && al16(a21i)) {
     const long long chunk = host::bjac2_chunk(nn, sizeof(T), CPLX, LANES);
     const int nout = CPLX ? 5 : 4;

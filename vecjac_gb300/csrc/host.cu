@@ -35,6 +35,18 @@ int sm_count()
   return n;
 }
 
+bool host_pinned(const void *p)
+{
+  if (!p)
+    return true;
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return at.type == cudaMemoryTypeHost;
+}
+
 bool pageable_access()
 {
   static int v = -1;

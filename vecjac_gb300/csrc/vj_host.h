@@ -33,6 +33,8 @@ bool gpu_ready();
 int sm_count();
 // the device can read and write pageable host memory (and VJ_STAGED is not set)
 bool pageable_access();
+// p (NULL counts as true) is page-locked host memory (cudaHostAlloc / cudaHostRegister)
+bool host_pinned(const void *p);
 
 // device memory reused across host-API calls; grows on demand, never shrinks
 struct Staging {
