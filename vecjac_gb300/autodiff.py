@@ -26,36 +26,42 @@ _BLOCK = {}
 
 
 def _tuned_block(A, strategy, swp):
-    """CTA size of the batched kernel for this matrix shape and precision: each of 64, 128
-    and 256 threads is timed on up to 512 of the matrices (after one warm-up), the fastest
-    is kept for the process."""
+    """Launch configuration of the batched kernel for this matrix shape and precision: the
+    CTA size (64, 128, 256 threads) at the default register bound, then the register bound
+    (resident 256-thread CTAs per SM) at the best size, each timed on up to 2432 of the
+    matrices (after one warm-up); the fastest (block, occupancy) is kept for the process."""
     import torch
     key = (tuple(A.shape[1:]), A.dtype, strategy)
     if key not in _BLOCK:
-        sub = A[: min(A.shape[0], 512)]
-        best, best_t = 128, None
-        for blk in (64, 128, 256):
-            svd_batch_dev(sub, strategy, swp, block=blk)
+        sub = A[: min(A.shape[0], 2432)]
+
+        def timed(blk, occ):
+            svd_batch_dev(sub, strategy, swp, block=(blk, occ))
             torch.cuda.synchronize()
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             e0.record()
-            svd_batch_dev(sub, strategy, swp, block=blk)
+            svd_batch_dev(sub, strategy, swp, block=(blk, occ))
             e1.record()
             torch.cuda.synchronize()
-            t = e0.elapsed_time(e1)
-            if best_t is None or t < best_t:
-                best, best_t = blk, t
-        _BLOCK[key] = best
+            return e0.elapsed_time(e1)
+
+        times = {(blk, 0): timed(blk, 0) for blk in (64, 128, 256)}
+        best_blk = min((64, 128, 256), key=lambda b: times[(b, 0)])
+        for occ in ((3, 4, 5) if A.dtype == torch.float32 else (2, 3, 4)):
+            times[(best_blk, occ)] = timed(best_blk, occ)
+        _BLOCK[key] = min(times, key=times.get)
     return _BLOCK[key]
 
 
 def svd_batch_dev(A, strategy=4, swp=999, block=None):
     """SVD of every matrix of A (B, m, n) CUDA tensor (float32 or float64) in one launch
-    (block: threads per CTA; None = autotuned per shape). Returns (S (B, n), U (B, m, n),
-    V (B, n, n), sweeps (B,)) unsorted, as the kernel leaves them."""
+    (block: threads per CTA, or (threads, register bound in resident 256-thread CTAs per
+    SM); None = autotuned per shape). Returns (S (B, n), U (B, m, n), V (B, n, n),
+    sweeps (B,)) unsorted, as the kernel leaves them."""
     import torch
     if block is None:
         block = _tuned_block(A, strategy, swp)
+    block, occ = block if isinstance(block, tuple) else (block, 0)
     Bn, m, n = A.shape
     kind = "s" if A.dtype == torch.float32 else "d"
     L = 16 if kind == "s" else 8
@@ -71,10 +77,10 @@ def svd_batch_dev(A, strategy=4, swp=999, block=None):
     nn = torch.full((Bn,), n, dtype=torch.int64, device=dev)
     ar = torch.arange(Bn, dtype=torch.int64, device=dev)
     offG, offV, offS = ar * (m * n), ar * (n * n), ar * n
-    f = getattr(api.lib(), "vj_%svjsvd_batch_dev" % kind)
+    f = getattr(api.lib(), "vj_%svjsvd_batch_tuned_dev" % kind)
     stream = torch.cuda.current_stream().cuda_stream
     r = f(C.c_longlong(Bn), _p(mm), _p(nn), _p(G), _p(offG), _p(V), _p(offV), _p(eS), _p(fS), _p(offS), None,
-          C.c_long(strategy), C.c_uint(swp), _p(info), C.c_int(block), C.c_void_p(stream))
+          C.c_long(strategy), C.c_uint(swp), _p(info), C.c_int(block), C.c_int(occ), C.c_void_p(stream))
     if r != 0:
         raise RuntimeError("batched SVD launch failed: %d" % r)
     S = fS * torch.exp2(eS)
