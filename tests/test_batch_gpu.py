@@ -75,7 +75,7 @@ def test_batch_autotune_and_graph(env, kind):
         mats = [A.astype(np.float32) for A in mats]
     b = B.Batch(mats, kind)
     blk, occ = B.autotune(b, 4, sample=32)
-    assert blk in (64, 128, 256) and occ in (0, 2, 3, 4, 5)
+    assert blk in (64, 128, 256) and occ in (2, 3, 4, 5)
     b.run(4, block=blk, occupancy=occ)
     torch.cuda.synchronize()
     first = b.results()

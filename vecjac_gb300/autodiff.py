@@ -45,10 +45,12 @@ def _tuned_block(A, strategy, swp):
             torch.cuda.synchronize()
             return e0.elapsed_time(e1)
 
-        times = {(blk, 0): timed(blk, 0) for blk in (64, 128, 256)}
-        best_blk = min((64, 128, 256), key=lambda b: times[(b, 0)])
+        d = 4 if A.dtype == torch.float32 else 2
+        times = {(blk, d): timed(blk, d) for blk in (64, 128, 256)}
+        best_blk = min((64, 128, 256), key=lambda b: times[(b, d)])
         for occ in ((3, 4, 5) if A.dtype == torch.float32 else (2, 3, 4)):
-            times[(best_blk, occ)] = timed(best_blk, occ)
+            if (best_blk, occ) not in times:
+                times[(best_blk, occ)] = timed(best_blk, occ)
         _BLOCK[key] = min(times, key=times.get)
     return _BLOCK[key]
 

@@ -16,6 +16,8 @@ import numpy as np
 from . import api
 
 _TUNED = {}
+# the library's default register bound (resident 256-thread CTAs per SM) per precision
+DEFAULT_OCC = {"s": 4, "d": 2}
 
 
 def padded_shape(m, n, kind):
@@ -131,12 +133,14 @@ def autotune(batch, strategy=4, blocks=(64, 128, 256), occupancies=None, sample=
         torch.cuda.synchronize()
         return e0.elapsed_time(e1)
 
+    d = DEFAULT_OCC[batch.kind]
     times = {}
     for blk in blocks:
-        times[(blk, 0)] = timed(blk, 0)
-    best_blk = min(blocks, key=lambda b_: times[(b_, 0)])
+        times[(blk, d)] = timed(blk, d)
+    best_blk = min(blocks, key=lambda b_: times[(b_, d)])
     for occ in occupancies:
-        times[(best_blk, occ)] = timed(best_blk, occ)
+        if (best_blk, occ) not in times:
+            times[(best_blk, occ)] = timed(best_blk, occ)
     best = min(times, key=times.get)
     _TUNED[key] = best
     return best
