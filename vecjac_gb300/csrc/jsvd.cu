@@ -1106,6 +1106,7 @@ extern "C" vj_fint vj_dvjsvd_dev_noalloc(vj_fnat m, vj_fnat n, double *G, vj_fna
     if (r < 0)
       return r;
   }
+  // (preset 2's all-pairs check keeps a list in a library buffer: not in the allocation-free form)
   return svd_dev<double, false>(m, n, G, ldG, nullptr, ldG, V, ldV, nullptr, ldV, eS, fS, js, (unsigned)stp, swp,
-                                preset, (cudaStream_t)stream, sc);
+                                preset ? 1 : 0, (cudaStream_t)stream, sc);
 }
