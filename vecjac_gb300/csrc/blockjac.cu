@@ -552,22 +552,23 @@ __device__ __forceinline__ Rot pair_rot(float ha, float hb, float cr, float ci, 
 
 // One CTA (256 threads) per block pair: from the pair's Gram matrix S forms H (complex
 // 64 x 64 from the real Gram of [Re | Im], or real 128 x 128), runs `sweeps` cyclic
-// Jacobi sweeps on H with the rotation accumulated in R (R := I first), orders R's columns
-// by descending diagonal of the final H, and writes R's split image for k_apply.
+// Jacobi sweeps on H, logs every step's rotations (rlog: sweeps (N - 1) steps x N/2
+// records per pair) and the order of the final diagonal (rranks: descending, ties by
+// index); k_build_r accumulates the rotations into R on more SMs.
 // stats[0] += rotations, stats[1] = max over rotated pairs of |h_pq| / sqrt(h_pp h_qq)
 // (as float bits).
-// Layout: complex H and R as interleaved (re, im) pairs, one 64-bit shared-memory access
-// per entry; each pair's rotation as one 16-byte record {c, Re s, Im s, p | q << 8 |
+// Layout: complex H as interleaved (re, im) pairs, one 64-bit shared-memory access per
+// entry; each pair's rotation as one 16-byte record {c, Re s, Im s, p | q << 8 |
 // active << 16}.
 // Per Jacobi step: warp 0 (lane u: pair u, and u + 32 for real data) reads the step's
 // pairs from H, writes their rotation records and, for the pairs it rotates, the new 2x2
 // diagonal blocks of H (no other block touches them); after a barrier every thread updates
-// off-diagonal 2x2 blocks (u, v), u < v, of H := J^H H J from a list, and columns of
-// R := R J (lane v: pair v, each warp a share of the rows); a second barrier ends the step.
+// off-diagonal 2x2 blocks (u, v), u < v, of H := J^H H J from a list; a second barrier
+// ends the step.
 constexpr int EVD_THREADS = 256;
 template <bool CPLX>
-__global__ void __launch_bounds__(EVD_THREADS) k_pair_evd(const float *Sred, int sweeps, float tol,
-                                                          unsigned char *Rimg, unsigned *stats)
+__global__ void __launch_bounds__(EVD_THREADS) k_pair_evd(const float *Sred, int sweeps, float tol, float4 *rlog,
+                                                          int *rranks, unsigned *stats)
 {
   using E = typename std::conditional<CPLX, float2, float>::type;
   constexpr int N = CPLX ? 64 : 128;  // order of H
@@ -579,8 +580,7 @@ __global__ void __launch_bounds__(EVD_THREADS) k_pair_evd(const float *Sred, int
   extern __shared__ __align__(16) float fsm[];
   float4 *rot = reinterpret_cast<float4 *>(fsm);  // P records
   E *H = reinterpret_cast<E *>(rot + P);
-  E *R = H + N * LD;
-  unsigned short *tri = reinterpret_cast<unsigned short *>(R + N * LD);  // NO entries: u << 8 | v
+  unsigned short *tri = reinterpret_cast<unsigned short *>(H + N * LD);  // NO entries: u << 8 | v
   int *rank = reinterpret_cast<int *>(tri + ((NO + 1) & ~1));
   __shared__ unsigned nrot_s, mu_s;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -594,7 +594,8 @@ __global__ void __launch_bounds__(EVD_THREADS) k_pair_evd(const float *Sred, int
     if (u < v)
       tri[u * P - u * (u + 1) / 2 + (v - u - 1)] = (unsigned short)((u << 8) | v);
   }
-  // H from S (upper triangle, mirrored: exactly Hermitian); R := I
+  float4 *lg = rlog + (size_t)blockIdx.x * sweeps * (N - 1) * P;
+  // H from S (upper triangle, mirrored: exactly Hermitian)
   for (int q = tid; q < N * N; q += EVD_THREADS) {
     const int i = q / N, j = q % N;
     if (i > j)
@@ -611,13 +612,6 @@ __global__ void __launch_bounds__(EVD_THREADS) k_pair_evd(const float *Sred, int
       H[i * LD + j] = h;
       H[j * LD + i] = h;
     }
-  }
-  for (int q = tid; q < N * N; q += EVD_THREADS) {
-    const int i = q / N, j = q % N;
-    if constexpr (CPLX)
-      R[i * LD + j] = make_float2((i == j) ? 1.f : 0.f, 0.f);
-    else
-      R[i * LD + j] = (i == j) ? 1.f : 0.f;
   }
   __syncthreads();
   auto re = [](const E &x) -> float {
@@ -662,7 +656,10 @@ __global__ void __launch_bounds__(EVD_THREADS) k_pair_evd(const float *Sred, int
           const Rot r = pair_rot(fmaxf(re(H[p * LD + p]), 0.f), fmaxf(re(H[q * LD + q]), 0.f), cr, ci, tol);
           const bool act = r.go && ((r.sr != 0.f) || (r.si != 0.f));
           const unsigned tag = (unsigned)p | ((unsigned)q << 8) | (act ? (1u << 16) : 0u);
-          rot[u] = act ? make_float4(r.c, r.sr, r.si, __uint_as_float(tag)) : make_float4(1.f, 0.f, 0.f, __uint_as_float(tag));
+          const float4 rec =
+              act ? make_float4(r.c, r.sr, r.si, __uint_as_float(tag)) : make_float4(1.f, 0.f, 0.f, __uint_as_float(tag));
+          rot[u] = rec;
+          lg[(size_t)(sw * (N - 1) + stp) * P + u] = rec;
           if (act) {
             if constexpr (CPLX) {
               H[p * LD + p] = make_float2(r.d1, 0.f);
@@ -740,30 +737,6 @@ __global__ void __launch_bounds__(EVD_THREADS) k_pair_evd(const float *Sred, int
           H[qv * LD + qu] = n11;
         }
       }
-      // R := R J: lane v takes pair v (and v + 32), warp w the rows w, w + NW, ...
-#pragma unroll
-      for (int h = 0; h < PL; ++h) {
-        const int v = lane + 32 * h;
-        const float4 rv = rot[v];
-        const unsigned tv = __float_as_uint(rv.w);
-        if (!(tv >> 16))
-          continue;
-        const int pv = tv & 255, qv = (tv >> 8) & 255;
-        const float cv = rv.x, svr = rv.y, svi = rv.z;
-#pragma unroll 4
-        for (int r = warp; r < N; r += NW) {
-          if constexpr (CPLX) {
-            const float2 x = R[r * LD + pv], y = R[r * LD + qv];
-            R[r * LD + pv] = make_float2(fmaf(cv, x.x, -fmaf(svr, y.x, svi * y.y)), fmaf(cv, x.y, -fmaf(svr, y.y, -(svi * y.x))));
-            R[r * LD + qv] = make_float2(fmaf(cv, y.x, fmaf(svr, x.x, -(svi * x.y))), fmaf(cv, y.y, fmaf(svr, x.y, svi * x.x)));
-          }
-          else {
-            const float x = R[r * LD + pv], y = R[r * LD + qv];
-            R[r * LD + pv] = fmaf(cv, x, -(svr * y));
-            R[r * LD + qv] = fmaf(cv, y, svr * x);
-          }
-        }
-      }
       __syncthreads();
     }
   // descending order of the diagonal (ties by index): column rank[r] of R goes to place r
@@ -788,20 +761,114 @@ __global__ void __launch_bounds__(EVD_THREADS) k_pair_evd(const float *Sred, int
       atomicMax(&mu_s, __float_as_uint(mu));
   }
   __syncthreads();
-  unsigned char *img = Rimg + (size_t)blockIdx.x * 6 * PLANE;
-  if constexpr (CPLX)
-    // Rb = [[Re R, Im R], [-Im R, Re R]] with R's columns reordered
-    write_rimg(img, [&](int k, int i) {
-      const float2 x = R[(k & 63) * LD + rank[i & 63]];
-      return (k < 64) ? ((i < 64) ? x.x : x.y) : ((i < 64) ? -x.y : x.x);
-    });
-  else
-    write_rimg(img, [&](int k, int i) { return R[k * LD + rank[i]]; });
+  for (int i = tid; i < N; i += EVD_THREADS)
+    rranks[(size_t)blockIdx.x * N + i] = rank[i];
   if (tid == 0) {
     if (nrot_s)
       atomicAdd(stats, nrot_s);
     if (mu_s)
       atomicMax(stats + 1, mu_s);
+  }
+}
+
+// R := J_1 J_2 ... (the logged rotations of a pair's eigenproblem, in order) and R's split
+// image for k_apply, with its columns in the order of rranks. BR_PARTS CTAs per pair, each
+// a share of R's rows: every warp owns whole rows (in shared memory), so consecutive steps
+// need only the warp's own synchronisation; lane v applies pair v's rotation (and v + 32's
+// for real data) to the columns p_v, q_v of each of its rows. The records are staged in
+// shared memory BR_CHUNK steps at a time.
+constexpr int BR_THREADS = 256, BR_PARTS = 4;
+template <bool CPLX> struct brc {
+  static constexpr int N = CPLX ? 64 : 128, LD = N + 1, ROWS = N / BR_PARTS, CHUNK = CPLX ? 32 : 16;
+};
+template <bool CPLX> static size_t br_smem()
+{
+  using C = brc<CPLX>;
+  return (size_t)C::ROWS * C::LD * (CPLX ? 8 : 4) + (size_t)C::CHUNK * (C::N / 2) * 16 + (size_t)C::N * 4;
+}
+template <bool CPLX>
+__global__ void __launch_bounds__(BR_THREADS) k_build_r(const float4 *rlog, const int *rranks, int sweeps,
+                                                        unsigned char *Rimg)
+{
+  using E = typename std::conditional<CPLX, float2, float>::type;
+  using C = brc<CPLX>;
+  constexpr int N = C::N, P = N / 2, PL = P / 32, LD = C::LD, ROWS = C::ROWS, CH = C::CHUNK;
+  constexpr int NW = BR_THREADS / 32, RPW = ROWS / NW;  // rows per warp
+  extern __shared__ __align__(16) float fsm[];
+  E *R = reinterpret_cast<E *>(fsm);                      // ROWS x LD: rows r0 .. r0 + ROWS - 1
+  float4 *lg = reinterpret_cast<float4 *>(R + ROWS * LD);  // CH steps x P records
+  int *rank = reinterpret_cast<int *>(lg + CH * P);
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int pair = blockIdx.x / BR_PARTS, r0 = (blockIdx.x % BR_PARTS) * ROWS;
+  const int steps = sweeps * (N - 1);
+  const float4 *src = rlog + (size_t)pair * steps * P;
+  for (int i = tid; i < N; i += BR_THREADS)
+    rank[i] = rranks[(size_t)pair * N + i];
+  for (int q = tid; q < ROWS * N; q += BR_THREADS) {
+    const int r = q / N, j = q % N;
+    if constexpr (CPLX)
+      R[r * LD + j] = make_float2((r0 + r == j) ? 1.f : 0.f, 0.f);
+    else
+      R[r * LD + j] = (r0 + r == j) ? 1.f : 0.f;
+  }
+  for (int c0 = 0; c0 < steps; c0 += CH) {
+    const int nst = (steps - c0 < CH) ? (steps - c0) : CH;
+    __syncthreads();  // the previous chunk's records are consumed
+    for (int q = tid; q < nst * P; q += BR_THREADS)
+      lg[q] = src[(size_t)c0 * P + q];
+    __syncthreads();
+    for (int st = 0; st < nst; ++st) {
+#pragma unroll
+      for (int h = 0; h < PL; ++h) {
+        const float4 rv = lg[st * P + lane + 32 * h];
+        const unsigned tv = __float_as_uint(rv.w);
+        if (!(tv >> 16))
+          continue;
+        const int pv = tv & 255, qv = (tv >> 8) & 255;
+        const float cv = rv.x, svr = rv.y, svi = rv.z;
+#pragma unroll
+        for (int i = 0; i < RPW; ++i) {
+          const int r = warp * RPW + i;
+          if constexpr (CPLX) {
+            const float2 x = R[r * LD + pv], y = R[r * LD + qv];
+            R[r * LD + pv] = make_float2(fmaf(cv, x.x, -fmaf(svr, y.x, svi * y.y)), fmaf(cv, x.y, -fmaf(svr, y.y, -(svi * y.x))));
+            R[r * LD + qv] = make_float2(fmaf(cv, y.x, fmaf(svr, x.x, -(svi * x.y))), fmaf(cv, y.y, fmaf(svr, x.y, svi * x.x)));
+          }
+          else {
+            const float x = R[r * LD + pv], y = R[r * LD + qv];
+            R[r * LD + pv] = fmaf(cv, x, -(svr * y));
+            R[r * LD + qv] = fmaf(cv, y, svr * x);
+          }
+        }
+      }
+      __syncwarp();
+    }
+  }
+  __syncthreads();
+  // the image: B[i][k] = Rb[k][i] for the rows k of Rb this CTA holds (real: R's rows
+  // r0 ..; complex: Rb = [[Re R, Im R], [-Im R, Re R]], rows r0 .. and 64 + r0 ..), columns
+  // i in rank order; 8 consecutive k per 16-byte store of each term (the layout of write_rimg)
+  unsigned char *img = Rimg + (size_t)pair * 6 * PLANE;
+  constexpr int NK8 = CPLX ? 2 * ROWS / 8 : ROWS / 8;
+  for (int q = tid; q < TILE * NK8; q += BR_THREADS) {
+    const int i = q % TILE, ci = q / TILE;
+    int k8;
+    if constexpr (CPLX)
+      k8 = (ci < ROWS / 8) ? (r0 + 8 * ci) : (64 + r0 + 8 * (ci - ROWS / 8));
+    else
+      k8 = r0 + 8 * ci;
+    float v[8];
+#pragma unroll
+    for (int e = 0; e < 8; ++e) {
+      const int k = k8 + e;
+      if constexpr (CPLX) {
+        const float2 x = R[((k & 63) - r0) * LD + rank[i & 63]];
+        v[e] = (k < 64) ? ((i < 64) ? x.x : x.y) : ((i < 64) ? -x.y : x.x);
+      }
+      else
+        v[e] = R[(k - r0) * LD + rank[i]];
+    }
+    store_split8(img + (k8 / KC) * 3 * PLANE + tile_off(i, k8 % KC), v);
   }
 }
 
@@ -816,7 +883,7 @@ __global__ void __launch_bounds__(256) k_rimg(const float *R, unsigned char *Rim
 static size_t evd_smem(bool cplx)
 {
   const int N = cplx ? 64 : 128, P = N / 2, LD = N + 1, NO = P * (P - 1) / 2;
-  return (size_t)P * 16 + (size_t)2 * N * LD * (cplx ? 8 : 4) + (size_t)((NO + 1) & ~1) * 2 + (size_t)N * 4;
+  return (size_t)P * 16 + (size_t)N * LD * (cplx ? 8 : 4) + (size_t)((NO + 1) & ~1) * 2 + (size_t)N * 4;
 }
 
 constexpr size_t GRAM_SMEM = 2 * 3 * PLANE + 1024;
@@ -891,10 +958,18 @@ bool block_sweeps_apply(bool cplx, long long m, long long n, long long ld)
 }
 
 // Scratch bytes of block_sweep for an m x n problem.
-size_t block_sweep_scratch(bool cplx, long long m, long long n)
+// (the Gram partials and their sum, R's split images, the rotation logs of `inner` sweeps
+// of the pair eigenproblems and their orders)
+static size_t rlog_records(bool cplx, int npairs, int inner)
+{
+  const int N = cplx ? 64 : 128;
+  return (size_t)npairs * inner * (N - 1) * (N / 2);
+}
+size_t block_sweep_scratch(bool cplx, long long m, long long n, int inner)
 {
   const bj::Plan p = bj::plan(cplx, m, n);
-  return (size_t)p.npairs * (p.ksplit * 2 + 1) * bj::TILE * bj::TILE * 4 + (size_t)p.npairs * 6 * bj::PLANE + 256;
+  return (size_t)p.npairs * (p.ksplit * 2 + 1) * bj::TILE * bj::TILE * 4 + (size_t)p.npairs * 6 * bj::PLANE +
+         rlog_records(cplx, p.npairs, inner) * 16 + (size_t)p.npairs * (cplx ? 64 : 128) * 4 + 256;
 }
 
 // One block sweep (nb - 1 block steps) on planar FP32 G (m x n) and W (n x n), both with
@@ -913,6 +988,8 @@ long long block_sweep(bool cplx, int m, int n, float *Gr, float *Gi, long long l
   float *Spart = reinterpret_cast<float *>(scratch);
   float *Sred = Spart + (size_t)p.npairs * p.ksplit * 2 * TILE * TILE;
   unsigned char *Rimg = scratch + (size_t)p.npairs * (p.ksplit * 2 + 1) * TILE * TILE * 4;
+  float4 *rlog = reinterpret_cast<float4 *>(Rimg + (size_t)p.npairs * 6 * PLANE);
+  int *rranks = reinterpret_cast<int *>(rlog + rlog_records(cplx, p.npairs, inner));
   const Cols G{Gr, cplx ? Gi : nullptr, ldg, p.b}, W{Wr, cplx ? Wi : nullptr, ldw, p.b};
   if (cudaMemsetAsync(stats, 0, 16, s) != cudaSuccess)
     return -1;
@@ -922,10 +999,14 @@ long long block_sweep(bool cplx, int m, int n, float *Gr, float *Gi, long long l
     else
       k_gram<6><<<p.npairs * p.ksplit, 128, GRAM_SMEM, s>>>(G, m, p.nb, step, p.ksplit, Spart, stats + 2);
     k_gram_reduce<<<p.npairs * 16, 256, 0, s>>>(Spart, p.ksplit, Sred);
-    if (cplx)
-      k_pair_evd<true><<<p.npairs, EVD_THREADS, evd_smem(true), s>>>(Sred, inner, tol, Rimg, stats);
-    else
-      k_pair_evd<false><<<p.npairs, EVD_THREADS, evd_smem(false), s>>>(Sred, inner, tol, Rimg, stats);
+    if (cplx) {
+      k_pair_evd<true><<<p.npairs, EVD_THREADS, evd_smem(true), s>>>(Sred, inner, tol, rlog, rranks, stats);
+      k_build_r<true><<<p.npairs * BR_PARTS, BR_THREADS, br_smem<true>(), s>>>(rlog, rranks, inner, Rimg);
+    }
+    else {
+      k_pair_evd<false><<<p.npairs, EVD_THREADS, evd_smem(false), s>>>(Sred, inner, tol, rlog, rranks, stats);
+      k_build_r<false><<<p.npairs * BR_PARTS, BR_THREADS, br_smem<false>(), s>>>(rlog, rranks, inner, Rimg);
+    }
     if (terms == 3)
       k_apply<3><<<p.npairs * p.q, APPLY_THREADS, APPLY_SMEM, s>>>(G, m, W, n, p.nb, step, p.tg, p.tw, p.q, Rimg,
                                                                     stats + 2);
@@ -1052,7 +1133,7 @@ extern "C" vj_fint vj_block_sweep_dev(int cplx, vj_fnat m, vj_fnat n, float *Gr,
     return VJ_ERR_NO_GPU;
   unsigned char *scr = nullptr;
   unsigned *stats = nullptr;
-  if (cudaMalloc(&scr, block_sweep_scratch(cplx != 0, (long long)m, (long long)n)) != cudaSuccess)
+  if (cudaMalloc(&scr, block_sweep_scratch(cplx != 0, (long long)m, (long long)n, inner)) != cudaSuccess)
     return VJ_ERR_NOMEM;
   if (cudaMalloc(&stats, 16) != cudaSuccess) {
     cudaFree(scr);

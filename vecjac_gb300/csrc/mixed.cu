@@ -42,7 +42,7 @@ namespace vj {
 
 // defined in blockjac.cu: block sweeps with split-BF16x3 tensor-core products
 bool block_sweeps_apply(bool cplx, long long m, long long n, long long ld);
-size_t block_sweep_scratch(bool cplx, long long m, long long n);
+size_t block_sweep_scratch(bool cplx, long long m, long long n, int inner);
 long long block_sweep(bool cplx, int m, int n, float *Gr, float *Gi, long long ldg, float *Wr, float *Wi,
                       long long ldw, unsigned char *scratch, unsigned *stats, float tol, int inner, int terms,
                       cudaStream_t s, float *mu);
@@ -655,7 +655,7 @@ static vj_fint mixed_dev(vj_fnat m_, vj_fnat n_, double *G, vj_fnat ldG, double 
   const int terms = (et && atoi(et) == 3) ? 3 : 6;
   const char *ei = getenv("VJ_BLOCK_INNER");
   const int inner = (ei && atoi(ei) >= 1 && atoi(ei) <= 8) ? atoi(ei) : 1;
-  const size_t blkb = blk ? ((block_sweep_scratch(CPLX, m, n) + 255) & ~(size_t)255) : 0;
+  const size_t blkb = blk ? ((block_sweep_scratch(CPLX, m, n, inner) + 255) & ~(size_t)255) : 0;
   host::Staging &stg = host::staging3();
   if (!stg.reserve(f32b + f64b + 256 + blkb))
     return VJ_ERR_NOMEM;
@@ -946,8 +946,9 @@ static vj_fint mixed_dev(vj_fnat m_, vj_fnat n_, double *G, vj_fnat ldG, double 
   // 6. FP64 finishing sweeps (the reference's algorithm) with V preset
   const vj_fint r = svd_dev_entry<double, CPLX>(m_, n_, G, ldG, Gi, ldGi, V, ldV, Vi, ldVi, eS, fS, js, stp, swp, 2, s);
   const double msfin = std::chrono::duration<double, std::milli>(now() - t0).count();
-  // FP32 launches: 3 per block step (n/b - 1 steps per block sweep), else 1 per pivot step
-  const double steps32 = blk ? (double)total32 * (double)(n / (CPLX ? 32 : 64) - 1) * 3.0 : (double)total32 * stp;
+  // FP32 launches: 5 per block step (Gram, its reduction, the pair eigenproblems, R, the
+  // rotation; n/b - 1 steps per block sweep), else 1 per pivot step
+  const double steps32 = blk ? (double)total32 * (double)(n / (CPLX ? 32 : 64) - 1) * 5.0 : (double)total32 * stp;
   host::mixed_phases_set(ms32, msgemm, ms64, msfin, steps32, blk ? 1.0 : 0.0);
   if (trace)
     std::fprintf(stderr, "mixed SVD phases (ms): FP32 sweeps %.1f, Newton-Schulz + GEMMs %.1f, plain FP64 sweeps + sort %.1f, "
