@@ -8,12 +8,13 @@
 // independent pairs per block step, and for each pair
 //   1. k_gram:  S = X^T X, the real Gram matrix of the pair's 128 real columns X (128 x 128,
 //      K = m, split over several CTAs), on the tensor cores (its symmetry halves the cross
-//      terms of the split products);
+//      terms of the split products), and k_gram_reduce: the sum over the K splits;
 //   2. k_pair_evd: the Hermitian Gram matrix H = [G_I G_J]^H [G_I G_J] (from S), one cyclic
-//      two-sided Jacobi sweep on H that accumulates the unitary R (2b x 2b) -- in exact
-//      arithmetic the rotations of one-sided Jacobi on the pair's columns, from the same
-//      2x2 Gram blocks, with the same threshold -- and a reordering of R's columns by
-//      descending norms (the block form of the scalar sweep's swap rule);
+//      two-sided Jacobi sweep on H -- in exact arithmetic the rotations of one-sided Jacobi
+//      on the pair's columns, from the same 2x2 Gram blocks, with the same threshold --
+//      with its rotations logged, and the order of descending norms (the block form of the
+//      scalar sweep's swap rule); k_build_r: the unitary R (2b x 2b) as the product of the
+//      logged rotations, its columns in that order, and R's split image;
 //   3. k_apply: [G_I G_J] := [G_I G_J] R and [W_I W_J] := [W_I W_J] R on the tensor cores
 //      (the real 128 x 128 form of R for complex data: [[Re R, Im R], [-Im R, Re R]]).
 // Each FP32 operand x is split into three BF16 terms x = h + m + l (exactly: 8 + 8 + 8
@@ -21,7 +22,7 @@
 // l h (the dropped ones are below 2^-24 relative), accumulated in FP32 in TMEM: the
 // accuracy of an FP32 product at tensor-core speed. Operands are converted from FP32 to
 // the split BF16 tiles by the CTA's threads (the A side) or copied by the bulk-copy TMA
-// engine from the split image that k_pair_evd writes (the R side of k_apply).
+// engine from the split image that k_build_r writes (the R side of k_apply).
 #include <cuda_bf16.h>
 #include <type_traits>
 #include <cuda_runtime.h>
