@@ -569,10 +569,14 @@ def svd_case(args, vj, dist, kind, m, n, lo, mixed_steps, plain_steps, warmup, s
         ou = float(torch.linalg.norm(U.conj() @ U.T - torch.eye(n, dtype=U.dtype, device="cuda")))
         ov = float(torch.linalg.norm(Vm.conj() @ Vm.T - torch.eye(n, dtype=Vm.dtype, device="cuda")))
         srt = np.sort(sig)[::-1]
+        # the stated orthogonality bound is ||U^H U - I||_F, ||V^H V - I||_F <= 16 n eps; the
+        # reference's own algorithm (the plain path, bit for bit) can exceed it for V, and
+        # the flag says so per configuration rather than loosening the bound
         return sig, {"max_rel_sigma_err_vs_exact": float(np.max(np.abs(srt - s) / s)),
                      "max_sigma_err_over_sigma_max": float(np.max(np.abs(srt - s)) / s[0]),
                      "orth_U_fro_over_n_eps": round(ou / (n * eps), 3),
-                     "orth_V_fro_over_n_eps": round(ov / (n * eps), 3)}
+                     "orth_V_fro_over_n_eps": round(ov / (n * eps), 3),
+                     "orth_within_16_n_eps": bool(max(ou, ov) <= 16 * n * eps)}
 
     per_pair = (36 * m + 20 * n) if cx else (12 * m + 6 * n)
     out = {"config": "%svjsvd %dx%d, sigma log-uniform in [1e%d, 1], pivot strategy id %d" % (kind, m, n, lo, args.pivot),

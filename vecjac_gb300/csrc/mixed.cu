@@ -156,38 +156,124 @@ template <typename T> __device__ void block_sum4(T &a, T &b, T &cr, T &ci, T (*r
   }
 }
 
-// (p, q) <- (cs p - sn e^{-i phi} q, sn e^{i phi} p + cs q), element-wise, with explicit
-// FMAs (the library is built without automatic contraction; these steps are not
-// reproductions of the reference's arithmetic): 3 operations per output element
+// Coefficients of one pair's rotation as the columns are stored:
+//   general form  p := cp p - conj(u) q,  q := cq q + v p   (3 operations per output)
+//   short form    p := p - conj(u) q,     q := q + v p      (2 FMAs per output)
+// Without column scales cp = cq = cs and u = v = sn e^{i phi}: the rotation of hestenes.
+// The FP64 sweeps store each column as d_j times a stored column (d_j in [2^-8, 1], one
+// scale per column of G and of V). A rotation then factors as
+//   p' = (cs d_p) (p~ - conj(sn e^{i phi}) (d_q / (cs d_p)) q~),
+//   q' = (cs d_q) (q~ + sn e^{i phi} (d_p / (cs d_q)) p~),
+// so the stored columns take the short form and the cosines go into the scales, which
+// are multiplied into the columns once per sweep: 8 instead of 12 FP64 operations per
+// complex element (2 instead of 4 per real one). A pair whose new scale would fall below
+// 2^-8 takes the general form with cp = cs d_p, cq = cs d_q, u = sn e^{i phi} d_q,
+// v = sn e^{i phi} d_p instead, and its scales return to 1, so that a stored column is
+// never more than 2^8 times its true length. (Not the reference's arithmetic: these
+// sweeps precondition the reference's own sweeps, which decide the result.)
+template <typename T> struct Rot {
+  T cp, cq, ur, ui, vr, vi;
+  bool go, swap, shrt;
+};
+constexpr double COL_SCALE_MIN = 1.0 / 256.0;
+// only the FP64 sweeps carry column scales: the FP32 kernels are compiled for the
+// unscaled rotation alone (cq = cp, v = u)
+template <typename T> __host__ __device__ constexpr bool has_scales() { return sizeof(T) == 8; }
+template <typename T> __device__ __forceinline__ void unscaled_form(Rot<T> &k)
+{
+  if (!has_scales<T>()) {
+    k.shrt = false;
+    k.cq = k.cp;
+    k.vr = k.ur;
+    k.vi = k.ui;
+  }
+}
+
+// the coefficients from hestenes' {cs, sn cos phi, sn sin phi, go, swap} and the pair's
+// column scales; with scales (dsc != nullptr) the new scales are written to dsc[p], dsc[q]
+template <typename T>
+__device__ Rot<T> pair_rot(const T *h, T dp, T dq, T *dsc, unsigned p, unsigned q)
+{
+  Rot<T> r;
+  const T cs = h[0], snr = h[1], sni = h[2];
+  r.go = h[3] != (T)0;
+  r.swap = h[4] != (T)0;
+  r.shrt = false;
+  r.cp = r.cq = cs;
+  r.ur = r.vr = snr;
+  r.ui = r.vi = sni;
+  if (!dsc || !r.go)
+    return r;
+  const T np = cs * dp, nq = cs * dq;
+  if (np >= (T)COL_SCALE_MIN && nq >= (T)COL_SCALE_MIN) {
+    const T k1 = dq / np, k2 = dp / nq;
+    r.shrt = true;
+    r.cp = r.cq = (T)1;
+    r.ur = snr * k1;
+    r.ui = sni * k1;
+    r.vr = snr * k2;
+    r.vi = sni * k2;
+    dsc[p] = r.swap ? nq : np;
+    dsc[q] = r.swap ? np : nq;
+  }
+  else {
+    r.cp = np;
+    r.cq = nq;
+    r.ur = snr * dq;
+    r.ui = sni * dq;
+    r.vr = snr * dp;
+    r.vi = sni * dp;
+    dsc[p] = dsc[q] = (T)1;
+  }
+  return r;
+}
+
+// (p, q) <- the rotation above, element-wise, with explicit FMAs (the library is built
+// without automatic contraction)
 template <typename T, bool CPLX>
-__device__ __forceinline__ void rot_elem(T cs, T snr, T sni, T &pr, T &pi, T &qr, T &qi)
+__device__ __forceinline__ void rot_elem(const Rot<T> &c, T &pr, T &pi, T &qr, T &qi)
 {
   const T Pr = pr, Qr = qr;
   if (CPLX) {
     const T Pi = pi, Qi = qi;
-    pr = fma(cs, Pr, -fma(snr, Qr, sni * Qi));
-    pi = fma(cs, Pi, -fma(snr, Qi, -(sni * Qr)));
-    qr = fma(cs, Qr, fma(snr, Pr, -(sni * Pi)));
-    qi = fma(cs, Qi, fma(snr, Pi, sni * Pr));
+    if (c.shrt) {
+      pr = fma(-c.ur, Qr, fma(-c.ui, Qi, Pr));
+      pi = fma(-c.ur, Qi, fma(c.ui, Qr, Pi));
+      qr = fma(c.vr, Pr, fma(-c.vi, Pi, Qr));
+      qi = fma(c.vr, Pi, fma(c.vi, Pr, Qi));
+    }
+    else {
+      pr = fma(c.cp, Pr, -fma(c.ur, Qr, c.ui * Qi));
+      pi = fma(c.cp, Pi, -fma(c.ur, Qi, -(c.ui * Qr)));
+      qr = fma(c.cq, Qr, fma(c.vr, Pr, -(c.vi * Pi)));
+      qi = fma(c.cq, Qi, fma(c.vr, Pi, c.vi * Pr));
+    }
+  }
+  else if (c.shrt) {
+    pr = fma(-c.ur, Qr, Pr);
+    qr = fma(c.vr, Pr, Qr);
   }
   else {
-    pr = fma(cs, Pr, -(snr * Qr));
-    qr = fma(cs, Qr, snr * Pr);
+    pr = fma(c.cp, Pr, -(c.ur * Qr));
+    qr = fma(c.cq, Qr, c.vr * Pr);
   }
 }
 
 // rotate columns (x, y); with swap the rotated y goes to x's place and the rotated x to y's
-template <typename T, bool CPLX>
-__device__ void rot_cols(int rows, T *xr, T *xi, T *yr, T *yi, T cs, T snr, T sni, bool swap)
+template <typename T, bool CPLX, bool SHRT>
+__device__ void rot_cols_(int rows, T *xr, T *xi, T *yr, T *yi, const Rot<T> &c)
 {
-  T *dxr = swap ? yr : xr, *dxi = swap ? yi : xi, *dyr = swap ? xr : yr, *dyi = swap ? xi : yi;
+  T *dxr = c.swap ? yr : xr, *dxi = c.swap ? yi : xi, *dyr = c.swap ? xr : yr, *dyi = c.swap ? xi : yi;
+  Rot<T> k = c;
+  k.shrt = SHRT;  // a compile-time form inside the loop
+  unscaled_form(k);
   for (int i = threadIdx.x; i < rows; i += blockDim.x) {
     T pr = xr[i], qr = yr[i], pi = 0, qi = 0;
     if (CPLX) {
       pi = xi[i];
       qi = yi[i];
     }
-    rot_elem<T, CPLX>(cs, snr, sni, pr, pi, qr, qi);
+    rot_elem<T, CPLX>(k, pr, pi, qr, qi);
     dxr[i] = pr;
     dyr[i] = qr;
     if (CPLX) {
@@ -196,18 +282,48 @@ __device__ void rot_cols(int rows, T *xr, T *xi, T *yr, T *yi, T cs, T snr, T sn
     }
   }
 }
+template <typename T, bool CPLX>
+__device__ void rot_cols(int rows, T *xr, T *xi, T *yr, T *yi, const Rot<T> &c)
+{
+  if (has_scales<T>() && c.shrt)
+    rot_cols_<T, CPLX, true>(rows, xr, xi, yr, yi, c);
+  else
+    rot_cols_<T, CPLX, false>(rows, xr, xi, yr, yi, c);
+}
+
+// the pair's rotation from its (stored) Gram entries, by thread 0 into *rs: the entries are
+// scaled by the column scales first, if there are any
+template <typename T>
+__device__ void pair_rotation(T a, T b, T cr, T ci, T tol, unsigned *cnt, T *dsc, unsigned p, unsigned q, Rot<T> *rs)
+{
+  T dp = 1, dq = 1;
+  if (!has_scales<T>())
+    dsc = nullptr;
+  if (dsc) {
+    dp = dsc[p];
+    dq = dsc[q];
+    a *= dp * dp;
+    b *= dq * dq;
+    cr *= dp * dq;
+    ci *= dp * dq;
+  }
+  T h[5];
+  hestenes(a, b, cr, ci, tol, h, cnt);
+  *rs = pair_rot(h, dp, dq, dsc, p, q);
+}
 
 // One pivot step of one-sided Jacobi (Hestenes) with plain dot products, FP32 or FP64, on
 // planar G (m x n) and W (n x n): CTA k takes pair (p, q) = row st of the pivot table,
 // forms a = |g_p|^2, b = |g_q|^2, c = g_p^H g_q (per-thread partial sums and a block
 // tree) and rotates columns p and q of G and W (hestenes above). Any m; G is read twice.
+// dsc: the column scales of the FP64 sweeps (Rot above), or nullptr.
 template <typename T, bool CPLX>
 __global__ void __launch_bounds__(256) k_presweep(int m, int n, T *Gr, long long ldr, T *Gi, long long ldi, T *Wr,
                                                   long long lwr, T *Wi, long long lwi, const unsigned *js, int st,
-                                                  T tol, unsigned *cnt)
+                                                  T tol, unsigned *cnt, T *dsc)
 {
   __shared__ T red[4][16];
-  __shared__ T rot[5];
+  __shared__ Rot<T> rs;
   pdl_enter();
   const int k = blockIdx.x;
   const unsigned p = js[(size_t)st * n + 2 * k], q = js[(size_t)st * n + 2 * k + 1];
@@ -230,15 +346,44 @@ __global__ void __launch_bounds__(256) k_presweep(int m, int n, T *Gr, long long
   }
   block_sum4(a, b, cr, ci, red);
   if (threadIdx.x == 0)
-    hestenes(a, b, cr, ci, tol, rot, cnt);
+    pair_rotation(a, b, cr, ci, tol, cnt, dsc, p, q, &rs);
   __syncthreads();
-  if (rot[3] == (T)0)
+  const Rot<T> c = rs;
+  if (!c.go)
     return;
-  const T cs = rot[0], snr = rot[1], sni = rot[2];
-  const bool swap = rot[4] != (T)0;
-  rot_cols<T, CPLX>(m, gpr, gpi, gqr, gqi, cs, snr, sni, swap);
+  rot_cols<T, CPLX>(m, gpr, gpi, gqr, gqi, c);
   rot_cols<T, CPLX>(n, Wr + (size_t)p * lwr, CPLX ? Wi + (size_t)p * lwi : nullptr, Wr + (size_t)q * lwr,
-                    CPLX ? Wi + (size_t)q * lwi : nullptr, cs, snr, sni, swap);
+                    CPLX ? Wi + (size_t)q * lwi : nullptr, c);
+}
+
+// the rotation of the register-resident column vectors of k_presweep_reg, written back
+template <typename T, bool CPLX, int R, int NT, bool SHRT, typename V>
+__device__ __forceinline__ void rot_regs(V (&xr)[R], V (&yr)[R], V (&xi)[R], V (&yi)[R], int mv, Rot<T> k, V *gpr,
+                                         V *gqr, V *gpi, V *gqi)
+{
+  constexpr int E = vec16<T>::E;
+  k.shrt = SHRT;
+  unscaled_form(k);
+  V *dpr = k.swap ? gqr : gpr, *dqr = k.swap ? gpr : gqr, *dpi = k.swap ? gqi : gpi, *dqi = k.swap ? gpi : gqi;
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    const int i = threadIdx.x + r * NT;
+    if (i < mv) {
+      T *X = reinterpret_cast<T *>(&xr[r]), *Y = reinterpret_cast<T *>(&yr[r]);
+      T *Xi = reinterpret_cast<T *>(&xi[r]), *Yi = reinterpret_cast<T *>(&yi[r]);
+#pragma unroll
+      for (int e = 0; e < E; ++e) {
+        T d0 = 0, d1 = 0;
+        rot_elem<T, CPLX>(k, X[e], CPLX ? Xi[e] : d0, Y[e], CPLX ? Yi[e] : d1);
+      }
+      dpr[i] = xr[r];
+      dqr[i] = yr[r];
+      if (CPLX) {
+        dpi[i] = xi[r];
+        dqi[i] = yi[r];
+      }
+    }
+  }
 }
 
 // The same step with the two columns of G held in registers between the dot products and
@@ -248,12 +393,12 @@ __global__ void __launch_bounds__(256) k_presweep(int m, int n, T *Gr, long long
 template <typename T, bool CPLX, int R, int NT>
 __global__ void __launch_bounds__(NT) k_presweep_reg(int m, int n, T *Gr, long long ldr, T *Gi, long long ldi,
                                                       T *Wr, long long lwr, T *Wi, long long lwi, const unsigned *js,
-                                                      int st, T tol, unsigned *cnt)
+                                                      int st, T tol, unsigned *cnt, T *dsc)
 {
   using V = typename vec16<T>::V;
   constexpr int E = vec16<T>::E;
   __shared__ T red[4][16];
-  __shared__ T rot[5];
+  __shared__ Rot<T> rs;
   pdl_enter();
   const int k = blockIdx.x;
   const unsigned p = js[(size_t)st * n + 2 * k], q = js[(size_t)st * n + 2 * k + 1];
@@ -298,52 +443,75 @@ __global__ void __launch_bounds__(NT) k_presweep_reg(int m, int n, T *Gr, long l
   }
   block_sum4(a, b, cr, ci, red);
   if (threadIdx.x == 0)
-    hestenes(a, b, cr, ci, tol, rot, cnt);
+    pair_rotation(a, b, cr, ci, tol, cnt, dsc, p, q, &rs);
   __syncthreads();
-  if (rot[3] == (T)0)
+  const Rot<T> c = rs;
+  if (!c.go)
     return;
-  const T cs = rot[0], snr = rot[1], sni = rot[2];
-  const bool swap = rot[4] != (T)0;
-  V *dpr = swap ? gqr : gpr, *dqr = swap ? gpr : gqr, *dpi = swap ? gqi : gpi, *dqi = swap ? gpi : gqi;
-#pragma unroll
-  for (int r = 0; r < R; ++r) {
-    const int i = threadIdx.x + r * NT;
-    if (i < mv) {
-      T *X = reinterpret_cast<T *>(&xr[r]), *Y = reinterpret_cast<T *>(&yr[r]);
-      T *Xi = reinterpret_cast<T *>(&xi[r]), *Yi = reinterpret_cast<T *>(&yi[r]);
-#pragma unroll
-      for (int e = 0; e < E; ++e) {
-        T d0 = 0, d1 = 0;
-        rot_elem<T, CPLX>(cs, snr, sni, X[e], CPLX ? Xi[e] : d0, Y[e], CPLX ? Yi[e] : d1);
-      }
-      dpr[i] = xr[r];
-      dqr[i] = yr[r];
+  if (has_scales<T>() && c.shrt)
+    rot_regs<T, CPLX, R, NT, true>(xr, yr, xi, yi, mv, c, gpr, gqr, gpi, gqi);
+  else
+    rot_regs<T, CPLX, R, NT, false>(xr, yr, xi, yi, mv, c, gpr, gqr, gpi, gqi);
+  rot_cols<T, CPLX>(n, Wr + (size_t)p * lwr, CPLX ? Wi + (size_t)p * lwi : nullptr, Wr + (size_t)q * lwr,
+                    CPLX ? Wi + (size_t)q * lwi : nullptr, c);
+}
+
+static dim3 grid2(long long rows, long long cols)
+{
+  long long gx = (rows + 255) / 256;
+  if (gx > 32)
+    gx = 32;
+  long long gy = cols < 65535 ? cols : 65535;
+  return dim3((unsigned)gx, (unsigned)(gy > 0 ? gy : 1));
+}
+
+template <typename T> __global__ void k_fill(T *x, int n, T v)
+{
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    x[i] = v;
+}
+
+// columns j of planar G (m x n) and W (n x n) times their scale dsc[j] (those != 1)
+template <typename T, bool CPLX>
+__global__ void k_apply_scales(int m, int n, T *Gr, long long ldr, T *Gi, long long ldi, T *Wr, long long lwr, T *Wi,
+                               long long lwi, const T *dsc)
+{
+  for (int j = blockIdx.y; j < n; j += gridDim.y) {
+    const T d = dsc[j];
+    if (d == (T)1)
+      continue;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m + n; i += gridDim.x * blockDim.x) {
+      const bool g = i < m;
+      const int r = g ? i : i - m;
+      T *pr = g ? Gr + (size_t)j * ldr + r : Wr + (size_t)j * lwr + r;
+      *pr *= d;
       if (CPLX) {
-        dpi[i] = xi[r];
-        dqi[i] = yi[r];
+        T *pi = g ? Gi + (size_t)j * ldi + r : Wi + (size_t)j * lwi + r;
+        *pi *= d;
       }
     }
   }
-  rot_cols<T, CPLX>(n, Wr + (size_t)p * lwr, CPLX ? Wi + (size_t)p * lwi : nullptr, Wr + (size_t)q * lwr,
-                    CPLX ? Wi + (size_t)q * lwi : nullptr, cs, snr, sni, swap);
 }
 
 // one sweep of presweep steps (stp launches); returns the number of rotations or < 0, and
-// in *mu the largest |cos| of a rotated pair
+// in *mu the largest |cos| of a rotated pair. With dsc (n entries of scratch) the columns
+// carry scales during the sweep (Rot above), multiplied into G and W at its end.
 template <typename T, bool CPLX>
 static long long presweep(int m, int n, T *Gr, long long ldr, T *Gi, long long ldi, T *Wr, long long lwr, T *Wi,
                           long long lwi, const unsigned *js, unsigned stp, T tol, unsigned *cnt, cudaStream_t s,
-                          float *mu)
+                          float *mu, T *dsc = nullptr)
 {
   constexpr int E = vec16<T>::E;
   const bool al = !(m % E) && !((ldr * (long long)sizeof(T)) % 16) && !((uintptr_t)Gr % 16) &&
                   (!CPLX || (!((ldi * (long long)sizeof(T)) % 16) && !((uintptr_t)Gi % 16)));
   if (cudaMemsetAsync(cnt, 0, 8, s) != cudaSuccess)
     return -1;
+  if (dsc)
+    k_fill<T><<<(n + 255) / 256, 256, 0, s>>>(dsc, n, (T)1);
   const unsigned nb = (unsigned)(n / 2);
   const long long cap = 256LL * E;  // rows per register vector slot
   void (*k)(int, int, T *, long long, T *, long long, T *, long long, T *, long long, const unsigned *, int, T,
-            unsigned *) = k_presweep<T, CPLX>;
+            unsigned *, T *) = k_presweep<T, CPLX>;
   int nt = 256;
   // register-resident columns: up to 2 vectors per thread and plane with 256 threads, then
   // (FP32) 2 vectors with 512 threads; beyond that the FP64 kernel's register use would
@@ -359,8 +527,10 @@ static long long presweep(int m, int n, T *Gr, long long ldr, T *Gi, long long l
   }
   for (unsigned st = 0; st < stp; ++st)
     if (host::launch_pdl(k, dim3(nb), dim3(nt), 0, s, m, n, Gr, ldr, Gi, ldi, Wr, lwr, Wi, lwi, js, (int)st, tol,
-                         cnt) != cudaSuccess)
+                         cnt, dsc) != cudaSuccess)
       return -1;
+  if (dsc)
+    k_apply_scales<T, CPLX><<<grid2(m + n, n), 256, 0, s>>>(m, n, Gr, ldr, Gi, ldi, Wr, lwr, Wi, lwi, dsc);
   unsigned hc[2] = {0u, 0u};
   if (cudaGetLastError() != cudaSuccess || cudaMemcpyAsync(hc, cnt, 8, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
       cudaStreamSynchronize(s) != cudaSuccess)
@@ -404,15 +574,6 @@ __global__ void k_gather_cols(int rows, int n, const double *A, long long lda, c
   for (int j = blockIdx.y; j < n; j += gridDim.y)
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < rows; i += gridDim.x * blockDim.x)
       B[(size_t)j * rows + i] = A[(size_t)perm[j] * lda + i];
-}
-
-static dim3 grid2(long long rows, long long cols)
-{
-  long long gx = (rows + 255) / 256;
-  if (gx > 32)
-    gx = 32;
-  long long gy = cols < 65535 ? cols : 65535;
-  return dim3((unsigned)gx, (unsigned)(gy > 0 ? gy : 1));
 }
 
 static cublasHandle_t cublas()
@@ -874,8 +1035,9 @@ static vj_fint mixed_dev(vj_fnat m_, vj_fnat n_, double *G, vj_fnat ldG, double 
   }
   // 5. FP64 sweeps with plain dot products on G and V themselves until no pair reaches half
   //    the reference's tolerance sqrt(m) eps / 2 (at most 20 sweeps): they take the columns from
-  //    FP32 to FP64 orthogonality at a fraction of a reference sweep's cost (about 12 FP64
-  //    operations per complex element instead of 68), so the reference's sweeps below
+  //    FP32 to FP64 orthogonality at a fraction of a reference sweep's cost (8 FP64
+  //    operations per complex element of G for the dot products and 8 for the rotation in
+  //    the short form of Rot, instead of 68), so the reference's sweeps below
   //    have at most the last rotations to do and the convergence to confirm.
   if (total32) {
     // half the reference's tolerance: the plain dot product's rounding (a few eps) stays
@@ -888,9 +1050,10 @@ static vj_fint mixed_dev(vj_fnat m_, vj_fnat n_, double *G, vj_fnat ldG, double 
     // confirming sweep is skipped, the reference's sweep below confirms.
     for (; sw64 < maxsw64; ++sw64) {
       float mu = 0.f;
+      // (column scales in Y, free scratch until the sort below)
       const long long hc = presweep<double, CPLX>(mi, ni, G, (long long)ldG, Gi, (long long)(CPLX ? ldGi : ldG), V,
                                                   (long long)ldV, Vi, (long long)(CPLX ? ldVi : ldV), js, stp, tol64,
-                                                  cnt, s, &mu);
+                                                  cnt, s, &mu, Y);
       if (hc < 0)
         return VJ_ERR_CUDA;
       if (trace)
