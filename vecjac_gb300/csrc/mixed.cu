@@ -101,10 +101,14 @@ template <> struct vec16<double> { using V = double2; static constexpr int E = 2
 // sn sin phi, go, swap}; go = 0 when |c| < tol sqrt(a b); swap = 1 when the rotated q
 // column is the longer one, which then goes to position p (columns drift into descending
 // order of norms, as in the reference's sweeps, which shortens convergence by ~30%).
-template <typename T> __device__ void hestenes(T a, T b, T cr, T ci, T tol, T *rot, unsigned *cnt)
+// nrm: the squared norms of the two rotated columns, a - t|c| and b + t|c| (in p, q order
+// before the swap), or a and b when nothing is rotated.
+template <typename T> __device__ void hestenes(T a, T b, T cr, T ci, T tol, T *rot, unsigned *cnt, T *nrm)
 {
   const T ac = hypot(cr, ci);
   T cs = 1, snr = 0, sni = 0, go = 0, sw = 0;
+  nrm[0] = a;
+  nrm[1] = b;
   if (ac > (T)0 && ac >= tol * sqrt(a) * sqrt(b)) {
     const T zeta = (b - a) / ((T)2 * ac);
     const T az = fabs(zeta);
@@ -116,6 +120,8 @@ template <typename T> __device__ void hestenes(T a, T b, T cr, T ci, T tol, T *r
     sni = sn * (ci / ac);
     go = 1;
     sw = (b + t * ac > a - t * ac) ? (T)1 : (T)0;
+    nrm[0] = a - t * ac;
+    nrm[1] = b + t * ac;
     atomicAdd(cnt, 1u);
     // the largest |cos| of the rotated pairs of this sweep (non-negative floats order as
     // their bit patterns)
@@ -291,14 +297,42 @@ __device__ void rot_cols(int rows, T *xr, T *xi, T *yr, T *yi, const Rot<T> &c)
     rot_cols_<T, CPLX, false>(rows, xr, xi, yr, yi, c);
 }
 
-// the pair's rotation from its (stored) Gram entries, by thread 0 into *rs: the entries are
-// scaled by the column scales first, if there are any
+// Squared column norms tracked through an FP64 sweep (nrm[j], or -1 when unknown): after
+// the rotation that makes a pair orthogonal its squared norms are a - t|c| and b + t|c|,
+// so a step needs only the inner product c -- 4 FP64 FMAs per complex row of G instead of
+// 8 (1 instead of 3 per real row). Each rotation adds a rounding of about one unit to a
+// tracked norm (its columns' new entries are rounded once or twice), so over a sweep of
+// n - 1 steps they stay within ~sqrt(n) units; every sweep starts from unknown norms
+// (the first step of each column computes them). The rotation angle depends on b - a, so a
+// pair whose tracked norms are within 1e-6 (relative) of each other computes them, and a
+// norm that fell below half its old value (cancellation in a - t|c|) becomes unknown.
+constexpr double NORM_NEAR = 1e-6;
+// by every thread before the dot products (the same two words for the whole CTA, so no
+// barrier is needed): the pair's tracked norms in nab, or -1 when the step must compute them
+template <typename T> __device__ __forceinline__ void tracked_norms(const T *nrm, unsigned p, unsigned q, T *nab)
+{
+  nab[0] = nab[1] = (T)-1;
+  if (!has_scales<T>() || !nrm)
+    return;
+  const T na = nrm[p], nb = nrm[q];
+  if (na >= (T)0 && nb >= (T)0 && fabs(nb - na) >= (T)NORM_NEAR * (na + nb)) {
+    nab[0] = na;
+    nab[1] = nb;
+  }
+}
+
+// the pair's rotation from its (stored) Gram entries, by thread 0 into *rs: with column
+// scales the entries are scaled first; with tracked norms (nab[0] >= 0) a and b are those
+// norms, and the new norms go back to nrm
 template <typename T>
-__device__ void pair_rotation(T a, T b, T cr, T ci, T tol, unsigned *cnt, T *dsc, unsigned p, unsigned q, Rot<T> *rs)
+__device__ void pair_rotation(T a, T b, T cr, T ci, T tol, unsigned *cnt, T *dsc, unsigned p, unsigned q, Rot<T> *rs,
+                              T *nrm, const T *nab)
 {
   T dp = 1, dq = 1;
-  if (!has_scales<T>())
+  if (!has_scales<T>()) {
     dsc = nullptr;
+    nrm = nullptr;
+  }
   if (dsc) {
     dp = dsc[p];
     dq = dsc[q];
@@ -307,20 +341,53 @@ __device__ void pair_rotation(T a, T b, T cr, T ci, T tol, unsigned *cnt, T *dsc
     cr *= dp * dq;
     ci *= dp * dq;
   }
-  T h[5];
-  hestenes(a, b, cr, ci, tol, h, cnt);
+  if (nrm && nab[0] >= (T)0) {
+    a = nab[0];
+    b = nab[1];
+  }
+  T h[5], nn[2];
+  hestenes(a, b, cr, ci, tol, h, cnt, nn);
   *rs = pair_rot(h, dp, dq, dsc, p, q);
+  if (nrm) {
+    const T np = (nn[0] >= (T)0.5 * a) ? nn[0] : (T)-1, nq = (nn[1] >= (T)0.5 * b) ? nn[1] : (T)-1;
+    const bool sw = h[4] != (T)0;
+    nrm[p] = sw ? nq : np;
+    nrm[q] = sw ? np : nq;
+  }
 }
 
 // One pivot step of one-sided Jacobi (Hestenes) with plain dot products, FP32 or FP64, on
 // planar G (m x n) and W (n x n): CTA k takes pair (p, q) = row st of the pivot table,
 // forms a = |g_p|^2, b = |g_q|^2, c = g_p^H g_q (per-thread partial sums and a block
 // tree) and rotates columns p and q of G and W (hestenes above). Any m; G is read twice.
-// dsc: the column scales of the FP64 sweeps (Rot above), or nullptr.
+// dsc, nrm: the column scales and tracked norms of the FP64 sweeps (above), or nullptr.
+template <typename T, bool CPLX, bool NORMS>
+__device__ __forceinline__ void pair_dots(int m, const T *gpr, const T *gqr, const T *gpi, const T *gqi, T &a, T &b,
+                                          T &cr, T &ci)
+{
+  for (int i = threadIdx.x; i < m; i += blockDim.x) {
+    const T xr = gpr[i], yr = gqr[i];
+    if (NORMS) {
+      a = fma(xr, xr, a);
+      b = fma(yr, yr, b);
+    }
+    cr = fma(xr, yr, cr);
+    if (CPLX) {
+      const T xi = gpi[i], yi = gqi[i];
+      if (NORMS) {
+        a = fma(xi, xi, a);
+        b = fma(yi, yi, b);
+      }
+      cr = fma(xi, yi, cr);
+      ci = fma(xr, yi, ci);
+      ci = fma(-xi, yr, ci);
+    }
+  }
+}
 template <typename T, bool CPLX>
 __global__ void __launch_bounds__(256) k_presweep(int m, int n, T *Gr, long long ldr, T *Gi, long long ldi, T *Wr,
                                                   long long lwr, T *Wi, long long lwi, const unsigned *js, int st,
-                                                  T tol, unsigned *cnt, T *dsc)
+                                                  T tol, unsigned *cnt, T *dsc, T *nrm)
 {
   __shared__ T red[4][16];
   __shared__ Rot<T> rs;
@@ -329,24 +396,17 @@ __global__ void __launch_bounds__(256) k_presweep(int m, int n, T *Gr, long long
   const unsigned p = js[(size_t)st * n + 2 * k], q = js[(size_t)st * n + 2 * k + 1];
   T *gpr = Gr + (size_t)p * ldr, *gqr = Gr + (size_t)q * ldr;
   T *gpi = CPLX ? Gi + (size_t)p * ldi : nullptr, *gqi = CPLX ? Gi + (size_t)q * ldi : nullptr;
+  T nab[2];
+  tracked_norms(nrm, p, q, nab);
+  const bool norms = nab[0] < (T)0;
   T a = 0, b = 0, cr = 0, ci = 0;
-  for (int i = threadIdx.x; i < m; i += blockDim.x) {
-    const T xr = gpr[i], yr = gqr[i];
-    a = fma(xr, xr, a);
-    b = fma(yr, yr, b);
-    cr = fma(xr, yr, cr);
-    if (CPLX) {
-      const T xi = gpi[i], yi = gqi[i];
-      a = fma(xi, xi, a);
-      b = fma(yi, yi, b);
-      cr = fma(xi, yi, cr);
-      ci = fma(xr, yi, ci);
-      ci = fma(-xi, yr, ci);
-    }
-  }
+  if (norms)
+    pair_dots<T, CPLX, true>(m, gpr, gqr, gpi, gqi, a, b, cr, ci);
+  else
+    pair_dots<T, CPLX, false>(m, gpr, gqr, gpi, gqi, a, b, cr, ci);
   block_sum4(a, b, cr, ci, red);
   if (threadIdx.x == 0)
-    pair_rotation(a, b, cr, ci, tol, cnt, dsc, p, q, &rs);
+    pair_rotation(a, b, cr, ci, tol, cnt, dsc, p, q, &rs, nrm, nab);
   __syncthreads();
   const Rot<T> c = rs;
   if (!c.go)
@@ -354,6 +414,36 @@ __global__ void __launch_bounds__(256) k_presweep(int m, int n, T *Gr, long long
   rot_cols<T, CPLX>(m, gpr, gpi, gqr, gqi, c);
   rot_cols<T, CPLX>(n, Wr + (size_t)p * lwr, CPLX ? Wi + (size_t)p * lwi : nullptr, Wr + (size_t)q * lwr,
                     CPLX ? Wi + (size_t)q * lwi : nullptr, c);
+}
+
+// the dot products of the register-resident column vectors of k_presweep_reg
+template <typename T, bool CPLX, int R, bool NORMS, typename V>
+__device__ __forceinline__ void reg_dots(const V (&xr)[R], const V (&yr)[R], const V (&xi)[R], const V (&yi)[R], T &a,
+                                         T &b, T &cr, T &ci)
+{
+  constexpr int E = vec16<T>::E;
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    const T *X = reinterpret_cast<const T *>(&xr[r]), *Y = reinterpret_cast<const T *>(&yr[r]);
+    const T *Xi = reinterpret_cast<const T *>(&xi[r]), *Yi = reinterpret_cast<const T *>(&yi[r]);
+#pragma unroll
+    for (int e = 0; e < E; ++e) {
+      if (NORMS) {
+        a = fma(X[e], X[e], a);
+        b = fma(Y[e], Y[e], b);
+      }
+      cr = fma(X[e], Y[e], cr);
+      if (CPLX) {
+        if (NORMS) {
+          a = fma(Xi[e], Xi[e], a);
+          b = fma(Yi[e], Yi[e], b);
+        }
+        cr = fma(Xi[e], Yi[e], cr);
+        ci = fma(X[e], Yi[e], ci);
+        ci = fma(-Xi[e], Y[e], ci);
+      }
+    }
+  }
 }
 
 // the rotation of the register-resident column vectors of k_presweep_reg, written back
@@ -386,14 +476,23 @@ __device__ __forceinline__ void rot_regs(V (&xr)[R], V (&yr)[R], V (&xi)[R], V (
   }
 }
 
+// resident CTAs per SM the FP64 register kernels are compiled for: a pivot step of a
+// 1024-column matrix is 512 CTAs, one wave on 152 SMs at 4 per SM and two at 3 (at
+// 1024 x 1024 real the FP64 sweeps took 61 ms with 4 per SM, 80 ms with 3); 0 (the FP32
+// kernels) leaves the compiler's own register choice, as a bound without a minimum does
+template <typename T, bool CPLX, int R, int NT> __host__ __device__ constexpr int presweep_min_ctas()
+{
+  return (sizeof(T) == 8 && NT == 256) ? ((CPLX && R == 2) ? 3 : 4) : 0;
+}
+
 // The same step with the two columns of G held in registers between the dot products and
 // the rotation (one read and one write of G): thread t of NT owns the 16-byte vectors
 // t + NT r, r < R, of each column, so m <= NT R E (E = 4 floats or 2 doubles per vector);
 // m % E == 0 and 16-byte aligned columns.
 template <typename T, bool CPLX, int R, int NT>
-__global__ void __launch_bounds__(NT) k_presweep_reg(int m, int n, T *Gr, long long ldr, T *Gi, long long ldi,
+__global__ void __launch_bounds__(NT, presweep_min_ctas<T, CPLX, R, NT>()) k_presweep_reg(int m, int n, T *Gr, long long ldr, T *Gi, long long ldi,
                                                       T *Wr, long long lwr, T *Wi, long long lwi, const unsigned *js,
-                                                      int st, T tol, unsigned *cnt, T *dsc)
+                                                      int st, T tol, unsigned *cnt, T *dsc, T *nrm)
 {
   using V = typename vec16<T>::V;
   constexpr int E = vec16<T>::E;
@@ -423,27 +522,17 @@ __global__ void __launch_bounds__(NT) k_presweep_reg(int m, int n, T *Gr, long l
       yi[r] = (i < mv) ? gqi[i] : z;
     }
   }
-#pragma unroll
-  for (int r = 0; r < R; ++r) {
-    const T *X = reinterpret_cast<const T *>(&xr[r]), *Y = reinterpret_cast<const T *>(&yr[r]);
-    const T *Xi = reinterpret_cast<const T *>(&xi[r]), *Yi = reinterpret_cast<const T *>(&yi[r]);
-#pragma unroll
-    for (int e = 0; e < E; ++e) {
-      a = fma(X[e], X[e], a);
-      b = fma(Y[e], Y[e], b);
-      cr = fma(X[e], Y[e], cr);
-      if (CPLX) {
-        a = fma(Xi[e], Xi[e], a);
-        b = fma(Yi[e], Yi[e], b);
-        cr = fma(Xi[e], Yi[e], cr);
-        ci = fma(X[e], Yi[e], ci);
-        ci = fma(-Xi[e], Y[e], ci);
-      }
-    }
-  }
+  // (the tracked norms are read after the column loads were issued: their latencies overlap)
+  T nab[2];
+  tracked_norms(nrm, p, q, nab);
+  const bool norms = nab[0] < (T)0;
+  if (norms)
+    reg_dots<T, CPLX, R, true>(xr, yr, xi, yi, a, b, cr, ci);
+  else
+    reg_dots<T, CPLX, R, false>(xr, yr, xi, yi, a, b, cr, ci);
   block_sum4(a, b, cr, ci, red);
   if (threadIdx.x == 0)
-    pair_rotation(a, b, cr, ci, tol, cnt, dsc, p, q, &rs);
+    pair_rotation(a, b, cr, ci, tol, cnt, dsc, p, q, &rs, nrm, nab);
   __syncthreads();
   const Rot<T> c = rs;
   if (!c.go)
@@ -495,11 +584,12 @@ __global__ void k_apply_scales(int m, int n, T *Gr, long long ldr, T *Gi, long l
 
 // one sweep of presweep steps (stp launches); returns the number of rotations or < 0, and
 // in *mu the largest |cos| of a rotated pair. With dsc (n entries of scratch) the columns
-// carry scales during the sweep (Rot above), multiplied into G and W at its end.
+// carry scales during the sweep (Rot above), multiplied into G and W at its end; with nrm
+// (n entries) the squared column norms are tracked through the sweep (tracked_norms).
 template <typename T, bool CPLX>
 static long long presweep(int m, int n, T *Gr, long long ldr, T *Gi, long long ldi, T *Wr, long long lwr, T *Wi,
                           long long lwi, const unsigned *js, unsigned stp, T tol, unsigned *cnt, cudaStream_t s,
-                          float *mu, T *dsc = nullptr)
+                          float *mu, T *dsc = nullptr, T *nrm = nullptr)
 {
   constexpr int E = vec16<T>::E;
   const bool al = !(m % E) && !((ldr * (long long)sizeof(T)) % 16) && !((uintptr_t)Gr % 16) &&
@@ -508,10 +598,12 @@ static long long presweep(int m, int n, T *Gr, long long ldr, T *Gi, long long l
     return -1;
   if (dsc)
     k_fill<T><<<(n + 255) / 256, 256, 0, s>>>(dsc, n, (T)1);
+  if (nrm)
+    k_fill<T><<<(n + 255) / 256, 256, 0, s>>>(nrm, n, (T)-1);
   const unsigned nb = (unsigned)(n / 2);
   const long long cap = 256LL * E;  // rows per register vector slot
   void (*k)(int, int, T *, long long, T *, long long, T *, long long, T *, long long, const unsigned *, int, T,
-            unsigned *, T *) = k_presweep<T, CPLX>;
+            unsigned *, T *, T *) = k_presweep<T, CPLX>;
   int nt = 256;
   // register-resident columns: up to 2 vectors per thread and plane with 256 threads, then
   // (FP32) 2 vectors with 512 threads; beyond that the FP64 kernel's register use would
@@ -527,7 +619,7 @@ static long long presweep(int m, int n, T *Gr, long long ldr, T *Gi, long long l
   }
   for (unsigned st = 0; st < stp; ++st)
     if (host::launch_pdl(k, dim3(nb), dim3(nt), 0, s, m, n, Gr, ldr, Gi, ldi, Wr, lwr, Wi, lwi, js, (int)st, tol,
-                         cnt, dsc) != cudaSuccess)
+                         cnt, dsc, nrm) != cudaSuccess)
       return -1;
   if (dsc)
     k_apply_scales<T, CPLX><<<grid2(m + n, n), 256, 0, s>>>(m, n, Gr, ldr, Gi, ldi, Wr, lwr, Wi, lwi, dsc);
@@ -1035,9 +1127,9 @@ static vj_fint mixed_dev(vj_fnat m_, vj_fnat n_, double *G, vj_fnat ldG, double 
   }
   // 5. FP64 sweeps with plain dot products on G and V themselves until no pair reaches half
   //    the reference's tolerance sqrt(m) eps / 2 (at most 20 sweeps): they take the columns from
-  //    FP32 to FP64 orthogonality at a fraction of a reference sweep's cost (8 FP64
-  //    operations per complex element of G for the dot products and 8 for the rotation in
-  //    the short form of Rot, instead of 68), so the reference's sweeps below
+  //    FP32 to FP64 orthogonality at a fraction of a reference sweep's cost (4 FP64
+  //    operations per complex element of G for the inner product with tracked norms and 8
+  //    for the rotation in the short form of Rot, instead of 68), so the reference's sweeps below
   //    have at most the last rotations to do and the convergence to confirm.
   if (total32) {
     // half the reference's tolerance: the plain dot product's rounding (a few eps) stays
@@ -1050,10 +1142,10 @@ static vj_fint mixed_dev(vj_fnat m_, vj_fnat n_, double *G, vj_fnat ldG, double 
     // confirming sweep is skipped, the reference's sweep below confirms.
     for (; sw64 < maxsw64; ++sw64) {
       float mu = 0.f;
-      // (column scales in Y, free scratch until the sort below)
+      // (column scales and tracked norms in Y, free scratch until the sort below)
       const long long hc = presweep<double, CPLX>(mi, ni, G, (long long)ldG, Gi, (long long)(CPLX ? ldGi : ldG), V,
                                                   (long long)ldV, Vi, (long long)(CPLX ? ldVi : ldV), js, stp, tol64,
-                                                  cnt, s, &mu, Y);
+                                                  cnt, s, &mu, Y, Y + n);
       if (hc < 0)
         return VJ_ERR_CUDA;
       if (trace)
