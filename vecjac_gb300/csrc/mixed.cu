@@ -297,6 +297,57 @@ __device__ void rot_cols(int rows, T *xr, T *xi, T *yr, T *yi, const Rot<T> &c)
     rot_cols_<T, CPLX, false>(rows, xr, xi, yr, yi, c);
 }
 
+// The same for the register kernels, U rows per thread loaded before any is stored: a
+// store may alias a later load as far as the compiler knows, so the loop above waits for one
+// memory round trip per row of the thread, which is most of a step at the small sizes the
+// register kernels serve (U = 4 real / 2 complex: 1024 x 1024 real FP32 sweeps 92 -> 80 ms).
+template <typename T, bool CPLX, bool SHRT, int U>
+__device__ void rot_cols_batched_(int rows, T *xr, T *xi, T *yr, T *yi, const Rot<T> &c)
+{
+  T *dxr = c.swap ? yr : xr, *dxi = c.swap ? yi : xi, *dyr = c.swap ? xr : yr, *dyi = c.swap ? xi : yi;
+  Rot<T> k = c;
+  k.shrt = SHRT;
+  unscaled_form(k);
+  const int nt = (int)blockDim.x;
+  for (int i0 = threadIdx.x; i0 < rows; i0 += U * nt) {
+    T pr[U], qr[U], pi[U], qi[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int i = i0 + u * nt;
+      pr[u] = qr[u] = pi[u] = qi[u] = (T)0;
+      if (i < rows) {
+        pr[u] = xr[i];
+        qr[u] = yr[i];
+        if (CPLX) {
+          pi[u] = xi[i];
+          qi[u] = yi[i];
+        }
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int i = i0 + u * nt;
+      if (i < rows) {
+        rot_elem<T, CPLX>(k, pr[u], pi[u], qr[u], qi[u]);
+        dxr[i] = pr[u];
+        dyr[i] = qr[u];
+        if (CPLX) {
+          dxi[i] = pi[u];
+          dyi[i] = qi[u];
+        }
+      }
+    }
+  }
+}
+template <typename T, bool CPLX, int U>
+__device__ void rot_cols_batched(int rows, T *xr, T *xi, T *yr, T *yi, const Rot<T> &c)
+{
+  if (has_scales<T>() && c.shrt)
+    rot_cols_batched_<T, CPLX, true, U>(rows, xr, xi, yr, yi, c);
+  else
+    rot_cols_batched_<T, CPLX, false, U>(rows, xr, xi, yr, yi, c);
+}
+
 // Squared column norms tracked through an FP64 sweep (nrm[j], or -1 when unknown): after
 // the rotation that makes a pair orthogonal its squared norms are a - t|c| and b + t|c|,
 // so a step needs only the inner product c -- 4 FP64 FMAs per complex row of G instead of
@@ -489,11 +540,15 @@ template <typename T, bool CPLX, int R, int NT> __host__ __device__ constexpr in
 // the rotation (one read and one write of G): thread t of NT owns the 16-byte vectors
 // t + NT r, r < R, of each column, so m <= NT R E (E = 4 floats or 2 doubles per vector);
 // m % E == 0 and 16-byte aligned columns.
-template <typename T, bool CPLX, int R, int NT>
+// PW: W's two columns are loaded as 16-byte vectors with G's at the start, and rotated from
+// registers (real FP32 data with 16-byte aligned columns of W); otherwise they are read
+// after the rotation is known.
+template <typename T, bool CPLX, int R, int NT, bool PW = false>
 __global__ void __launch_bounds__(NT, presweep_min_ctas<T, CPLX, R, NT>()) k_presweep_reg(int m, int n, T *Gr, long long ldr, T *Gi, long long ldi,
                                                       T *Wr, long long lwr, T *Wi, long long lwi, const unsigned *js,
                                                       int st, T tol, unsigned *cnt, T *dsc, T *nrm)
 {
+  static_assert(!PW || (!CPLX && sizeof(T) == 4), "W prefetch: real FP32 data");
   using V = typename vec16<T>::V;
   constexpr int E = vec16<T>::E;
   __shared__ T red[4][16];
@@ -522,6 +577,23 @@ __global__ void __launch_bounds__(NT, presweep_min_ctas<T, CPLX, R, NT>()) k_pre
       yi[r] = (i < mv) ? gqi[i] : z;
     }
   }
+  // W's columns (n <= m rows, so R vectors per thread cover them)
+  const int nv = n / E;
+  V *wpr = reinterpret_cast<V *>(Wr + (size_t)p * lwr), *wqr = reinterpret_cast<V *>(Wr + (size_t)q * lwr);
+  V wp[PW ? R : 1], wq[PW ? R : 1];
+  if constexpr (PW) {
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      const int i = threadIdx.x + r * NT;
+      V z;
+      T *zz = reinterpret_cast<T *>(&z);
+#pragma unroll
+      for (int e = 0; e < E; ++e)
+        zz[e] = 0;
+      wp[r] = (i < nv) ? wpr[i] : z;
+      wq[r] = (i < nv) ? wqr[i] : z;
+    }
+  }
   // (the tracked norms are read after the column loads were issued: their latencies overlap)
   T nab[2];
   tracked_norms(nrm, p, q, nab);
@@ -541,8 +613,11 @@ __global__ void __launch_bounds__(NT, presweep_min_ctas<T, CPLX, R, NT>()) k_pre
     rot_regs<T, CPLX, R, NT, true>(xr, yr, xi, yi, mv, c, gpr, gqr, gpi, gqi);
   else
     rot_regs<T, CPLX, R, NT, false>(xr, yr, xi, yi, mv, c, gpr, gqr, gpi, gqi);
-  rot_cols<T, CPLX>(n, Wr + (size_t)p * lwr, CPLX ? Wi + (size_t)p * lwi : nullptr, Wr + (size_t)q * lwr,
-                    CPLX ? Wi + (size_t)q * lwi : nullptr, c);
+  if constexpr (PW)
+    rot_regs<T, CPLX, R, NT, false>(wp, wq, wp, wq, nv, c, wpr, wqr, wpr, wqr);
+  else
+    rot_cols_batched<T, CPLX, CPLX ? 2 : 4>(n, Wr + (size_t)p * lwr, CPLX ? Wi + (size_t)p * lwi : nullptr,
+                                            Wr + (size_t)q * lwr, CPLX ? Wi + (size_t)q * lwi : nullptr, c);
 }
 
 static dim3 grid2(long long rows, long long cols)
@@ -616,6 +691,16 @@ static long long presweep(int m, int n, T *Gr, long long ldr, T *Gi, long long l
   else if (al && sizeof(T) == 4 && m <= 4 * cap) {
     k = k_presweep_reg<T, CPLX, 2, 512>;
     nt = 512;
+  }
+  // real FP32 with 16-byte aligned columns of W: the variant that loads W with G
+  if constexpr (!CPLX && sizeof(T) == 4) {
+    const bool alw = !(n % E) && !((lwr * (long long)sizeof(T)) % 16) && !((uintptr_t)Wr % 16);
+    if (alw && al && m <= cap)
+      k = k_presweep_reg<T, CPLX, 1, 256, true>;
+    else if (alw && al && m <= 2 * cap)
+      k = k_presweep_reg<T, CPLX, 2, 256, true>;
+    else if (alw && al && m <= 4 * cap)
+      k = k_presweep_reg<T, CPLX, 2, 512, true>;
   }
   for (unsigned st = 0; st < stp; ++st)
     if (host::launch_pdl(k, dim3(nb), dim3(nt), 0, s, m, n, Gr, ldr, Gi, ldi, Wr, lwr, Wi, lwi, js, (int)st, tol,
