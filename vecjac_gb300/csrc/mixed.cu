@@ -14,8 +14,10 @@
 // FP32 rounding is relative to each element, so from the second stage on the FP32 sweeps
 // see the columns of G_{s-1} to their own relative accuracy and resolve the directions of
 // small singular values that the first stage (on A itself) could not. FP64 sweeps with
-// plain dot products (the same step kernel in FP64, on G and V themselves) then bring the
-// columns to FP64 orthogonality. Finally dvjsvd_/zvjsvd_'s algorithm runs on G with V as
+// plain dot products (the same step kernel in FP64, on G and V themselves, with a scale
+// factor per column so that a rotation takes two FMAs per output, and the squared column
+// norms tracked through the sweep so that a step forms only the inner product) then bring
+// the columns to FP64 orthogonality. Finally dvjsvd_/zvjsvd_'s algorithm runs on G with V as
 // the preset matrix (the reference's iwork[0] != 0 mode, src/dvjsvd.c:88-96,
 // src/zvjsvd.c:100-110): G R = U Sigma and V R = V, so A = U Sigma V^H with the FP64
 // algorithm's accuracy and convergence test; its first sweep is checked for every pair at
