@@ -237,9 +237,11 @@ vj_fint vj_svjsvd_batch_tuned_dev(vj_fint count, const long long *m, const long 
  * the control block live in a fixed 1 MiB + 512 B device array inside the library, present
  * on every GPU that loads it until the process exits. n must not exceed 512 (VJ_ERR_ARG
  * otherwise); the other arguments and the result are those of vj_dvjsvd_dev (it also
- * synchronises `stream` once per sweep; any nonzero preset acts as 1). The first call on a device looks up that array's
- * address for that device and keeps it. Every call shares the array: calls that overlap on
- * the GPU, on any stream or thread, race and must be serialised by the caller. */
+ * synchronises `stream` once per sweep; any nonzero preset acts as 1). The first call on
+ * a device looks up that array's address for that device (with the device current) and
+ * keeps it; make that first call before any stream capture begins. Every call shares the
+ * array: calls that overlap on the GPU, on any stream or thread, race and must be
+ * serialised by the caller. */
 vj_fint vj_dvjsvd_dev_noalloc(vj_fnat m, vj_fnat n, double *G, vj_fnat ldG, double *V, vj_fnat ldV, double *eS,
                               double *fS, long strategy, unsigned swp, int preset, void *stream);
 

@@ -1062,7 +1062,9 @@ constexpr size_t NOALLOC_JS = 262144;  // unsigned entries of the pivot table
 static_assert(sizeof(SvdGlobal) + 64 + 8 <= NOALLOC_CTL, "control block does not fit");
 static __device__ __align__(256) unsigned char vj_noalloc_scratch[NOALLOC_CTL + NOALLOC_JS * sizeof(unsigned)];
 
-// device address of the scratch array, looked up once per device with that device current
+// device address of the scratch array, looked up once per device with that device current:
+// the first call of vj_dvjsvd_dev_noalloc on a device does it, so that call belongs before
+// any stream capture begins
 static unsigned char *noalloc_scratch()
 {
   static std::mutex mu;

@@ -646,9 +646,10 @@ __global__ void k_apply_scales(int m, int n, T *Gr, long long ldr, T *Gi, long l
     const T d = dsc[j];
     if (d == (T)1)
       continue;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m + n; i += gridDim.x * blockDim.x) {
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < (long long)m + n;
+         i += (long long)gridDim.x * blockDim.x) {
       const bool g = i < m;
-      const int r = g ? i : i - m;
+      const long long r = g ? i : i - m;
       T *pr = g ? Gr + (size_t)j * ldr + r : Wr + (size_t)j * lwr + r;
       *pr *= d;
       if (CPLX) {
