@@ -577,7 +577,6 @@ __global__ void __launch_bounds__(EVD_THREADS) k_pair_evd(const float *Sred, int
   constexpr int PL = P / 32;           // pairs per lane
   constexpr int LD = N + 1;
   constexpr int NO = P * (P - 1) / 2;  // off-diagonal blocks u < v
-  constexpr int NW = EVD_THREADS / 32;
   extern __shared__ __align__(16) float fsm[];
   float4 *rot = reinterpret_cast<float4 *>(fsm);  // P records
   E *H = reinterpret_cast<E *>(rot + P);
@@ -596,7 +595,8 @@ __global__ void __launch_bounds__(EVD_THREADS) k_pair_evd(const float *Sred, int
       tri[u * P - u * (u + 1) / 2 + (v - u - 1)] = (unsigned short)((u << 8) | v);
   }
   float4 *lg = rlog + (size_t)blockIdx.x * sweeps * (N - 1) * P;
-  // H from S (upper triangle, mirrored: exactly Hermitian)
+  // H from S; only the upper triangle of H is stored (an entry (i, j) with i > j is the
+  // conjugate of the stored (j, i)), so that an update writes each entry once
   for (int q = tid; q < N * N; q += EVD_THREADS) {
     const int i = q / N, j = q % N;
     if (i > j)
@@ -606,13 +606,9 @@ __global__ void __launch_bounds__(EVD_THREADS) k_pair_evd(const float *Sred, int
       const float hr = S(i, j) + S(64 + i, 64 + j);
       const float hi = (i == j) ? 0.f : (S(i, 64 + j) - S(64 + i, j));
       H[i * LD + j] = make_float2(hr, hi);
-      H[j * LD + i] = make_float2(hr, -hi);
     }
-    else {
-      const float h = S(i, j);
-      H[i * LD + j] = h;
-      H[j * LD + i] = h;
-    }
+    else
+      H[i * LD + j] = S(i, j);
   }
   __syncthreads();
   auto re = [](const E &x) -> float {
@@ -620,6 +616,20 @@ __global__ void __launch_bounds__(EVD_THREADS) k_pair_evd(const float *Sred, int
       return x.x;
     else
       return x;
+  };
+  auto cj = [](const E &x) -> E {
+    if constexpr (CPLX)
+      return make_float2(x.x, -x.y);
+    else
+      return x;
+  };
+  // entry (i, j), i != j, of the Hermitian H, and its store
+  auto hget = [&](int i, int j) -> E { return (i < j) ? H[i * LD + j] : cj(H[j * LD + i]); };
+  auto hput = [&](int i, int j, const E &x) {
+    if (i < j)
+      H[i * LD + j] = x;
+    else
+      H[j * LD + i] = cj(x);
   };
   unsigned nrot = 0u;
   float mu = 0.f;
@@ -646,7 +656,7 @@ __global__ void __launch_bounds__(EVD_THREADS) k_pair_evd(const float *Sred, int
           // modulo N - 1, and so are the second ones, so that the row and column accesses of
           // the updates fall into distinct shared-memory banks)
           const int p = a, q = c;
-          const E hpq = H[p * LD + q];
+          const E hpq = hget(p, q);
           float cr, ci = 0.f;
           if constexpr (CPLX) {
             cr = hpq.x;
@@ -665,14 +675,12 @@ __global__ void __launch_bounds__(EVD_THREADS) k_pair_evd(const float *Sred, int
             if constexpr (CPLX) {
               H[p * LD + p] = make_float2(r.d1, 0.f);
               H[q * LD + q] = make_float2(r.d2, 0.f);
-              H[p * LD + q] = make_float2(0.f, 0.f);
-              H[q * LD + p] = make_float2(0.f, 0.f);
+              H[min(p, q) * LD + max(p, q)] = make_float2(0.f, 0.f);
             }
             else {
               H[p * LD + p] = r.d1;
               H[q * LD + q] = r.d2;
-              H[p * LD + q] = 0.f;
-              H[q * LD + p] = 0.f;
+              H[min(p, q) * LD + max(p, q)] = 0.f;
             }
           }
           if (r.go) {
@@ -694,7 +702,7 @@ __global__ void __launch_bounds__(EVD_THREADS) k_pair_evd(const float *Sred, int
         const float cu = ru.x, sur = ru.y, sui = ru.z;
         const float cv = rv.x, svr = rv.y, svi = rv.z;
         if constexpr (CPLX) {
-          const float2 b00 = H[pu * LD + pv], b01 = H[pu * LD + qv], b10 = H[qu * LD + pv], b11 = H[qu * LD + qv];
+          const float2 b00 = hget(pu, pv), b01 = hget(pu, qv), b10 = hget(qu, pv), b11 = hget(qu, qv);
           // C = B J_v: C[:,0] = cv B[:,0] - conj(s_v) B[:,1], C[:,1] = cv B[:,1] + s_v B[:,0]
           const float c00r = fmaf(cv, b00.x, -fmaf(svr, b01.x, svi * b01.y));
           const float c00i = fmaf(cv, b00.y, -fmaf(svr, b01.y, -(svi * b01.x)));
@@ -713,29 +721,21 @@ __global__ void __launch_bounds__(EVD_THREADS) k_pair_evd(const float *Sred, int
           const float n10i = fmaf(cu, c10i, fmaf(sur, c00i, -(sui * c00r)));
           const float n11r = fmaf(cu, c11r, fmaf(sur, c01r, sui * c01i));
           const float n11i = fmaf(cu, c11i, fmaf(sur, c01i, -(sui * c01r)));
-          H[pu * LD + pv] = make_float2(n00r, n00i);
-          H[pu * LD + qv] = make_float2(n01r, n01i);
-          H[qu * LD + pv] = make_float2(n10r, n10i);
-          H[qu * LD + qv] = make_float2(n11r, n11i);
-          H[pv * LD + pu] = make_float2(n00r, -n00i);
-          H[qv * LD + pu] = make_float2(n01r, -n01i);
-          H[pv * LD + qu] = make_float2(n10r, -n10i);
-          H[qv * LD + qu] = make_float2(n11r, -n11i);
+          hput(pu, pv, make_float2(n00r, n00i));
+          hput(pu, qv, make_float2(n01r, n01i));
+          hput(qu, pv, make_float2(n10r, n10i));
+          hput(qu, qv, make_float2(n11r, n11i));
         }
         else {
-          const float b00 = H[pu * LD + pv], b01 = H[pu * LD + qv], b10 = H[qu * LD + pv], b11 = H[qu * LD + qv];
+          const float b00 = hget(pu, pv), b01 = hget(pu, qv), b10 = hget(qu, pv), b11 = hget(qu, qv);
           const float c00 = fmaf(cv, b00, -(svr * b01)), c10 = fmaf(cv, b10, -(svr * b11));
           const float c01 = fmaf(cv, b01, svr * b00), c11 = fmaf(cv, b11, svr * b10);
           const float n00 = fmaf(cu, c00, -(sur * c10)), n01 = fmaf(cu, c01, -(sur * c11));
           const float n10 = fmaf(cu, c10, sur * c00), n11 = fmaf(cu, c11, sur * c01);
-          H[pu * LD + pv] = n00;
-          H[pu * LD + qv] = n01;
-          H[qu * LD + pv] = n10;
-          H[qu * LD + qv] = n11;
-          H[pv * LD + pu] = n00;
-          H[qv * LD + pu] = n01;
-          H[pv * LD + qu] = n10;
-          H[qv * LD + qu] = n11;
+          hput(pu, pv, n00);
+          hput(pu, qv, n01);
+          hput(qu, pv, n10);
+          hput(qu, qv, n11);
         }
       }
       __syncthreads();
