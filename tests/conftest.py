@@ -14,5 +14,11 @@ def pytest_configure(config):
 
 def pytest_collection_modifyitems(session, config, items):
     # the fast bit-exact parity tests first, the full-size workloads and the checks that
-    # depend on the host (a second GPU process, a bundled LAPACK) after them
-    items.sort(key=lambda it: 1 if it.get_closest_marker("late") else 0)
+    # depend on the host (a second GPU process, a bundled LAPACK) after them, and the
+    # test_zz_* files last of all (a run that stops at their first failure has run the rest)
+    def rank(it):
+        if os.path.basename(str(it.fspath)).startswith("test_zz_"):
+            return 2
+        return 1 if it.get_closest_marker("late") else 0
+
+    items.sort(key=rank)

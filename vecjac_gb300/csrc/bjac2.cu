@@ -159,6 +159,7 @@ static vj_fint bjac2_host(vj_fint n, int internal, const T *a11, const T *a22, c
   const long long nn = (n < 0) ? -n : n;
   if (!nn)
     return 1;
+  std::lock_guard<std::recursive_mutex> lk(host::host_call_lock());  // the device's staging buffers
   // On a GPU that reads pageable host memory coherently (Grace-Blackwell: NVLink-C2C with
   // address translation), the kernel reads the caller's inputs in place and writes its
   // outputs to device buffers, whose copies back to the caller's arrays overlap the

@@ -898,8 +898,8 @@ struct Plan {
 
 static bool attrs_set(bool cplx)
 {
-  static int done[2] = {0, 0};
-  int &d = done[cplx ? 1 : 0];
+  static int done[host::MAX_DEVICES][2] = {};  // kernel attributes are set per device
+  int &d = done[host::device_slot()][cplx ? 1 : 0];
   if (!d) {
     bool ok = cudaFuncSetAttribute(k_gram<6>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)GRAM_SMEM) ==
                   cudaSuccess &&

@@ -17,15 +17,21 @@ bool gpu_ready()
   return ok == 1;
 }
 
+int device_slot()
+{
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0)
+    dev = 0;
+  return dev & (MAX_DEVICES - 1);
+}
+
 int sm_count()
 {
   // per device: a process may drive GPUs of different sizes (grids are sized for the
   // current device of each call)
-  static int cnt[64] = {};
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0)
-    dev = 0;
-  int &n = cnt[dev & 63];
+  static int cnt[MAX_DEVICES] = {};
+  const int dev = device_slot();
+  int &n = cnt[dev];
   if (!n) {
     int v = 0;
     if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0)
@@ -49,16 +55,17 @@ bool host_pinned(const void *p)
 
 bool pageable_access()
 {
-  static int v = -1;
-  if (v < 0) {
-    int dev = 0, a = 0;
-    cudaGetDevice(&dev);
+  static int vs[MAX_DEVICES] = {};  // 0 unknown, 1 yes, 2 no
+  const int dev = device_slot();
+  int &v = vs[dev];
+  if (!v) {
+    int a = 0;
     if (cudaDeviceGetAttribute(&a, cudaDevAttrPageableMemoryAccess, dev) != cudaSuccess)
       a = 0;
     const char *e = getenv("VJ_STAGED");
     if (e && *e == '1')
       a = 0;
-    v = a ? 1 : 0;
+    v = a ? 1 : 2;
   }
   return v == 1;
 }
@@ -82,42 +89,53 @@ bool Staging::reserve(size_t bytes)
   return true;
 }
 
+// (each on the current device: one instance per device)
 Staging &staging()
 {
-  static Staging s;
-  return s;
+  static Staging s[MAX_DEVICES];
+  return s[device_slot()];
 }
 
 unsigned *batch_queue()
 {
-  static Staging q;
-  return q.reserve(256) ? reinterpret_cast<unsigned *>(q.ptr) : nullptr;
+  static Staging q[MAX_DEVICES];
+  Staging &b = q[device_slot()];
+  return b.reserve(256) ? reinterpret_cast<unsigned *>(b.ptr) : nullptr;
 }
 
 Staging &staging2()
 {
-  static Staging s;
-  return s;
+  static Staging s[MAX_DEVICES];
+  return s[device_slot()];
 }
 
 Staging &staging3()
 {
-  static Staging s;
-  return s;
+  static Staging s[MAX_DEVICES];
+  return s[device_slot()];
 }
 
 bool streams2(cudaStream_t s[2])
 {
-  static cudaStream_t st[2] = {nullptr, nullptr};
-  static bool ok = false;
-  static std::once_flag once;
-  std::call_once(once, [] {
-    ok = (cudaStreamCreateWithFlags(&st[0], cudaStreamNonBlocking) == cudaSuccess) &&
-         (cudaStreamCreateWithFlags(&st[1], cudaStreamNonBlocking) == cudaSuccess);
-  });
-  s[0] = st[0];
-  s[1] = st[1];
-  return ok;
+  static std::mutex mu;
+  static cudaStream_t st[MAX_DEVICES][2] = {};
+  static int made[MAX_DEVICES] = {};  // 0 not yet, 1 made, -1 failed
+  const int dev = device_slot();
+  std::lock_guard<std::mutex> lk(mu);
+  if (!made[dev])
+    made[dev] = ((cudaStreamCreateWithFlags(&st[dev][0], cudaStreamNonBlocking) == cudaSuccess) &&
+                 (cudaStreamCreateWithFlags(&st[dev][1], cudaStreamNonBlocking) == cudaSuccess))
+                    ? 1
+                    : -1;
+  s[0] = st[dev][0];
+  s[1] = st[dev][1];
+  return made[dev] == 1;
+}
+
+std::recursive_mutex &host_call_lock()
+{
+  static std::recursive_mutex m[MAX_DEVICES];
+  return m[device_slot()];
 }
 
 long long bjac2_chunk(long long n, size_t elem, bool cplx, int lanes)

@@ -780,7 +780,8 @@ static vj_fint svd_dev(vj_fnat m_, vj_fnat n_, T *G, vj_fnat ldG, T *Gi, vj_fnat
       // flag and list count in dmx; the list in the caller-owned V scratch is not
       // available, so it lives in its own cached device buffer (cap entries)
       unsigned *flag = reinterpret_cast<unsigned *>(dmx), *nl = flag + 1;
-      static host::Staging lst;
+      static host::Staging lsts[host::MAX_DEVICES];
+      host::Staging &lst = lsts[host::device_slot()];
       const unsigned cap = 1u << 20;
       if (!lst.reserve((size_t)cap * sizeof(unsigned)))
         return VJ_ERR_NOMEM;
@@ -900,6 +901,7 @@ static vj_fint svd_host(const vj_fnat *m, const vj_fnat *n, T *G, const vj_fnat 
   }
   if (!host::gpu_ready())
     return VJ_ERR_NO_GPU;
+  std::lock_guard<std::recursive_mutex> lk(host::host_call_lock());  // the device's staging buffers
   const int preset = (*iwork != 0u);
   cudaStream_t st2[2];
   if (!host::streams2(st2))

@@ -756,9 +756,13 @@ __global__ void k_gather_cols(int rows, int n, const double *A, long long lda, c
       B[(size_t)j * rows + i] = A[(size_t)perm[j] * lda + i];
 }
 
+// library handles, one per device (created with that device current)
 static cublasHandle_t cublas()
 {
-  static cublasHandle_t h = nullptr;
+  static std::mutex mu;
+  static cublasHandle_t hs[host::MAX_DEVICES] = {};
+  std::lock_guard<std::mutex> lk(mu);
+  cublasHandle_t &h = hs[host::device_slot()];
   if (!h && cublasCreate(&h) != CUBLAS_STATUS_SUCCESS)
     h = nullptr;
   return h;
@@ -766,7 +770,10 @@ static cublasHandle_t cublas()
 
 static cusolverDnHandle_t cusolver()
 {
-  static cusolverDnHandle_t h = nullptr;
+  static std::mutex mu;
+  static cusolverDnHandle_t hs[host::MAX_DEVICES] = {};
+  std::lock_guard<std::mutex> lk(mu);
+  cusolverDnHandle_t &h = hs[host::device_slot()];
   if (!h && cusolverDnCreate(&h) != CUSOLVER_STATUS_SUCCESS)
     h = nullptr;
   return h;
@@ -1134,7 +1141,8 @@ static vj_fint mixed_dev(vj_fnat m_, vj_fnat n_, double *G, vj_fnat ldG, double 
       if (!hs || cusolverDnSetStream(hs, s) != CUSOLVER_STATUS_SUCCESS)
         return VJ_ERR_CUDA;
       int *info = reinterpret_cast<int *>(cell);
-      static host::Staging wsp;  // the factorisation's workspace
+      static host::Staging wsps[host::MAX_DEVICES];  // the factorisation's workspace, per device
+      host::Staging &wsp = wsps[host::device_slot()];
       const double one = 1.0;
       int lw = 0, hinfo = 0;
       if (!CPLX) {

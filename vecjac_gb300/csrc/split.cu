@@ -155,6 +155,7 @@ static vj_fint convert_host(bool merge, long long m, long long n, const T *A_in,
     return VJ_ERR_NO_GPU;
   if (n <= 0 || !m)
     return 1;
+  std::lock_guard<std::recursive_mutex> lk(host::host_call_lock());  // the device's staging buffers
   const size_t colb = (size_t)m * 4 * sizeof(T);  // one column: interleaved + two planes
   long long cols = (long long)(((size_t)256 << 20) / colb);
   if (cols < 1)

@@ -1,6 +1,7 @@
 // Host-side services shared by the entry points: device discovery, a growable device
 // staging buffer for the host-pointer forms, and a pair of library-owned streams.
 #pragma once
+#include <mutex>
 #include <cfenv>
 #include <cstddef>
 #include <cuda_runtime.h>
@@ -30,6 +31,10 @@ struct NearestRounding {
 
 // true when a CUDA device is usable (checked once; the current device is used)
 bool gpu_ready();
+// Library state is kept per device (the current device of each call): SM count, staging
+// buffers, streams, the batch queue, the cuBLAS / cuSOLVER handles of the mixed SVD.
+constexpr int MAX_DEVICES = 64;
+int device_slot();
 int sm_count();
 // the device can read and write pageable host memory (and VJ_STAGED is not set)
 bool pageable_access();
@@ -52,6 +57,12 @@ unsigned *batch_queue();
 
 // two non-blocking streams owned by the library
 bool streams2(cudaStream_t s[2]);
+
+// Taken by the host-pointer entry points (dbjac2_ ... zsplit_ ...), which share the
+// device's staging buffers: calls from several host threads run one at a time on a device,
+// so those entry points are reentrant like the reference's. (Recursive: a host form may
+// call another.)
+std::recursive_mutex &host_call_lock();
 
 // launch with programmatic stream serialisation (the kernel calls pdl_enter first)
 template <typename... KArgs, typename... Args>
