@@ -409,11 +409,7 @@ __device__ void pair_rotation(T a, T b, T cr, T ci, T tol, unsigned *cnt, T *dsc
   }
 }
 
-// One pivot step of one-sided Jacobi (Hestenes) with plain dot products, FP32 or FP64, on
-// planar G (m x n) and W (n x n): CTA k takes pair (p, q) = row st of the pivot table,
-// forms a = |g_p|^2, b = |g_q|^2, c = g_p^H g_q (per-thread partial sums and a block
-// tree) and rotates columns p and q of G and W (hestenes above). Any m; G is read twice.
-// dsc, nrm: the column scales and tracked norms of the FP64 sweeps (above), or nullptr.
+// this thread's share of c = g_p^H g_q and, with NORMS, of |g_p|^2 and |g_q|^2
 template <typename T, bool CPLX, bool NORMS>
 __device__ __forceinline__ void pair_dots(int m, const T *gpr, const T *gqr, const T *gpi, const T *gqi, T &a, T &b,
                                           T &cr, T &ci)
@@ -437,6 +433,11 @@ __device__ __forceinline__ void pair_dots(int m, const T *gpr, const T *gqr, con
     }
   }
 }
+// One pivot step of one-sided Jacobi (Hestenes) with plain dot products, FP32 or FP64, on
+// planar G (m x n) and W (n x n): CTA k takes pair (p, q) = row st of the pivot table,
+// forms a = |g_p|^2, b = |g_q|^2, c = g_p^H g_q (per-thread partial sums and a block
+// tree) and rotates columns p and q of G and W (hestenes above). Any m; G is read twice.
+// dsc, nrm: the column scales and tracked norms of the FP64 sweeps (above), or nullptr.
 template <typename T, bool CPLX>
 __global__ void __launch_bounds__(256) k_presweep(int m, int n, T *Gr, long long ldr, T *Gi, long long ldi, T *Wr,
                                                   long long lwr, T *Wi, long long lwi, const unsigned *js, int st,
