@@ -177,7 +177,7 @@ vj_fint vj_block_apply_dev(int cplx, vj_fnat m, vj_fnat n, float *Gr, float *Gi,
 vj_fint vj_block_sweep_dev(int cplx, vj_fnat m, vj_fnat n, float *Gr, float *Gi, vj_fnat ldG, float *Wr, float *Wi,
                            vj_fnat ldW, float tol, int inner, int terms, float *mu, void *stream);
 
-/* Phase times of the last vj_?vjsvd_mixed_dev call on this process, in milliseconds:
+/* Phase times of the calling thread's last vj_?vjsvd_mixed_dev call, in milliseconds:
  * out[0] FP32 sweeps, out[1] orthonormalisation of W and the GEMMs, out[2] plain-dot FP64 sweeps
  * and the column sort, out[3] the reference's finishing sweeps; out[4] the number of FP32
  * kernel launches; out[5] 1 when the FP32 stages ran as block sweeps on the tensor cores,
@@ -287,8 +287,9 @@ unsigned *pjs(long id, unsigned n, unsigned stp[1]);
 vj_fint vj_pjs_dev(long id, unsigned n, unsigned *table, void *stream);
 
 /* ---------------- library ---------------- */
-/* Statistics of the last host-API SVD call, the counterpart of the reference's JTRACE
- * log (src/dvjsvd.c:596,635): transformed pairs per sweep (first 64 sweeps) and, when
+/* Statistics of the calling thread's last host-API SVD call, the counterpart of the
+ * reference's JTRACE log (src/dvjsvd.c:596,635): transformed pairs per sweep (first 64
+ * sweeps) and, when
  * VJ_TRACE=1 is set in the environment, SM cycles spent by one CTA in each phase of the
  * pivot steps: 0 control/rescaling, 1 staging, 2 dot products, 3 2x2 and classification,
  * 4 rotations, 5 norms. */

@@ -151,7 +151,8 @@ long long bjac2_chunk(long long n, size_t elem, bool cplx, int lanes)
   return c;
 }
 
-static vj_trace g_trace;
+// the calling thread's last call (each host thread keeps its own record)
+static thread_local vj_trace g_trace;
 
 void trace_reset()
 {
@@ -177,7 +178,7 @@ void trace_sweep(unsigned sweep, unsigned long long rotations)
   g_trace.sweeps = sweep + 1;
 }
 
-static double g_mixed[6];
+static thread_local double g_mixed[6];
 
 void mixed_phases_set(double fp32, double gemm, double fp64, double fin, double fp32_steps, double block)
 {
